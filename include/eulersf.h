@@ -1,0 +1,238 @@
+/*
+ * eulersf.h - C ABI of the GB300 implementation of EULERSF's coupled
+ * solid-fluid step (yunteng/EULERSF).
+ *
+ * The reference has no FFI: the step sits behind C++ class call surfaces.
+ * Each entry point below replaces one of them; the citation names the
+ * reference interface it stands in for. All host pointers are plain C
+ * arrays; all "device" pointers are CUDA global-memory addresses. No entry
+ * point exits, traps or throws: every failure is an esf_status.
+ *
+ * Grid and indexing follow the reference: node (x, y, z) has index
+ * x + y*xRes + z*xRes*yRes (include/geometry/FIELD_3D.h:72); pressure row
+ * (cell) c has index x + y*(xRes-1) + z*(xRes-1)*(yRes-1)
+ * (COUPLED_INTEGRATOR_3D.cpp:302-306); velocity unknown 3*k+d belongs to the
+ * k-th interior node in z, y, x order (COUPLED_INTEGRATOR_3D.cpp:123-131).
+ */
+#ifndef EULERSF_H
+#define EULERSF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ESF_ABI_VERSION 1
+#define ESF_MAX_SOLIDS 8
+
+typedef enum esf_status {
+  ESF_OK = 0,
+  ESF_ERR_INVALID_ARG = 1,   /* bad pointer, size or enum */
+  ESF_ERR_STATE = 2,         /* call out of order (e.g. step before init) */
+  ESF_ERR_CUDA = 3,          /* a CUDA runtime call failed; see esf_last_error */
+  ESF_ERR_OOM = 4,           /* device allocation failed */
+  ESF_ERR_IO = 5,            /* config / frame file could not be read or written */
+  ESF_ERR_NUMERIC = 6,       /* NaN/Inf met in a solve (the step still returns) */
+  ESF_ERR_NO_DEVICE = 7,     /* no CUDA device visible */
+  ESF_ERR_UNSUPPORTED = 8
+} esf_status;
+
+typedef enum esf_precision {
+  ESF_FP64 = 0,   /* plain method: everything in FP64 */
+  ESF_MIXED = 1   /* FP32 inner solves inside FP64 iterative refinement */
+} esf_precision;
+
+/* Grid of the coupled integrator: COUPLED_INTEGRATOR_3D(int xRes, int yRes,
+ * int zRes, Real dh, VEC3F origin) (COUPLED_INTEGRATOR_3D.h:31). */
+typedef struct esf_grid {
+  int xRes, yRes, zRes;
+  double dh;
+  double origin[3];
+} esf_grid;
+
+/* Every config key the step reads (SIMPLE_PARSER keys, name in quotes).
+ * esf_params_default() fills the reference's own defaults. */
+typedef struct esf_params {
+  double dt;                       /* "dt" (0.01 in the integrator ctor) */
+  double fluid_density;            /* "fluid density" (1) */
+  double fluid_viscosity;          /* "fluid viscocity" (stored, unused) */
+  double vorticity_eps;            /* "vorticity eps" (2.0), raw cfg value */
+  double buoyancy;                 /* "buoyancy" (0.1) */
+  double gravity;                  /* "gravity" (0) */
+  double rayleigh_alpha;           /* "rayleigh alpha" (0) */
+  double rayleigh_beta;            /* "rayleigh beta" (0) */
+  double implicit_solver_eps;      /* "implicit solver eps" (1e-8) */
+  double div_free_solver_eps;      /* "div free solver eps" (1e-8) */
+  int cr_max_iterations;           /* "cr max iterations" (10) */
+  double mass_sample_dh;           /* "mass sample dh" (dh/10) */
+  int tight_border;                /* "tight border" (3) */
+  int extrapolation_cells;         /* "extrapolation cells" (20) */
+  int particles_per_cell;          /* "number of particles per material cell" (8) */
+  double flip_alpha;               /* "flip alpha" (0.95) */
+  double contact_safe_distance;    /* "contact safe distance" (dh/2) */
+  double wall_thickness;           /* "wall thickness" (1.5 dh) */
+  double contact_spring_stiffness; /* "contact spring stiffness" (10000) */
+  double friction;                 /* "friction" (0.5) */
+  int flip_cutoff;                 /* "flip cutoff" (3) */
+  double flow_rate;                /* "flow rate" (0); plasticity only */
+  /* GB300 additions (no reference key) */
+  int precision;                   /* esf_precision */
+  double inner_eps;                /* mixed: FP32 inner relative tolerance (1e-4) */
+  int max_refinements;             /* mixed: outer FP64 refinement cap (50) */
+} esf_params;
+
+/* One elastic solid: DEFOR_SOLID_3D(xRes, yRes, zRes, dh, origin, restMass)
+ * + setMaterial + setMassDensity + setInitialState + setInitialVelocity +
+ * loadSurfaceMesh (DEFOR_SOLID_3D.h:43-71; main.cpp:99-160). The mesh is
+ * given in its rest pose (as loaded from the OBJ); scaling, rotation and
+ * translation are applied as main.cpp:150-154 does. */
+typedef struct esf_solid_desc {
+  int mass_res[3];            /* rest-pose mass grid (FIELD_3Df "<mesh>.mass") */
+  double mass_dh;
+  double mass_origin[3];
+  const double* rest_mass;    /* mass_res[0]*mass_res[1]*mass_res[2], x fastest */
+  double lambda, mu;          /* "material lambda/mu i" */
+  double density;             /* "solid mass density i" */
+  double rotation[9];         /* row-major 3x3 */
+  double translation[3];      /* "solid translation i" */
+  double scaling[3];          /* "solid scaling i" */
+  double initial_velocity[3]; /* "solid initial velocity i" */
+  int num_vertices;
+  const double* vertices;     /* num_vertices x 3, rest pose */
+  int num_triangles;
+  const int* triangles;       /* num_triangles x 3, 0-based */
+} esf_solid_desc;
+
+/* What one stepImplicit() call did (COUPLED_INTEGRATOR_3D.cpp:377-636). */
+typedef struct esf_step_report {
+  double dt;                  /* time step taken (CFL-limited) */
+  double energy;              /* kinetic + potential + strain (return value) */
+  int iterations[3];          /* solid solve 1, pressure solve, solid solve 2 */
+  int converged[3];
+  double rel_residual[3];     /* ||Ax-b|| / ||b|| at exit */
+  int refinements[3];         /* mixed: outer FP64 refinement steps per solve */
+  int prone_to_contact;       /* CFL factor 0.6 instead of 1.8 */
+  int num_particles;
+  int status;                 /* esf_status of the step */
+  double device_ms;           /* device time of the step (CUDA events) */
+} esf_step_report;
+
+/* Field identifiers for esf_get_field / esf_set_field / esf_field_info. */
+typedef enum esf_field {
+  /* integrator, per node (xRes*yRes*zRes entries) */
+  ESF_F_VELOCITY = 0,          /* f64 x3 _velocity */
+  ESF_F_INTENSITY = 1,         /* f64 _intensity */
+  ESF_F_SOLID_MASS = 2,        /* f64 _solidMass */
+  ESF_F_NODE_SOLID_VF = 3,     /* f64 _nodeSolidVolumeFraction */
+  ESF_F_DOF_MAP = 4,           /* i32 _gridIdxToSolutionIdx */
+  ESF_F_SOLID_DOF_MAP = 5,     /* i32 _gridIdxToSolidIdx */
+  /* integrator, per pressure row (cells) */
+  ESF_F_PRESSURE = 10,         /* f64 lambda1 (warm-started pressure) */
+  ESF_F_JMINVJT_DIAG = 11,     /* f64 _JMInvJTDiag */
+  ESF_F_DIV_RHS = 12,          /* f64 _divergenceConstraintsRHS */
+  ESF_F_B1 = 13,               /* f64 J v* - rhs */
+  /* integrator, per velocity unknown (3 * interior nodes) */
+  ESF_F_NZ_MASS_INV = 20,      /* f64 _nzMassVecInv */
+  ESF_F_VELOCITY_DT0 = 21,     /* f64 _velocityAtDt0 (v*) */
+  ESF_F_VELOCITY_DT1 = 22,     /* f64 _velocityAtDt1 */
+  ESF_F_UNIT_FORCE = 23,       /* f64 _unitForce after "*= dt; += mv" */
+  /* integrator, per solid unknown (3 * solid nodes) */
+  ESF_F_SOLID_UNIT_FORCE = 30, /* f64 _solidUnitForce after "*= dt; += mv" */
+  ESF_F_SOLID_VELOCITY_DT0 = 31,
+  ESF_F_SOLID_PRESSURE_CORRECTION = 32,
+  ESF_F_DAMPED_SOLID_MASS = 33,
+  ESF_F_SYSTEM_DIAG = 34,      /* f64 _systemMatrix.diagonal() */
+  ESF_F_SYSTEM_BLOCKS = 35,    /* f64 [solid node][27 neighbours][3][3] of _systemMatrix */
+  ESF_F_SYSTEM_MASK = 36,      /* i32 [solid node] bit j = structural block j present */
+  /* per solid (solid index argument) */
+  ESF_F_S_U = 50,              /* f64 x3 per node */
+  ESF_F_S_X = 51,              /* f64 x3 per node */
+  ESF_F_S_VELOCITY = 52,       /* f64 x3 per node */
+  ESF_F_S_VEC_WORKSPACE = 53,  /* f64 x3 per node (previous extended velocity) */
+  ESF_F_S_MASS = 54,           /* f64 per node */
+  ESF_F_S_PHI = 55,            /* f64 per node */
+  ESF_F_S_DET_FINV = 56,       /* f64 per node */
+  ESF_F_S_VALID = 57,          /* i8 per cell, (xRes-1)(yRes-1)(zRes-1) */
+  ESF_F_S_QUARTER_FRACTIONS = 58, /* f64 8 per node */
+  ESF_F_S_PARTICLES = 59,      /* f64 10 per particle: pos, velocity, restPos, mass */
+  ESF_F_S_MESH_VERTICES = 60,  /* f64 x3 per vertex (current pose) */
+  ESF_F_S_BOXES = 61           /* i32 12: xmin..zmax, tightMin, tightMax */
+} esf_field;
+
+typedef struct esf_scene esf_scene;
+
+/* ---- library ----------------------------------------------------------- */
+int esf_abi_version(void);
+/* Text of the last error on this thread (never NULL). */
+const char* esf_last_error(void);
+/* Fills the reference defaults for a grid (see esf_params). */
+esf_status esf_params_default(const esf_grid* grid, esf_params* params);
+/* SIMPLE_PARSER::parse + the getInt/getFloat reads of main.cpp:63-141 and of
+ * the step path: reads a reference cfg file into grid, params and up to
+ * max_solids solid descriptors (mesh/mass paths are returned, not loaded).
+ * Replaces SIMPLE_PARSER (src/util/SIMPLE_PARSER.cpp:64-168). */
+esf_status esf_parse_config(const char* path, esf_grid* grid, esf_params* params,
+                            int* num_solids, char* solid_paths, size_t path_stride,
+                            esf_solid_desc* solids, int max_solids);
+
+/* ---- scene lifetime (COUPLED_INTEGRATOR_3D.h:29-78) ---------------------- */
+/* COUPLED_INTEGRATOR_3D::COUPLED_INTEGRATOR_3D (COUPLED_INTEGRATOR_3D.cpp:36-78).
+ * stream: a cudaStream_t to run on, or NULL for the scene's own stream. */
+esf_status esf_create(const esf_grid* grid, const esf_params* params, void* stream,
+                      esf_scene** out);
+/* ~COUPLED_INTEGRATOR_3D (COUPLED_INTEGRATOR_3D.cpp:79-86): frees everything. */
+esf_status esf_destroy(esf_scene* scene);
+/* new DEFOR_SOLID_3D + setters + COUPLED_INTEGRATOR_3D::addSolid
+ * (main.cpp:99-160; COUPLED_INTEGRATOR_3D.h:44). Copies all inputs. */
+esf_status esf_add_solid(esf_scene* scene, const esf_solid_desc* solid);
+/* COUPLED_INTEGRATOR_3D::setFluidDensity / setFluidViscocity (h:45-46). */
+esf_status esf_set_fluid(esf_scene* scene, double density, double viscosity);
+/* COUPLED_INTEGRATOR_3D::init (COUPLED_INTEGRATOR_3D.cpp:104-135). */
+esf_status esf_init(esf_scene* scene);
+/* COUPLED_INTEGRATOR_3D::setMaxDt (COUPLED_INTEGRATOR_3D.h:47). */
+esf_status esf_set_max_dt(esf_scene* scene, double max_dt);
+/* COUPLED_INTEGRATOR_3D::stepImplicit (COUPLED_INTEGRATOR_3D.cpp:377-636).
+ * report may be NULL. Synchronises the scene's stream before returning. */
+esf_status esf_step(esf_scene* scene, esf_step_report* report);
+/* COUPLED_INTEGRATOR_3D::dt() (h:48). */
+double esf_dt(const esf_scene* scene);
+
+/* ---- field access (the reference's member access; dumps, noise, I/O) ---- */
+/* count = number of elements, elem_bytes = bytes per element (8 f64, 4 i32,
+ * 1 i8); a field of 3-vectors counts 3 elements per node. */
+esf_status esf_field_info(const esf_scene* scene, esf_field field, int solid,
+                          size_t* count, size_t* elem_bytes);
+/* Copy a field to host memory (bytes must equal count*elem_bytes). */
+esf_status esf_get_field(esf_scene* scene, esf_field field, int solid, void* host,
+                         size_t bytes);
+/* Overwrite a field from host memory (node/solid fields only). */
+esf_status esf_set_field(esf_scene* scene, esf_field field, int solid,
+                         const void* host, size_t bytes);
+
+/* ---- solver operator seam ----------------------------------------------- */
+/* COUPLED_INTEGRATOR_3D::getMatVecMult (COUPLED_INTEGRATOR_3D.cpp:638-660):
+ * out = J diag(mass_inv) J^T in over the (xRes-1)(yRes-1)(zRes-1) pressure
+ * rows of `grid`. mass_inv: one value per node (xRes*yRes*zRes, boundary
+ * entries ignored). Device pointers, FP64. */
+esf_status esf_pressure_apply(const esf_grid* grid, const double* mass_inv_node,
+                              const double* in, double* out, void* stream);
+/* CONJUGATE_RESIDUAL<JACOBI_PRECONDITIONER>::solvePCR(b, x, getMatVecMult, app)
+ * (CONJUGATE_RESIDUAL.inl:109-192) with the pressure operator above and the
+ * Jacobi diagonal `diag`. x is the warm start on entry and the solution on
+ * exit. Device pointers; FP64 (precision ESF_FP64) or FP32 inner solves in
+ * FP64 refinement (ESF_MIXED). iterations/rel_residual may be NULL. */
+esf_status esf_pressure_solve(const esf_grid* grid, const double* mass_inv_node,
+                              const double* diag, const double* b, double* x,
+                              double eps, int max_iterations, int precision,
+                              int* iterations, double* rel_residual, void* stream);
+
+/* ---- checkpoint (COUPLED_INTEGRATOR_3D::writeFrame/readFrame :977-1012) --- */
+esf_status esf_write_frame(esf_scene* scene, const char* data_path, int frame, int debug);
+esf_status esf_read_frame(esf_scene* scene, const char* data_path, int frame, int debug);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EULERSF_H */
