@@ -1,0 +1,66 @@
+"""GB300 (sm_103a) implementation of EULERSF's coupled solid-fluid step.
+
+The product is the C-ABI library eulersf_gb300/_lib/libeulersf_gb300.so
+(include/eulersf.h). This package loads it with ctypes and mirrors the
+reference's integrator call surface (``CoupledIntegrator3D``). There is no
+CPU fallback: if the library is missing or no GPU is visible, the calls fail.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import abi
+from .integrator import CoupledIntegrator3D, build_from_scene, run_frames  # noqa: F401
+from .scene import SceneDesc, SolidDesc  # noqa: F401
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libeulersf_gb300.so")
+_lib = None
+
+# every symbol include/eulersf.h declares
+EXPORTS = [
+    "esf_abi_version", "esf_last_error", "esf_params_default", "esf_parse_config", "esf_create",
+    "esf_destroy", "esf_add_solid", "esf_set_fluid", "esf_init", "esf_set_max_dt", "esf_step",
+    "esf_dt", "esf_field_info", "esf_get_field", "esf_set_field", "esf_pressure_apply",
+    "esf_pressure_solve", "esf_write_frame", "esf_read_frame",
+]
+
+
+def load(build_if_missing: bool = False) -> C.CDLL:
+    """Load the CUDA library (raises if it is not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise RuntimeError(f"{LIB_PATH} is not built; run eulersf_gb300/build.py")
+        from .build import build
+        build()
+    lib = C.CDLL(LIB_PATH)
+    abi.declare(lib, "esf_", device_pointer_ops=True)
+    vp = C.c_void_p
+    lib.esf_create.argtypes = [C.POINTER(abi.Grid), C.POINTER(abi.Params), vp, C.POINTER(vp)]
+    lib.esf_create.restype = C.c_int
+    lib.esf_last_error.restype = C.c_char_p
+    lib.esf_abi_version.restype = C.c_int
+    lib.esf_pressure_apply.argtypes = [C.POINTER(abi.Grid), vp, vp, vp, vp]
+    lib.esf_pressure_solve.argtypes = [C.POINTER(abi.Grid), vp, vp, vp, vp, C.c_double, C.c_int,
+                                       C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), vp]
+    lib.esf_parse_config.argtypes = [C.c_char_p, C.POINTER(abi.Grid), C.POINTER(abi.Params),
+                                     C.POINTER(C.c_int), C.c_char_p, C.c_size_t,
+                                     C.POINTER(abi.SolidDesc), C.c_int]
+    lib.esf_write_frame.argtypes = [vp, C.c_char_p, C.c_int, C.c_int]
+    lib.esf_read_frame.argtypes = [vp, C.c_char_p, C.c_int, C.c_int]
+    _lib = lib
+    return lib
+
+
+def make_scene(desc: SceneDesc, precision: int = abi.ESF_FP64, noise: bool = True,
+          stream: int | None = None) -> CoupledIntegrator3D:
+    """GPU integrator for a synthetic scene, set up as the reference's driver does."""
+    return build_from_scene(load(), "esf_", desc, precision=precision, noise=noise, stream=stream)
+
+
+def last_error() -> str:
+    return (load().esf_last_error() or b"").decode()

@@ -1,0 +1,988 @@
+// Linear algebra of the coupled step on sm_103a:
+//  * the matrix-free pressure operator J diag(m^-1) J^T of
+//    COUPLED_INTEGRATOR_3D::getMatVecMult (COUPLED_INTEGRATOR_3D.cpp:638-660)
+//    as one fused z-marching stencil kernel (no J, no J^T, no mid vector);
+//  * the Jacobi-preconditioned Conjugate Residual recurrence of
+//    CONJUGATE_RESIDUAL::solvePCR (CONJUGATE_RESIDUAL.inl:109-276) as two
+//    kernels per iteration (axpy+norm, update+SpMV+dot) plus a residual check
+//    every 5th iteration, with all scalars kept on the device and the
+//    iteration chunks replayed as CUDA graphs;
+//  * FP32 inner solves inside FP64 iterative refinement (ESF_MIXED);
+//  * the solid system (M + dt^2 K) in 27-neighbour 3x3 block rows.
+#include <stdio.h>
+#include <string.h>
+
+#include <vector>
+
+#include "esf_common.cuh"
+
+namespace esf {
+
+// ------------------------------------------------------------ reductions
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  __syncthreads();
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double r = 0;
+  if (threadIdx.x < 32) {
+    r = (threadIdx.x < NT / 32) ? sh[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+  }
+  return r;  // valid in thread 0
+}
+
+// Deposit this block's partial; returns true in the block that arrives last,
+// after which `*total` holds the sum of all partials in block order.
+template <int NT>
+__device__ bool last_block_sum(double mine, double* partial, unsigned int* ticket, int nblocks,
+                               double* total, double* sh) {
+  __shared__ bool amLast;
+  const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  if (threadIdx.x == 0) {
+    partial[bid] = mine;
+    __threadfence();
+    unsigned int t = atomicAdd(ticket, 1u);
+    amLast = (t == (unsigned)nblocks - 1);
+  }
+  __syncthreads();
+  if (!amLast) return false;
+  __threadfence();
+  double acc = 0;
+  for (int i = threadIdx.x; i < nblocks; i += NT) acc += __ldcg(partial + i);
+  double s = block_sum<NT>(acc, sh);
+  if (threadIdx.x == 0) {
+    *total = s;
+    *ticket = 0;
+  }
+  return true;
+}
+
+// Scalars after the phase-B reduction r.s (CONJUGATE_RESIDUAL.inl:150-154).
+// Reference solves count iterations and leave the stop to the residual check
+// every 5th iteration; inner solves of a refinement stop as soon as the
+// preconditioned residual's energy r.Ar has fallen by eps^2.
+__device__ __forceinline__ void finish_update(PcrState* st, double total) {
+  if (st->setup) {
+    st->delta = total;
+    st->delta0 = total;
+    st->beta = 0.0;
+    st->setup = 0;
+    if (st->inner && !(total > 0.0)) {  // zero right-hand side: nothing to do
+      st->converged = 1;
+      st->done = 1;
+    }
+  } else {
+    st->beta = total / st->delta;
+    st->delta = total;
+    if (st->inner) {
+      st->iter++;
+      if (total <= st->eps * st->eps * st->delta0) {
+        st->converged = 1;
+        st->done = 1;
+      }
+    } else if (!(st->iter > 0 && st->iter % 5 == 0)) {
+      st->iter++;
+    }
+  }
+  if (!(total == total)) {
+    st->status = ESF_ERR_NUMERIC;
+    st->done = 1;
+  }
+}
+
+// r - alpha * (Ap / diag), evaluated identically wherever it is formed.
+__device__ __forceinline__ double upd_r(double r, double alpha, double ap, double iv) {
+  return __fma_rn(-alpha, __dmul_rn(ap, iv), r);
+}
+__device__ __forceinline__ float upd_r(float r, float alpha, float ap, float iv) {
+  return __fmaf_rn(-alpha, __fmul_rn(ap, iv), r);
+}
+
+// ------------------------------------------------------- pressure stencil
+// Tile of TX x TY cells marching over a z-chunk of CZ cell layers. Per layer:
+// (a) each halo cell column forms P = v(k-1)+v(k), Q = v(k-1)-v(k) of the
+//     stencil input v; (b) each node forms mid = J^T v from 4 P/Q values,
+//     scales by m^-1 and pairs with the previous node layer; (c) each cell
+//     forms out = J m from 4 node pairs.  ~36 flops/row, 1 read of v and
+//     m^-1, 1 write of out.
+constexpr int TX = 32, TY = 8, NT = TX * TY, HX = TX + 2, HY = TY + 2, NXN = TX + 1,
+              NYN = TY + 1;
+constexpr int NHALO = HX * HY, NNODE = NXN * NYN;
+
+enum StencilMode { S_APPLY = 0, S_UPDATE = 1, S_CHECK = 2, S_RESID_INIT = 3, S_RESID64 = 4 };
+
+template <typename T>
+struct StencilArgs {
+  const T* in;      // stencil input (APPLY/CHECK/RESID*: x)
+  T* x;             // UPDATE: x += alpha d
+  const T* d;
+  T* r;             // UPDATE: r (read; r - alpha Ap invd is the stencil input); RESID_INIT: out
+  const T* Ap;
+  const T* invd;
+  const T* minv;    // per node, zero on boundary nodes
+  T* out;           // APPLY: out; UPDATE: s
+  const T* b;       // CHECK / RESID*
+  float* out32;     // RESID64: float copy of b - Ax
+  double* partial;
+  PcrState* st;
+};
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(NT) pressure_stencil(GridDev g, StencilArgs<T> a, int cz) {
+  __shared__ T sP[NHALO], sQ[NHALO], sV[2][NHALO];
+  __shared__ T sA[NNODE], sB[NNODE], sC[NNODE];
+  __shared__ double sred[32];
+  if (MODE != S_APPLY && a.st->done) return;
+  const int tid = threadIdx.x;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * cz;
+  const int z1 = min(z0 + cz, g.cZ);
+  T alpha = 0;
+  if (MODE == S_UPDATE) alpha = (T)a.st->alpha;
+
+  // halo slots owned by this thread (column offsets into a cell layer)
+  long long hc[2];
+  bool hin[2], hown[2], hslot[2];
+  T prev[2] = {0, 0};
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const int hs = tid + q * NT;
+    const int hx = hs % HX, hy = hs / HX;
+    const int cx = x0 - 1 + hx, cy = y0 - 1 + hy;
+    hslot[q] = hs < NHALO;
+    hin[q] = hslot[q] && cx >= 0 && cx < g.cX && cy >= 0 && cy < g.cY;
+    hown[q] = hin[q] && hx >= 1 && hx <= TX && hy >= 1 && hy <= TY;
+    hc[q] = hin[q] ? cx + (long long)cy * g.cX : 0;
+  }
+  // node slots (boundary nodes carry no unknown: their m^-1 counts as 0)
+  long long nc[2];
+  bool nok[2], nslot[2];
+  T mpx[2] = {0, 0}, mpy[2] = {0, 0}, mpz[2] = {0, 0};
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const int ns = tid + q * NT;
+    const int nx = x0 + ns % NXN, ny = y0 + ns / NXN;
+    nslot[q] = ns < NNODE;
+    nok[q] = nslot[q] && nx > 0 && nx < g.X - 1 && ny > 0 && ny < g.Y - 1;
+    nc[q] = nok[q] ? nx + (long long)ny * g.X : 0;
+  }
+  const int ccx = tid % TX, ccy = tid / TX;
+  const int cgx = x0 + ccx, cgy = y0 + ccy;
+  const bool cin = cgx < g.cX && cgy < g.cY;
+  const long long ccol = cgx + (long long)cgy * g.cX;
+  double acc = 0.0;
+
+  // register prefetch of one layer: stencil input pieces + node m^-1
+  T pr[2], pa[2], pi[2], pm[2];
+  auto fetch = [&](int kk) {
+    const bool layerOk = kk >= 0 && kk < g.cZ;
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      pr[q] = 0;
+      pa[q] = 0;
+      pi[q] = 0;
+      if (hin[q] && layerOk) {
+        const long long c = hc[q] + (long long)kk * g.cslab;
+        if (MODE == S_UPDATE) {
+          pr[q] = a.r[c];
+          pa[q] = a.Ap[c];
+          pi[q] = a.invd[c];
+        } else {
+          pr[q] = a.in[c];
+        }
+      }
+      pm[q] = 0;
+      if (nok[q] && kk > 0 && kk < g.Z - 1) pm[q] = a.minv[nc[q] + (long long)kk * g.slab];
+    }
+  };
+  fetch(z0 - 1);
+  for (int kk = z0 - 1; kk <= z1; kk++) {
+    const int vb = kk & 1;
+    T cr[2], ca[2], ci[2], cm[2];
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      cr[q] = pr[q];
+      ca[q] = pa[q];
+      ci[q] = pi[q];
+      cm[q] = pm[q];
+    }
+    if (kk < z1) fetch(kk + 1);  // in flight while this layer computes
+    // (a) stencil input of cell layer kk
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      if (!hslot[q]) continue;
+      T v = cr[q];
+      if (MODE == S_UPDATE) {
+        // r itself is advanced by the next phase A: neighbouring tiles read
+        // r as halo during this kernel, so it is not written here.
+        v = upd_r(cr[q], alpha, ca[q], ci[q]);
+        if (hown[q] && kk >= z0 && kk < z1) {
+          const long long c = hc[q] + (long long)kk * g.cslab;
+          a.x[c] = a.x[c] + alpha * a.d[c];
+        }
+      }
+      const int hs = tid + q * NT;
+      sP[hs] = prev[q] + v;
+      sQ[hs] = prev[q] - v;
+      sV[vb][hs] = prev[q];  // layer kk-1, read in (c) of this layer
+      prev[q] = v;
+    }
+    __syncthreads();
+    // (b) node layer kk
+    if (kk >= z0) {
+#pragma unroll
+      for (int q = 0; q < 2; q++) {
+        if (!nslot[q]) continue;
+        const int ns = tid + q * NT;
+        const int nx = ns % NXN, ny = ns / NXN;
+        const int s00 = nx + ny * HX, s10 = s00 + 1, s01 = s00 + HX, s11 = s01 + 1;
+        T mi = cm[q];
+        T mx = ((sP[s00] + sP[s01]) - (sP[s10] + sP[s11])) * mi;
+        T my = ((sP[s00] + sP[s10]) - (sP[s01] + sP[s11])) * mi;
+        T mz = ((sQ[s00] + sQ[s10]) + (sQ[s01] + sQ[s11])) * mi;
+        if (kk >= z0 + 1) {
+          sA[ns] = mpx[q] + mx;
+          sB[ns] = mpy[q] + my;
+          sC[ns] = mz - mpz[q];
+        }
+        mpx[q] = mx;
+        mpy[q] = my;
+        mpz[q] = mz;
+      }
+    }
+    __syncthreads();
+    // (c) output cell layer kk-1
+    if (kk >= z0 + 1 && cin) {
+      const int n00 = ccx + ccy * NXN, n10 = n00 + 1, n01 = n00 + NXN, n11 = n01 + 1;
+      T xp = (sA[n10] + sA[n11]) - (sA[n00] + sA[n01]);
+      T yp = (sB[n01] + sB[n11]) - (sB[n00] + sB[n10]);
+      T zp = (sC[n00] + sC[n10]) + (sC[n01] + sC[n11]);
+      T o = xp + yp + zp;
+      const long long c = ccol + (long long)(kk - 1) * g.cslab;
+      if (MODE == S_APPLY) {
+        a.out[c] = o;
+      } else if (MODE == S_UPDATE) {
+        a.out[c] = o;
+        T rv = sV[vb][(ccx + 1) + (ccy + 1) * HX];
+        acc += (double)(rv * o);
+      } else if (MODE == S_CHECK) {
+        double t = (double)o - (double)a.b[c];
+        acc += t * t;
+      } else if (MODE == S_RESID_INIT) {
+        T bb = a.b[c];
+        a.r[c] = (bb - o) * a.invd[c];
+        acc += (double)bb * (double)bb;
+      } else if (MODE == S_RESID64) {
+        T rr = a.b[c] - o;
+        a.r[c] = rr;
+        a.out32[c] = (float)rr;
+        acc += (double)rr * (double)rr;
+      }
+    }
+  }
+  if (MODE == S_APPLY) return;
+  __syncthreads();
+  double bs = block_sum<NT>(acc, sred);
+  const int nblocks = gridDim.x * gridDim.y * gridDim.z;
+  double total;
+  if (last_block_sum<NT>(bs, a.partial, &a.st->ticket[1], nblocks, &total, sred) &&
+      threadIdx.x == 0) {
+    PcrState* st = a.st;
+    if (MODE == S_UPDATE) {
+      finish_update(st, total);
+    } else if (MODE == S_CHECK || MODE == S_RESID64) {
+      st->resid2 = total;
+      if (MODE == S_CHECK) {
+        if (sqrt(total) < st->eps * sqrt(st->bnorm2)) {
+          st->converged = 1;
+          st->done = 1;
+        } else {
+          st->iter++;
+        }
+      }
+      if (!(total == total)) {
+        st->status = ESF_ERR_NUMERIC;
+        st->done = 1;
+      }
+    } else if (MODE == S_RESID_INIT) {
+      st->bnorm2 = total;
+    }
+  }
+}
+
+// ------------------------------------------------------- vector kernels
+constexpr int VT = 256;
+
+// Phase A of iteration i (CONJUGATE_RESIDUAL.inl:146, 139-142, 156-160):
+// [UPDR] r = r - alpha_{i-1} Ap_{i-1}/diag (the residual update of the
+// previous iteration); d = beta d + r; Ap = beta Ap + s;
+// alpha_i = delta / (Ap . Ap/diag).
+template <typename T, bool UPDR>
+__global__ void __launch_bounds__(VT) pcr_phase_a(long long n, T* d, T* r, T* Ap, const T* s,
+                                                  const T* invd, double* partial, PcrState* st) {
+  __shared__ double sred[32];
+  if (st->done) return;
+  if (st->iter >= st->maxIt) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->done = 1;
+    return;
+  }
+  const T beta = (T)st->beta;
+  const T alpha = (T)st->alpha;
+  T acc = 0;
+  for (long long i = blockIdx.x * (long long)VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT) {
+    T a = Ap[i], iv = invd[i], rv = r[i];
+    if (UPDR) {
+      rv = upd_r(rv, alpha, a, iv);
+      r[i] = rv;
+    }
+    T dv = beta * d[i] + rv;
+    T av = beta * a + s[i];
+    d[i] = dv;
+    Ap[i] = av;
+    acc += av * (av * iv);
+  }
+  double bs = block_sum<VT>((double)acc, sred);
+  double total;
+  if (last_block_sum<VT>(bs, partial, &st->ticket[0], gridDim.x, &total, sred) &&
+      threadIdx.x == 0) {
+    st->alpha = (fabs(total) > 0.0) ? st->delta / total : total;
+    if (!(total == total)) {
+      st->status = ESF_ERR_NUMERIC;
+      st->done = 1;
+    }
+  }
+}
+
+// Zero-start set-up for a vector b: r = b/diag, ||b||^2; d = Ap = 0.
+template <typename T>
+__global__ void __launch_bounds__(VT) pcr_zero_start(long long n, const T* b, const T* invd, T* x,
+                                                     T* r, T* d, T* Ap, double* partial,
+                                                     PcrState* st) {
+  __shared__ double sred[32];
+  double acc = 0;
+  for (long long i = blockIdx.x * (long long)VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT) {
+    T bv = b[i];
+    x[i] = 0;
+    r[i] = bv * invd[i];
+    d[i] = 0;
+    Ap[i] = 0;
+    acc += (double)bv * (double)bv;
+  }
+  double bs = block_sum<VT>(acc, sred);
+  double total;
+  if (last_block_sum<VT>(bs, partial, &st->ticket[2], gridDim.x, &total, sred) &&
+      threadIdx.x == 0)
+    st->bnorm2 = total;
+}
+
+// *out = sum b^2 (deterministic block order)
+template <typename T>
+__global__ void __launch_bounds__(VT) vec_norm2(long long n, const T* b, double* partial,
+                                                unsigned int* ticket, double* out) {
+  __shared__ double sred[32];
+  double acc = 0;
+  for (long long i = blockIdx.x * (long long)VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT)
+    acc += (double)b[i] * (double)b[i];
+  double bs = block_sum<VT>(acc, sred);
+  double total;
+  if (last_block_sum<VT>(bs, partial, ticket, gridDim.x, &total, sred) && threadIdx.x == 0)
+    *out = total;
+}
+
+template <typename T>
+__global__ void zero2(long long n, T* a, T* b) {
+  for (long long i = blockIdx.x * (long long)VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT) {
+    a[i] = 0;
+    b[i] = 0;
+  }
+}
+
+template <typename A, typename B>
+__global__ void convert_vec(long long n, const A* in, B* out) {
+  for (long long i = blockIdx.x * (long long)VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT)
+    out[i] = (B)in[i];
+}
+__global__ void inv_vec(long long n, const double* in, double* out64, float* out32) {
+  for (long long i = blockIdx.x * (long long)VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT) {
+    double v = 1.0 / in[i];
+    if (out64) out64[i] = v;
+    if (out32) out32[i] = (float)v;
+  }
+}
+__global__ void add_correction(long long n, double* x, const float* e) {
+  for (long long i = blockIdx.x * (long long)VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT)
+    x[i] += (double)e[i];
+}
+
+static int vec_blocks(long long n) {
+  long long b = (n + VT - 1) / VT;
+  int cap = 152 * 8;
+  return (int)(b < cap ? (b > 0 ? b : 1) : cap);
+}
+
+// ------------------------------------------------------ pressure solver
+struct PressureWork {
+  long long R, T;
+  // FP64 path (also the outer loop of the mixed path)
+  double *r, *d, *Ap, *s, *invd;
+  // mixed inner path
+  float *x32, *r32, *d32, *Ap32, *s32, *invd32, *minv32, *b32;
+  double* partial;
+  PcrState* st;      // device state (FP64 solve / outer loop)
+  PcrState* st32;    // device state (inner solve)
+  PcrState* hst;     // pinned host copies [8]
+  cudaGraphExec_t gFirst, gChunk, gFirst32, gChunk32;
+  GridDev g;
+  bool graphsFor64, graphsFor32;
+  const void* keyA[8];  // pointers the captured graphs were built for
+  const void* keyB[8];
+  cudaStream_t capStream;
+  cudaEvent_t ev[4];
+};
+
+// z-chunk depth: deep enough to amortise the two halo layers, shallow
+// enough to give every SM several tiles.
+static int stencil_cz(const GridDev& g) {
+  long long xy = (long long)((g.cX + TX - 1) / TX) * ((g.cY + TY - 1) / TY);
+  long long want = 152LL * 6;
+  long long cz = (xy * g.cZ + want - 1) / want;
+  if (cz < 4) cz = 4;
+  if (cz > 32) cz = 32;
+  if (cz > g.cZ) cz = g.cZ;
+  return (int)cz;
+}
+template <typename T>
+static dim3 stencil_grid(const GridDev& g) {
+  int cz = stencil_cz(g);
+  return dim3((g.cX + TX - 1) / TX, (g.cY + TY - 1) / TY, (g.cZ + cz - 1) / cz);
+}
+
+template <typename T>
+esf_status pressure_apply(const GridDev& g, const T* minv, const T* in, T* out, cudaStream_t st) {
+  StencilArgs<T> a;
+  memset(&a, 0, sizeof a);
+  a.in = in;
+  a.minv = minv;
+  a.out = out;
+  pressure_stencil<T, S_APPLY><<<stencil_grid<T>(g), NT, 0, st>>>(g, a, stencil_cz(g));
+  ESF_LAUNCH_CHECK();
+  return ESF_OK;
+}
+template esf_status pressure_apply<double>(const GridDev&, const double*, const double*, double*,
+                                           cudaStream_t);
+template esf_status pressure_apply<float>(const GridDev&, const float*, const float*, float*,
+                                          cudaStream_t);
+
+esf_status pressure_work_alloc(PressureWork** out, const GridDev& g, int mixed) {
+  PressureWork* w = new PressureWork();
+  memset(w, 0, sizeof *w);
+  w->R = g.R;
+  w->T = g.T;
+  w->g = g;
+  size_t R = g.R;
+  ESF_CUDA(cudaMalloc(&w->r, R * 8));
+  ESF_CUDA(cudaMalloc(&w->d, R * 8));
+  ESF_CUDA(cudaMalloc(&w->Ap, R * 8));
+  ESF_CUDA(cudaMalloc(&w->s, R * 8));
+  ESF_CUDA(cudaMalloc(&w->invd, R * 8));
+  if (mixed) {
+    ESF_CUDA(cudaMalloc(&w->x32, R * 4));
+    ESF_CUDA(cudaMalloc(&w->r32, R * 4));
+    ESF_CUDA(cudaMalloc(&w->d32, R * 4));
+    ESF_CUDA(cudaMalloc(&w->Ap32, R * 4));
+    ESF_CUDA(cudaMalloc(&w->s32, R * 4));
+    ESF_CUDA(cudaMalloc(&w->invd32, R * 4));
+    ESF_CUDA(cudaMalloc(&w->b32, R * 4));
+    ESF_CUDA(cudaMalloc(&w->minv32, g.T * 4));
+  }
+  ESF_CUDA(cudaMalloc(&w->partial, ESF_MAX_PARTIALS * 8));
+  ESF_CUDA(cudaMalloc(&w->st, sizeof(PcrState)));
+  ESF_CUDA(cudaMalloc(&w->st32, sizeof(PcrState)));
+  ESF_CUDA(cudaMemset(w->st, 0, sizeof(PcrState)));
+  ESF_CUDA(cudaMemset(w->st32, 0, sizeof(PcrState)));
+  ESF_CUDA(cudaMallocHost(&w->hst, 8 * sizeof(PcrState)));
+  ESF_CUDA(cudaStreamCreateWithFlags(&w->capStream, cudaStreamNonBlocking));
+  for (int i = 0; i < 4; i++) ESF_CUDA(cudaEventCreateWithFlags(&w->ev[i], cudaEventDisableTiming));
+  *out = w;
+  return ESF_OK;
+}
+
+void pressure_work_free(PressureWork* w) {
+  if (!w) return;
+  cudaFree(w->r); cudaFree(w->d); cudaFree(w->Ap); cudaFree(w->s); cudaFree(w->invd);
+  cudaFree(w->x32); cudaFree(w->r32); cudaFree(w->d32); cudaFree(w->Ap32); cudaFree(w->s32);
+  cudaFree(w->invd32); cudaFree(w->b32); cudaFree(w->minv32);
+  cudaFree(w->partial); cudaFree(w->st); cudaFree(w->st32);
+  if (w->hst) cudaFreeHost(w->hst);
+  if (w->gFirst) cudaGraphExecDestroy(w->gFirst);
+  if (w->gChunk) cudaGraphExecDestroy(w->gChunk);
+  if (w->gFirst32) cudaGraphExecDestroy(w->gFirst32);
+  if (w->gChunk32) cudaGraphExecDestroy(w->gChunk32);
+  if (w->capStream) cudaStreamDestroy(w->capStream);
+  for (int i = 0; i < 4; i++)
+    if (w->ev[i]) cudaEventDestroy(w->ev[i]);
+  delete w;
+}
+
+// Enqueue iterations of the PCR loop for precision T on stream s.
+template <typename T>
+struct PressureKernels {
+  GridDev g;
+  const T *minv, *invd, *b;
+  T *x, *r, *d, *Ap, *s;
+  double* partial;
+  PcrState* st;
+  void setup_warm(cudaStream_t cs) const {  // r = (b - Ax)/diag, ||b||; then s = Ar, delta
+    StencilArgs<T> a;
+    memset(&a, 0, sizeof a);
+    a.in = x; a.b = b; a.r = r; a.invd = invd; a.minv = minv; a.partial = partial; a.st = st;
+    pressure_stencil<T, S_RESID_INIT><<<stencil_grid<T>(g), NT, 0, cs>>>(g, a, stencil_cz(g));
+    zero2<T><<<vec_blocks(g.R), VT, 0, cs>>>(g.R, d, Ap);
+    update(cs);
+  }
+  void setup_zero(cudaStream_t cs) const {
+    pcr_zero_start<T><<<vec_blocks(g.R), VT, 0, cs>>>(g.R, b, invd, x, r, d, Ap, partial, st);
+    update(cs);
+  }
+  void phase_a(cudaStream_t cs) const {
+    pcr_phase_a<T, true><<<vec_blocks(g.R), VT, 0, cs>>>(g.R, d, r, Ap, s, invd, partial, st);
+  }
+  void update(cudaStream_t cs) const {
+    StencilArgs<T> a;
+    memset(&a, 0, sizeof a);
+    a.x = x; a.d = d; a.r = r; a.Ap = Ap; a.invd = invd; a.minv = minv; a.out = s;
+    a.partial = partial; a.st = st;
+    pressure_stencil<T, S_UPDATE><<<stencil_grid<T>(g), NT, 0, cs>>>(g, a, stencil_cz(g));
+  }
+  void check(cudaStream_t cs) const {
+    StencilArgs<T> a;
+    memset(&a, 0, sizeof a);
+    a.in = x; a.b = b; a.minv = minv; a.partial = partial; a.st = st;
+    pressure_stencil<T, S_CHECK><<<stencil_grid<T>(g), NT, 0, cs>>>(g, a, stencil_cz(g));
+  }
+  // iterations [i0, i0+n) followed by the residual check of iteration
+  // i0+n-1 (reference solves only; inner solves stop on delta)
+  void chunk(cudaStream_t cs, int n, bool withCheck) const {
+    for (int k = 0; k < n; k++) {
+      phase_a(cs);
+      update(cs);
+    }
+    if (withCheck) check(cs);
+  }
+};
+
+template <typename K>
+static esf_status capture(cudaStream_t cs, const K& k, bool first, bool warm, cudaGraphExec_t* exec) {
+  cudaGraph_t graph;
+  ESF_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+  // reference solves warm-start and check every 5th iteration; inner solves
+  // of a refinement start from zero and stop on delta
+  if (first) {
+    if (warm) k.setup_warm(cs);
+    else k.setup_zero(cs);
+    k.chunk(cs, 6, warm);  // iterations 0..5, first check at i = 5
+  } else {
+    k.chunk(cs, 5, warm);  // iterations 5j+1 .. 5j+5
+  }
+  ESF_CUDA(cudaStreamEndCapture(cs, &graph));
+  if (*exec) cudaGraphExecDestroy(*exec);
+  ESF_CUDA(cudaGraphInstantiate(exec, graph, 0));
+  cudaGraphDestroy(graph);
+  return ESF_OK;
+}
+
+// Runs one PCR solve from graphs; keeps up to 3 chunks in flight and polls
+// pinned copies of the device state.
+static esf_status run_graph_solve(PressureWork* w, PcrState* dst, cudaGraphExec_t gFirst,
+                                  cudaGraphExec_t gChunk, int maxIt, cudaStream_t st,
+                                  PcrState* out) {
+  const int inflight = 3;
+  int launched = 0, waited = 0;
+  const int maxChunks = maxIt / 5 + 3;
+  bool done = false;
+  while (!done) {
+    if (launched < maxChunks) {
+      ESF_CUDA(cudaGraphLaunch(launched == 0 ? gFirst : gChunk, st));
+      ESF_CUDA(cudaMemcpyAsync(&w->hst[launched % 4], dst, sizeof(PcrState), cudaMemcpyDeviceToHost, st));
+      ESF_CUDA(cudaEventRecord(w->ev[launched % 4], st));
+      launched++;
+    }
+    if (launched - waited >= inflight || launched >= maxChunks) {
+      ESF_CUDA(cudaEventSynchronize(w->ev[waited % 4]));
+      PcrState h = w->hst[waited % 4];
+      waited++;
+      if (h.done) {
+        done = true;
+        *out = h;
+      } else if (waited >= maxChunks) {
+        done = true;
+        *out = h;
+      }
+    }
+  }
+  // drain chunks still queued (they exit at once on `done`)
+  ESF_CUDA(cudaStreamSynchronize(st));
+  ESF_CUDA(cudaMemcpy(out, dst, sizeof(PcrState), cudaMemcpyDeviceToHost));
+  return ESF_OK;
+}
+
+static esf_status init_state(PcrState* d, double eps, int maxIt, cudaStream_t st, int inner = 0) {
+  PcrState h;
+  memset(&h, 0, sizeof h);
+  h.eps = eps;
+  h.maxIt = maxIt;
+  h.setup = 1;
+  h.inner = inner;
+  ESF_CUDA(cudaMemcpyAsync(d, &h, sizeof h, cudaMemcpyHostToDevice, st));
+  // the pageable source must not change before the copy runs
+  ESF_CUDA(cudaStreamSynchronize(st));
+  return ESF_OK;
+}
+
+esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv64,
+                          const double* diag64, const double* b, double* x, double eps, int maxIt,
+                          int precision, double innerEps, int maxRefine, int* iters,
+                          double* relres, int* refinements, int* converged, cudaStream_t st) {
+  {
+    dim3 gr = stencil_grid<double>(g);
+    if ((long long)gr.x * gr.y * gr.z > ESF_MAX_PARTIALS) return ESF_ERR_UNSUPPORTED;
+  }
+  inv_vec<<<vec_blocks(g.R), VT, 0, st>>>(g.R, diag64, w->invd, w->invd32);
+  ESF_LAUNCH_CHECK();
+  if (precision == ESF_FP64) {
+    PressureKernels<double> k{g, minv64, w->invd, b, x, w->r, w->d, w->Ap, w->s, w->partial, w->st};
+    const void* key[8] = {minv64, diag64, b, x, nullptr, nullptr, nullptr, nullptr};
+    bool rebuild = !w->graphsFor64 || memcmp(key, w->keyA, sizeof key) != 0;
+    if (rebuild) {
+      esf_status e = capture(w->capStream, k, true, true, &w->gFirst);
+      if (e) return e;
+      e = capture(w->capStream, k, false, true, &w->gChunk);
+      if (e) return e;
+      memcpy(w->keyA, key, sizeof key);
+      w->graphsFor64 = true;
+    }
+    esf_status e = init_state(w->st, eps, maxIt, st);
+    if (e) return e;
+    PcrState h;
+    e = run_graph_solve(w, w->st, w->gFirst, w->gChunk, maxIt, st, &h);
+    if (e) return e;
+    if (iters) *iters = h.iter;
+    if (converged) *converged = h.converged;
+    if (refinements) *refinements = 0;
+    if (relres) *relres = h.bnorm2 > 0 ? sqrt(h.resid2 / h.bnorm2) : sqrt(h.resid2);
+    return h.status ? (esf_status)h.status : ESF_OK;
+  }
+  // ---- mixed: FP32 inner PCR inside FP64 iterative refinement
+  convert_vec<double, float><<<vec_blocks(g.T), VT, 0, st>>>(g.T, minv64, w->minv32);
+  PressureKernels<float> k32{g, w->minv32, w->invd32, w->b32, w->x32, w->r32, w->d32, w->Ap32,
+                             w->s32, w->partial, w->st32};
+  const void* key[8] = {w->minv32, w->invd32, w->b32, w->x32, nullptr, nullptr, nullptr, nullptr};
+  if (!w->graphsFor32 || memcmp(key, w->keyB, sizeof key) != 0) {
+    esf_status e = capture(w->capStream, k32, true, false, &w->gFirst32);
+    if (e) return e;
+    e = capture(w->capStream, k32, false, false, &w->gChunk32);
+    if (e) return e;
+    memcpy(w->keyB, key, sizeof key);
+    w->graphsFor32 = true;
+  }
+  int total = 0, ref = 0, conv = 0;
+  double bnorm2 = -1, rel = 0;
+  esf_status status = ESF_OK;
+  for (ref = 0; ref <= maxRefine; ref++) {
+    // r = b - A x in FP64 (also ||b||^2 the first time)
+    esf_status e = init_state(w->st, eps, maxIt, st);
+    if (e) return e;
+    StencilArgs<double> a;
+    memset(&a, 0, sizeof a);
+    a.in = x; a.b = b; a.r = w->r; a.out32 = w->b32; a.minv = minv64; a.partial = w->partial;
+    a.st = w->st;
+    pressure_stencil<double, S_RESID64><<<stencil_grid<double>(g), NT, 0, st>>>(g, a, stencil_cz(g));
+    ESF_LAUNCH_CHECK();
+    if (bnorm2 < 0) {
+      vec_norm2<double><<<vec_blocks(g.R), VT, 0, st>>>(g.R, b, w->partial + ESF_MAX_PARTIALS / 2,
+                                                      &w->st->ticket[3], &w->st->bnorm2);
+      ESF_LAUNCH_CHECK();
+    }
+    PcrState h;
+    ESF_CUDA(cudaMemcpyAsync(&h, w->st, sizeof h, cudaMemcpyDeviceToHost, st));
+    ESF_CUDA(cudaStreamSynchronize(st));
+    if (bnorm2 < 0) bnorm2 = h.bnorm2;
+    rel = bnorm2 > 0 ? sqrt(h.resid2 / bnorm2) : sqrt(h.resid2);
+    if (!(h.resid2 == h.resid2)) {
+      status = ESF_ERR_NUMERIC;
+      break;
+    }
+    if (sqrt(h.resid2) < eps * sqrt(bnorm2)) {
+      conv = 1;
+      break;
+    }
+    if (ref == maxRefine || total >= maxIt) break;
+    // inner FP32 solve of A e = r from e = 0
+    e = init_state(w->st32, innerEps, maxIt - total, st, 1);
+    if (e) return e;
+    PcrState hi;
+    e = run_graph_solve(w, w->st32, w->gFirst32, w->gChunk32, maxIt - total, st, &hi);
+    if (e) return e;
+    total += hi.iter + (hi.converged ? 0 : 0);
+    if (hi.status) {
+      status = (esf_status)hi.status;
+      break;
+    }
+    add_correction<<<vec_blocks(g.R), VT, 0, st>>>(g.R, x, w->x32);
+    ESF_LAUNCH_CHECK();
+  }
+  if (iters) *iters = total;
+  if (refinements) *refinements = ref;
+  if (relres) *relres = rel;
+  if (converged) *converged = conv;
+  return status;
+}
+
+// -------------------------------------------------------- solid solver
+// Block-row SpMV y = A x over the 27-neighbour 3x3 blocks; modes as for the
+// pressure stencil.
+template <typename T, int MODE>
+__global__ void __launch_bounds__(VT) solid_spmv(long long S, const T* __restrict__ blocks,
+                                                 const int* __restrict__ nbr, const T* in,
+                                                 const T* b, T* r, T* out, float* out32,
+                                                 double* partial, PcrState* st) {
+  __shared__ double sred[32];
+  if (MODE != S_APPLY && st->done) return;
+  double acc = 0;
+  for (long long a = blockIdx.x * (long long)VT + threadIdx.x; a < S; a += (long long)gridDim.x * VT) {
+    T y0 = 0, y1 = 0, y2 = 0;
+    const T* B = blocks + a * 243;
+    const int* nb = nbr + a * 27;
+#pragma unroll 1
+    for (int j = 0; j < 27; j++) {
+      int m = nb[j];
+      if (m < 0) continue;
+      T v0 = in[3 * (long long)m], v1 = in[3 * (long long)m + 1], v2 = in[3 * (long long)m + 2];
+      const T* Bj = B + 9 * j;
+      y0 += Bj[0] * v0 + Bj[1] * v1 + Bj[2] * v2;
+      y1 += Bj[3] * v0 + Bj[4] * v1 + Bj[5] * v2;
+      y2 += Bj[6] * v0 + Bj[7] * v1 + Bj[8] * v2;
+    }
+    T y[3] = {y0, y1, y2};
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      long long i = 3 * a + c;
+      if (MODE == S_APPLY) {
+        out[i] = y[c];
+      } else if (MODE == S_UPDATE) {
+        out[i] = y[c];
+        acc += (double)(in[i] * y[c]);
+      } else if (MODE == S_CHECK) {
+        double t = (double)y[c] - (double)b[i];
+        acc += t * t;
+      } else if (MODE == S_RESID64) {
+        T rr = b[i] - y[c];
+        r[i] = rr;
+        out32[i] = (float)rr;
+        acc += (double)rr * (double)rr;
+      }
+    }
+  }
+  if (MODE == S_APPLY) return;
+  double bs = block_sum<VT>(acc, sred);
+  double total;
+  if (last_block_sum<VT>(bs, partial, &st->ticket[1], gridDim.x, &total, sred) &&
+      threadIdx.x == 0) {
+    if (MODE == S_UPDATE) {
+      finish_update(st, total);
+    } else {
+      st->resid2 = total;
+      if (MODE == S_CHECK) {
+        if (sqrt(total) < st->eps * sqrt(st->bnorm2)) {
+          st->converged = 1;
+          st->done = 1;
+        } else {
+          st->iter++;
+        }
+      }
+      if (!(total == total)) {
+        st->status = ESF_ERR_NUMERIC;
+        st->done = 1;
+      }
+    }
+  }
+}
+
+// x += alpha d; r -= alpha Ap/diag (pointwise part of phase B).
+template <typename T>
+__global__ void __launch_bounds__(VT) pcr_update_xr(long long n, T* x, const T* d, T* r, const T* Ap,
+                                                    const T* invd, const PcrState* st) {
+  if (st->done) return;
+  const T alpha = (T)st->alpha;
+  for (long long i = blockIdx.x * (long long)VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT) {
+    x[i] = x[i] + alpha * d[i];
+    r[i] = upd_r(r[i], alpha, Ap[i], invd[i]);
+  }
+}
+
+struct SolidWork {
+  long long S;
+  double *r, *d, *Ap, *s, *invd, *partial;
+  float *blocks32, *x32, *r32, *d32, *Ap32, *s32, *invd32, *b32;
+  PcrState *st, *st32;
+  long long cap;
+};
+
+esf_status solid_work_alloc(SolidWork** out, long long S, int mixed) {
+  SolidWork* w = new SolidWork();
+  memset(w, 0, sizeof *w);
+  w->S = S;
+  w->cap = S > 0 ? S : 1;
+  size_t n = 3 * w->cap;
+  ESF_CUDA(cudaMalloc(&w->r, n * 8));
+  ESF_CUDA(cudaMalloc(&w->d, n * 8));
+  ESF_CUDA(cudaMalloc(&w->Ap, n * 8));
+  ESF_CUDA(cudaMalloc(&w->s, n * 8));
+  ESF_CUDA(cudaMalloc(&w->invd, n * 8));
+  ESF_CUDA(cudaMalloc(&w->partial, ESF_MAX_PARTIALS * 8));
+  ESF_CUDA(cudaMalloc(&w->st, sizeof(PcrState)));
+  ESF_CUDA(cudaMalloc(&w->st32, sizeof(PcrState)));
+  if (mixed) {
+    ESF_CUDA(cudaMalloc(&w->blocks32, w->cap * 243 * 4));
+    ESF_CUDA(cudaMalloc(&w->x32, n * 4));
+    ESF_CUDA(cudaMalloc(&w->r32, n * 4));
+    ESF_CUDA(cudaMalloc(&w->d32, n * 4));
+    ESF_CUDA(cudaMalloc(&w->Ap32, n * 4));
+    ESF_CUDA(cudaMalloc(&w->s32, n * 4));
+    ESF_CUDA(cudaMalloc(&w->invd32, n * 4));
+    ESF_CUDA(cudaMalloc(&w->b32, n * 4));
+  }
+  *out = w;
+  return ESF_OK;
+}
+long long solid_work_capacity(const SolidWork* w) { return w ? w->cap : 0; }
+void solid_work_free(SolidWork* w) {
+  if (!w) return;
+  cudaFree(w->r); cudaFree(w->d); cudaFree(w->Ap); cudaFree(w->s); cudaFree(w->invd);
+  cudaFree(w->partial); cudaFree(w->st); cudaFree(w->st32); cudaFree(w->blocks32);
+  cudaFree(w->x32); cudaFree(w->r32); cudaFree(w->d32); cudaFree(w->Ap32); cudaFree(w->s32);
+  cudaFree(w->invd32); cudaFree(w->b32);
+  delete w;
+}
+
+template <typename T>
+static esf_status solid_pcr(long long S, const T* blocks, const int* nbr, const T* invd,
+                            const T* b, T* x, T* r, T* d, T* Ap, T* s, double* partial,
+                            PcrState* dst, double eps, int maxIt, cudaStream_t st, PcrState* out,
+                            int inner) {
+  const long long n = 3 * S;
+  const int vb = vec_blocks(n), sb = vec_blocks(S);
+  esf_status e = init_state(dst, eps, maxIt, st, inner);
+  if (e) return e;
+  // assembled variant: x = 0, r = b/diag (CONJUGATE_RESIDUAL.inl:196-205)
+  pcr_zero_start<T><<<vb, VT, 0, st>>>(n, b, invd, x, r, d, Ap, partial, dst);
+  solid_spmv<T, S_UPDATE><<<sb, VT, 0, st>>>(S, blocks, nbr, r, nullptr, nullptr, s, nullptr,
+                                             partial, dst);
+  ESF_LAUNCH_CHECK();
+  PcrState h;
+  memset(&h, 0, sizeof h);
+  const int maxChunks = maxIt / 5 + 3;
+  for (int chunk = 0; chunk < maxChunks; chunk++) {
+    const int nIt = (chunk == 0) ? 6 : 5;  // iterations 0..5, then 5j+1..5j+5
+    for (int k = 0; k < nIt; k++) {
+      pcr_phase_a<T, false><<<vb, VT, 0, st>>>(n, d, r, Ap, s, invd, partial, dst);
+      pcr_update_xr<T><<<vb, VT, 0, st>>>(n, x, d, r, Ap, invd, dst);
+      solid_spmv<T, S_UPDATE><<<sb, VT, 0, st>>>(S, blocks, nbr, r, nullptr, nullptr, s, nullptr,
+                                                 partial, dst);
+    }
+    if (!inner)
+      solid_spmv<T, S_CHECK><<<sb, VT, 0, st>>>(S, blocks, nbr, x, b, nullptr, nullptr, nullptr,
+                                                partial, dst);
+    ESF_LAUNCH_CHECK();
+    ESF_CUDA(cudaMemcpyAsync(&h, dst, sizeof h, cudaMemcpyDeviceToHost, st));
+    ESF_CUDA(cudaStreamSynchronize(st));
+    if (h.done) break;
+  }
+  *out = h;
+  return ESF_OK;
+}
+
+esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const int* nbr,
+                       const double* diag, const double* b, double* x, double eps, int maxIt,
+                       int precision, double innerEps, int maxRefine, int* iters, double* relres,
+                       int* refinements, int* converged, cudaStream_t st) {
+  if (S <= 0) {
+    if (iters) *iters = 0;
+    if (converged) *converged = 0;
+    if (relres) *relres = 0;
+    if (refinements) *refinements = 0;
+    return ESF_OK;
+  }
+  const long long n = 3 * S;
+  if ((n + VT - 1) / VT > ESF_MAX_PARTIALS * 64LL) return ESF_ERR_UNSUPPORTED;
+  inv_vec<<<vec_blocks(n), VT, 0, st>>>(n, diag, w->invd, w->invd32);
+  ESF_LAUNCH_CHECK();
+  if (precision == ESF_FP64) {
+    PcrState h;
+    esf_status e = solid_pcr<double>(S, blocks, nbr, w->invd, b, x, w->r, w->d, w->Ap, w->s,
+                                     w->partial, w->st, eps, maxIt, st, &h, 0);
+    if (e) return e;
+    if (iters) *iters = h.iter;
+    if (converged) *converged = h.converged;
+    if (refinements) *refinements = 0;
+    if (relres) *relres = h.bnorm2 > 0 ? sqrt(h.resid2 / h.bnorm2) : sqrt(h.resid2);
+    return h.status ? (esf_status)h.status : ESF_OK;
+  }
+  // mixed: FP32 blocks; x starts at 0 as in the assembled reference variant
+  convert_vec<double, float><<<vec_blocks(S * 243), VT, 0, st>>>(S * 243, blocks, w->blocks32);
+  ESF_CUDA(cudaMemsetAsync(x, 0, n * 8, st));
+  double bnorm2 = 0;
+  {
+    esf_status e0 = init_state(w->st, eps, maxIt, st);
+    if (e0) return e0;
+    vec_norm2<double><<<vec_blocks(n), VT, 0, st>>>(n, b, w->partial, &w->st->ticket[3],
+                                                    &w->st->bnorm2);
+    PcrState hb;
+    ESF_CUDA(cudaMemcpyAsync(&hb, w->st, sizeof hb, cudaMemcpyDeviceToHost, st));
+    ESF_CUDA(cudaStreamSynchronize(st));
+    bnorm2 = hb.bnorm2;
+  }
+  int total = 0, ref = 0, conv = 0;
+  double rel = 0;
+  esf_status status = ESF_OK;
+  for (ref = 0; ref <= maxRefine; ref++) {
+    init_state(w->st, eps, maxIt, st);
+    solid_spmv<double, S_RESID64><<<vec_blocks(S), VT, 0, st>>>(S, blocks, nbr, x, b, w->r,
+                                                                nullptr, w->b32, w->partial,
+                                                                w->st);
+    ESF_LAUNCH_CHECK();
+    PcrState h;
+    ESF_CUDA(cudaMemcpyAsync(&h, w->st, sizeof h, cudaMemcpyDeviceToHost, st));
+    ESF_CUDA(cudaStreamSynchronize(st));
+    rel = bnorm2 > 0 ? sqrt(h.resid2 / bnorm2) : sqrt(h.resid2);
+    if (!(h.resid2 == h.resid2)) {
+      status = ESF_ERR_NUMERIC;
+      break;
+    }
+    if (sqrt(h.resid2) < eps * sqrt(bnorm2)) {
+      conv = 1;
+      break;
+    }
+    if (ref == maxRefine || total >= maxIt) break;
+    PcrState hi;
+    esf_status e = solid_pcr<float>(S, w->blocks32, nbr, w->invd32, w->b32, w->x32, w->r32, w->d32,
+                                    w->Ap32, w->s32, w->partial, w->st32, innerEps, maxIt - total,
+                                    st, &hi, 1);
+    if (e) return e;
+    total += hi.iter;
+    if (hi.status) {
+      status = (esf_status)hi.status;
+      break;
+    }
+    add_correction<<<vec_blocks(n), VT, 0, st>>>(n, x, w->x32);
+  }
+  if (iters) *iters = total;
+  if (refinements) *refinements = ref;
+  if (relres) *relres = rel;
+  if (converged) *converged = conv;
+  return status;
+}
+
+}  // namespace esf

@@ -1,0 +1,1171 @@
+// Host orchestration of the coupled step and the C ABI of include/eulersf.h.
+// The order of operations follows COUPLED_INTEGRATOR_3D::stepImplicit
+// (COUPLED_INTEGRATOR_3D.cpp:377-636), pcrImplicitSolve (:662-764) and
+// finalizeSolution (:828-917); every array stays resident in HBM and the host
+// only reads back a handful of integers per step (bounding boxes, particle
+// and solid-node counts, the CFL speed).
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+#include <string>
+#include <vector>
+
+#include "esf_kernels.cuh"
+
+namespace esf {
+
+static thread_local char g_err[1024] = "";
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+}
+
+static int kblocks(long long n, int per = KT) {
+  long long b = (n + per - 1) / per;
+  if (b < 1) b = 1;
+  if (b > 152LL * 16) b = 152LL * 16;
+  return (int)b;
+}
+
+// grow-only device buffer
+struct DBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  esf_status ensure(size_t b) {
+    if (b <= bytes && p) return ESF_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    size_t nb = b + b / 4 + 256;
+    cudaError_t e = cudaMalloc(&p, nb);
+    if (e != cudaSuccess) {
+      set_error("cudaMalloc(%zu): %s", nb, cudaGetErrorString(e));
+      return ESF_ERR_OOM;
+    }
+    bytes = nb;
+    return ESF_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <typename T>
+  T* as() const {
+    return (T*)p;
+  }
+};
+
+struct Solid {
+  SolidDev d;
+  // host copies of the description
+  double rot[9], trans[3], scale[3], v0[3];
+  int nv = 0, ntri = 0;
+  std::vector<double> restPose;
+  std::vector<int> tris;
+  double *dRot = nullptr, *dVerts = nullptr, *dRest = nullptr, *dRestMass = nullptr;
+  int* dTris = nullptr;
+  // boxes (reference members _xmin.._zmax, _tightMin/_tightMax)
+  int ex[6];   // xmin ymin zmin xmax ymax zmax
+  int tmin[3], tmax[3];
+  double safeMin[3], safeMax[3];
+  // particles and valid-cell list
+  DBuf part, cellList, cellFlag, cellScan;
+  long long np = 0, nValid = 0;
+  double pmass = 0;
+};
+
+}  // namespace esf
+
+struct esf_scene {
+  GridDev g;
+  esf_params p;
+  cudaStream_t stream = nullptr;
+  bool ownStream = false;
+  int device = 0;
+  int ns = 0;
+  esf::Solid* s[ESF_MAX_SOLIDS] = {};
+  bool inited = false;
+  double fluidDensity = 1.0, defaultDt = 0.01, dt = 0.01, vortEps = 0.0;
+  // node fields
+  double *vel = nullptr, *vws = nullptr, *vort = nullptr, *intensity = nullptr, *ws = nullptr;
+  double *solidMass = nullptr, *nodeVF = nullptr, *quarter = nullptr, *minv = nullptr;
+  double *uf = nullptr, *mvf = nullptr, *vstar = nullptr, *v1 = nullptr, *pc = nullptr;
+  int *sdof = nullptr, *nodeFlag = nullptr, *nodeScan = nullptr;
+  // cell fields
+  double *lambda = nullptr, *jdiag = nullptr, *rhs = nullptr, *b1 = nullptr;
+  int* cellOrd = nullptr;
+  // solid unknowns (grow-only)
+  long long S = 0;
+  esf::DBuf sNode, solidF, solidMv, damped, solidV0, solidPC, solidB1, sysDiag, blocks, nbr, mask;
+  esf::DBuf Ke, nf, energy;
+  // scratch
+  esf::DBuf cubTmp, keys, vals, skeys, svals, bstart, bend, mt;
+  long long mtLen = 0;
+  int *dInts = nullptr, *hInts = nullptr;
+  unsigned long long* dU64 = nullptr;
+  unsigned long long* hU64 = nullptr;
+  esf::PressureWork* pw = nullptr;
+  esf::SolidWork* sw = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int status = 0;
+};
+
+using namespace esf;
+
+#define TRY(x)                   \
+  do {                           \
+    esf_status _s = (x);         \
+    if (_s != ESF_OK) return _s; \
+  } while (0)
+
+extern "C" {
+
+int esf_abi_version(void) { return ESF_ABI_VERSION; }
+const char* esf_last_error(void) { return esf::g_err; }
+
+esf_status esf_params_default(const esf_grid* g, esf_params* p) {
+  if (!g || !p) return ESF_ERR_INVALID_ARG;
+  memset(p, 0, sizeof *p);
+  p->dt = 0.01;
+  p->fluid_density = 1.0;
+  p->vorticity_eps = 2.0;
+  p->buoyancy = 0.1;
+  p->gravity = 0.0;
+  p->implicit_solver_eps = 1e-8;
+  p->div_free_solver_eps = 1e-8;
+  p->cr_max_iterations = 10;
+  p->mass_sample_dh = g->dh / 10;
+  p->tight_border = 3;
+  p->extrapolation_cells = 20;
+  p->particles_per_cell = 8;
+  p->flip_alpha = 0.95;
+  p->contact_safe_distance = g->dh * 0.5;
+  p->wall_thickness = g->dh * 1.5;
+  p->contact_spring_stiffness = 10000;
+  p->friction = 0.5;
+  p->flip_cutoff = 3;
+  p->precision = ESF_FP64;
+  p->inner_eps = 1e-4;
+  p->max_refinements = 50;
+  return ESF_OK;
+}
+
+}  // extern "C"
+
+static esf_status dalloc(void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes ? bytes : 8);
+  if (e != cudaSuccess) {
+    set_error("cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    return ESF_ERR_OOM;
+  }
+  return ESF_OK;
+}
+
+extern "C" esf_status esf_create(const esf_grid* g, const esf_params* p, void* stream,
+                                 esf_scene** out) {
+  if (!g || !p || !out) {
+    set_error("esf_create: null argument");
+    return ESF_ERR_INVALID_ARG;
+  }
+  *out = nullptr;
+  if (g->xRes < 4 || g->yRes < 4 || g->zRes < 4 || !(g->dh > 0)) {
+    set_error("esf_create: grid must have >= 4 nodes per axis and dh > 0");
+    return ESF_ERR_INVALID_ARG;
+  }
+  if ((long long)g->xRes * g->yRes * g->zRes * 8 >= (1LL << 31)) {
+    set_error("esf_create: grid too large for 32-bit solid/particle indices");
+    return ESF_ERR_UNSUPPORTED;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    set_error("esf_create: no CUDA device");
+    return ESF_ERR_NO_DEVICE;
+  }
+  esf_scene* s = new esf_scene();
+  cudaGetDevice(&s->device);
+  GridDev& G = s->g;
+  G.X = g->xRes;
+  G.Y = g->yRes;
+  G.Z = g->zRes;
+  G.slab = (long long)G.X * G.Y;
+  G.T = G.slab * G.Z;
+  G.cX = G.X - 1;
+  G.cY = G.Y - 1;
+  G.cZ = G.Z - 1;
+  G.cslab = (long long)G.cX * G.cY;
+  G.R = G.cslab * G.cZ;
+  G.dh = g->dh;
+  G.dhInv = 1.0 / g->dh;
+  for (int k = 0; k < 3; k++) G.o[k] = g->origin[k];
+  s->p = *p;
+  s->defaultDt = s->dt = p->dt;
+  int maxRes = G.X > G.Y ? (G.X > G.Z ? G.X : G.Z) : (G.Y > G.Z ? G.Y : G.Z);
+  double scaling = 64.0f / maxRes;
+  scaling = (scaling < 1.0f) ? 1.0f : scaling;
+  s->vortEps = p->vorticity_eps / scaling;  // COUPLED_INTEGRATOR_3D.cpp:67-71
+  if (stream) {
+    s->stream = (cudaStream_t)stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete s;
+      set_error("cudaStreamCreate failed");
+      return ESF_ERR_CUDA;
+    }
+    s->ownStream = true;
+  }
+  const size_t T = G.T, R = G.R;
+  esf_status e = ESF_OK;
+#define A(ptr, bytes) \
+  if (!e) e = dalloc((void**)&s->ptr, bytes)
+  A(vel, T * 24);
+  A(vws, T * 24);
+  A(vort, T * 24);
+  A(intensity, T * 8);
+  A(ws, T * 8);
+  A(solidMass, T * 8);
+  A(nodeVF, T * 8);
+  A(quarter, T * 64);
+  A(minv, T * 8);
+  A(uf, T * 24);
+  A(mvf, T * 24);
+  A(vstar, T * 24);
+  A(v1, T * 24);
+  A(pc, T * 24);
+  A(sdof, T * 4);
+  A(nodeFlag, T * 4);
+  A(nodeScan, T * 4);
+  A(lambda, R * 8);
+  A(jdiag, R * 8);
+  A(rhs, R * 8);
+  A(b1, R * 8);
+  A(cellOrd, R * 4);
+  A(dInts, 64 * 4);
+  A(dU64, 16 * 8);
+#undef A
+  if (!e && cudaMallocHost(&s->hInts, 64 * 4) != cudaSuccess) e = ESF_ERR_OOM;
+  if (!e && cudaMallocHost(&s->hU64, 16 * 8) != cudaSuccess) e = ESF_ERR_OOM;
+  if (!e) {
+    // zero-initialised like the reference's Eigen/vector fields
+    cudaMemsetAsync(s->vel, 0, T * 24, s->stream);
+    cudaMemsetAsync(s->vws, 0, T * 24, s->stream);
+    cudaMemsetAsync(s->vort, 0, T * 24, s->stream);
+    cudaMemsetAsync(s->intensity, 0, T * 8, s->stream);
+    cudaMemsetAsync(s->ws, 0, T * 8, s->stream);
+    cudaMemsetAsync(s->solidMass, 0, T * 8, s->stream);
+    cudaMemsetAsync(s->nodeVF, 0, T * 8, s->stream);
+    cudaMemsetAsync(s->uf, 0, T * 24, s->stream);
+    cudaMemsetAsync(s->mvf, 0, T * 24, s->stream);
+    cudaMemsetAsync(s->vstar, 0, T * 24, s->stream);
+    cudaMemsetAsync(s->v1, 0, T * 24, s->stream);
+    cudaMemsetAsync(s->pc, 0, T * 24, s->stream);
+    cudaMemsetAsync(s->lambda, 0, R * 8, s->stream);
+    cudaMemsetAsync(s->jdiag, 0, R * 8, s->stream);
+    cudaMemsetAsync(s->rhs, 0, R * 8, s->stream);
+    cudaMemsetAsync(s->b1, 0, R * 8, s->stream);
+    e = pressure_work_alloc(&s->pw, G, p->precision == ESF_MIXED);
+  }
+  if (!e && cudaEventCreate(&s->e0) != cudaSuccess) e = ESF_ERR_CUDA;
+  if (!e && cudaEventCreate(&s->e1) != cudaSuccess) e = ESF_ERR_CUDA;
+  if (e) {
+    esf_destroy(s);
+    return e;
+  }
+  *out = s;
+  return ESF_OK;
+}
+
+static void free_solid(Solid* d) {
+  if (!d) return;
+  SolidDev& x = d->d;
+  cudaFree(x.X); cudaFree(x.u); cudaFree(x.vel); cudaFree(x.vws); cudaFree(x.tmp3);
+  cudaFree(x.mass); cudaFree(x.phi); cudaFree(x.detFInv); cudaFree(x.quarter); cudaFree(x.valid);
+  cudaFree(d->dRot); cudaFree(d->dVerts); cudaFree(d->dRest); cudaFree(d->dRestMass); cudaFree(d->dTris);
+  d->part.release(); d->cellList.release(); d->cellFlag.release(); d->cellScan.release();
+  delete d;
+}
+
+extern "C" esf_status esf_destroy(esf_scene* s) {
+  if (!s) return ESF_OK;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  for (int i = 0; i < s->ns; i++) free_solid(s->s[i]);
+  double* d64[] = {s->vel, s->vws, s->vort, s->intensity, s->ws, s->solidMass, s->nodeVF, s->quarter,
+                   s->minv, s->uf, s->mvf, s->vstar, s->v1, s->pc, s->lambda, s->jdiag, s->rhs, s->b1};
+  for (double* p : d64) cudaFree(p);
+  cudaFree(s->sdof); cudaFree(s->nodeFlag); cudaFree(s->nodeScan); cudaFree(s->cellOrd);
+  cudaFree(s->dInts); cudaFree(s->dU64);
+  if (s->hInts) cudaFreeHost(s->hInts);
+  if (s->hU64) cudaFreeHost(s->hU64);
+  DBuf* bufs[] = {&s->sNode, &s->solidF, &s->solidMv, &s->damped, &s->solidV0, &s->solidPC,
+                  &s->solidB1, &s->sysDiag, &s->blocks, &s->nbr, &s->mask, &s->Ke, &s->nf,
+                  &s->energy, &s->cubTmp, &s->keys, &s->vals, &s->skeys, &s->svals, &s->bstart,
+                  &s->bend, &s->mt};
+  for (DBuf* b : bufs) b->release();
+  pressure_work_free(s->pw);
+  solid_work_free(s->sw);
+  if (s->e0) cudaEventDestroy(s->e0);
+  if (s->e1) cudaEventDestroy(s->e1);
+  if (s->ownStream && s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return ESF_OK;
+}
+
+extern "C" esf_status esf_add_solid(esf_scene* sc, const esf_solid_desc* dd) {
+  if (!sc || !dd) {
+    set_error("esf_add_solid: null argument");
+    return ESF_ERR_INVALID_ARG;
+  }
+  if (sc->inited || sc->ns >= ESF_MAX_SOLIDS) {
+    set_error("esf_add_solid: scene already initialised or too many solids");
+    return ESF_ERR_STATE;
+  }
+  if (!dd->rest_mass || dd->mass_res[0] < 2 || dd->mass_res[1] < 2 || dd->mass_res[2] < 2 ||
+      !(dd->mass_dh > 0) || dd->num_vertices <= 0 || !dd->vertices || dd->num_triangles <= 0 ||
+      !dd->triangles) {
+    set_error("esf_add_solid: invalid rest mass grid or mesh");
+    return ESF_ERR_INVALID_ARG;
+  }
+  for (long long t = 0; t < 3LL * dd->num_triangles; t++)
+    if (dd->triangles[t] < 0 || dd->triangles[t] >= dd->num_vertices) {
+      set_error("esf_add_solid: triangle index out of range");
+      return ESF_ERR_INVALID_ARG;
+    }
+  const GridDev& G = sc->g;
+  Solid* d = new Solid();
+  SolidDev& x = d->d;
+  memset(&x, 0, sizeof x);
+  const size_t T = G.T;
+  esf_status e = ESF_OK;
+#define A(ptr, bytes) \
+  if (!e) e = dalloc((void**)&(ptr), bytes)
+  A(x.X, T * 24);
+  A(x.u, T * 24);
+  A(x.vel, T * 24);
+  A(x.vws, T * 24);
+  A(x.tmp3, T * 24);
+  A(x.mass, T * 8);
+  A(x.phi, T * 8);
+  A(x.detFInv, T * 8);
+  A(x.quarter, T * 64);
+  A(x.valid, G.R);
+  size_t mn = (size_t)dd->mass_res[0] * dd->mass_res[1] * dd->mass_res[2];
+  A(d->dRestMass, mn * 8);
+  A(d->dRot, 9 * 8);
+  A(d->dVerts, (size_t)dd->num_vertices * 24);
+  A(d->dRest, (size_t)dd->num_vertices * 24);
+  A(d->dTris, (size_t)dd->num_triangles * 12);
+#undef A
+  if (e) {
+    free_solid(d);
+    return e;
+  }
+  cudaStream_t st = sc->stream;
+  for (int k = 0; k < 3; k++) {
+    x.mres[k] = dd->mass_res[k];
+    x.morig[k] = dd->mass_origin[k];
+    d->trans[k] = dd->translation[k];
+    d->scale[k] = dd->scaling[k];
+    d->v0[k] = dd->initial_velocity[k];
+  }
+  memcpy(d->rot, dd->rotation, sizeof d->rot);
+  x.mdh = dd->mass_dh;
+  x.rest = d->dRestMass;
+  x.lambda = dd->lambda;
+  x.mu = dd->mu;
+  x.qcm = dd->density * G.dh * G.dh * G.dh * 0.125;  // setMassDensity (DEFOR_SOLID_3D.h:64-66)
+  x.G = 0.25 * G.dhInv;
+  x.dt = sc->p.dt;
+  d->pmass = (x.qcm / (G.dh * G.dh * G.dh * 0.125)) * (G.dh * G.dh * G.dh / sc->p.particles_per_cell);
+  ESF_CUDA(cudaMemcpy(d->dRestMass, dd->rest_mass, mn * 8, cudaMemcpyHostToDevice));
+  ESF_CUDA(cudaMemcpy(d->dRot, d->rot, 72, cudaMemcpyHostToDevice));
+  d->nv = dd->num_vertices;
+  d->ntri = dd->num_triangles;
+  d->restPose.assign(dd->vertices, dd->vertices + 3 * d->nv);
+  d->tris.assign(dd->triangles, dd->triangles + 3 * d->ntri);
+  // current pose: OBJ::scale, transformMesh, translateMesh (main.cpp:150-154)
+  std::vector<double> cur(3 * d->nv);
+  for (int v = 0; v < d->nv; v++) {
+    double pp[3], q[3];
+    for (int k = 0; k < 3; k++) pp[k] = d->restPose[3 * v + k] * d->scale[k];
+    for (int i = 0; i < 3; i++) q[i] = (d->rot[i * 3 + 0] * pp[0] + d->rot[i * 3 + 1] * pp[1]) + d->rot[i * 3 + 2] * pp[2];
+    for (int k = 0; k < 3; k++) cur[3 * v + k] = q[k] + d->trans[k];
+  }
+  ESF_CUDA(cudaMemcpy(d->dVerts, cur.data(), cur.size() * 8, cudaMemcpyHostToDevice));
+  ESF_CUDA(cudaMemcpy(d->dRest, d->restPose.data(), cur.size() * 8, cudaMemcpyHostToDevice));
+  ESF_CUDA(cudaMemcpy(d->dTris, d->tris.data(), d->tris.size() * 4, cudaMemcpyHostToDevice));
+  for (int k = 0; k < 3; k++) d->safeMin[k] = G.o[k] + 2 * G.dh;
+  d->safeMax[0] = G.o[0] + (G.X - 3) * G.dh;
+  d->safeMax[1] = G.o[1] + (G.Y - 3) * G.dh;
+  d->safeMax[2] = G.o[2] + (G.Z - 3) * G.dh;
+  ESF_CUDA(cudaMemsetAsync(x.vws, 0, T * 24, st));
+  ESF_CUDA(cudaMemsetAsync(x.tmp3, 0, T * 24, st));
+  ESF_CUDA(cudaMemsetAsync(x.mass, 0, T * 8, st));
+  ESF_CUDA(cudaMemsetAsync(x.phi, 0, T * 8, st));
+  ESF_CUDA(cudaMemsetAsync(x.detFInv, 0, T * 8, st));
+  ESF_CUDA(cudaMemsetAsync(x.quarter, 0, T * 64, st));
+  ESF_CUDA(cudaMemsetAsync(x.valid, 0, G.R, st));
+  k_initial_state<<<kblocks(G.T), KT, 0, st>>>(G, x, d->dRot, d->trans[0], d->trans[1], d->trans[2],
+                                               d->scale[0], d->scale[1], d->scale[2], d->v0[0],
+                                               d->v0[1], d->v0[2]);
+  ESF_LAUNCH_CHECK();
+  ESF_CUDA(cudaStreamSynchronize(st));
+  sc->s[sc->ns++] = d;
+  return ESF_OK;
+}
+
+extern "C" esf_status esf_set_fluid(esf_scene* s, double density, double viscosity) {
+  if (!s) return ESF_ERR_INVALID_ARG;
+  (void)viscosity;  // stored but unused by the reference (COUPLED_INTEGRATOR_3D.cpp:46)
+  s->fluidDensity = density;
+  return ESF_OK;
+}
+extern "C" esf_status esf_set_max_dt(esf_scene* s, double max_dt) {
+  if (!s) return ESF_ERR_INVALID_ARG;
+  s->defaultDt = max_dt;
+  return ESF_OK;
+}
+extern "C" double esf_dt(const esf_scene* s) { return s ? s->dt : 0.0; }
+
+// ------------------------------------------------------------ step pieces
+static Box mkbox(int x0, int y0, int z0, int x1, int y1, int z1) {
+  Box b;
+  b.lo[0] = x0;
+  b.lo[1] = y0;
+  b.lo[2] = z0;
+  b.hi[0] = x1;
+  b.hi[1] = y1;
+  b.hi[2] = z1;
+  return b;
+}
+static long long boxn(const Box& b) {
+  long long n = 1;
+  for (int k = 0; k < 3; k++) n *= (b.hi[k] > b.lo[k]) ? (b.hi[k] - b.lo[k]) : 0;
+  return n;
+}
+
+// computeSolidMass (DEFOR_SOLID_3D.cpp:576-669)
+static esf_status compute_solid_mass(esf_scene* sc, Solid* d, int usesdf) {
+  const GridDev& G = sc->g;
+  cudaStream_t st = sc->stream;
+  SolidDev& x = d->d;
+  ESF_CUDA(cudaMemsetAsync(x.mass, 0, G.T * 8, st));
+  ESF_CUDA(cudaMemsetAsync(x.valid, 0, G.R, st));
+  ESF_CUDA(cudaMemsetAsync(x.detFInv, 0, G.T * 8, st));
+  ESF_CUDA(cudaMemsetAsync(x.quarter, 0, G.T * 64, st));
+  Box cells = mkbox(d->tmin[0], d->tmin[1], d->tmin[2], d->tmax[0] - 1, d->tmax[1] - 1, d->tmax[2] - 1);
+  Box nodes = mkbox(d->tmin[0], d->tmin[1], d->tmin[2], d->tmax[0], d->tmax[1], d->tmax[2]);
+  long long nc = boxn(cells);
+  if (nc <= 0) return ESF_OK;
+  const double subDh = sc->p.mass_sample_dh;
+  const int res = (int)(G.dh / subDh);
+  k_det_finv<<<kblocks(nc), KT, 0, st>>>(G, x, cells);
+  k_mass_subsample<<<kblocks(nc, 128), 128, 0, st>>>(G, x, cells, usesdf, subDh, res);
+  k_mass_gather<<<kblocks(boxn(nodes)), KT, 0, st>>>(G, x, cells, nodes);
+  ESF_LAUNCH_CHECK();
+  return ESF_OK;
+}
+
+// computeSDF (DEFOR_SOLID_3D.cpp:216-268): phi, the boxes, 2 x sweepPhi.
+static esf_status compute_sdf(esf_scene* sc, Solid* d) {
+  const GridDev& G = sc->g;
+  cudaStream_t st = sc->stream;
+  int init[6] = {G.X, G.Y, G.Z, 0, 0, 0};
+  memcpy(sc->hInts, init, sizeof init);
+  ESF_CUDA(cudaMemcpyAsync(sc->dInts, sc->hInts, sizeof init, cudaMemcpyHostToDevice, st));
+  double large = G.X + G.Y + G.Z + 2;
+  k_phi_init<<<kblocks(G.T), KT, 0, st>>>(G, d->d, large, sc->dInts);
+  ESF_LAUNCH_CHECK();
+  ESF_CUDA(cudaMemcpyAsync(sc->hInts, sc->dInts, sizeof init, cudaMemcpyDeviceToHost, st));
+  ESF_CUDA(cudaStreamSynchronize(st));
+  int xmin = sc->hInts[0], ymin = sc->hInts[1], zmin = sc->hInts[2];
+  int xmax = sc->hInts[3], ymax = sc->hInts[4], zmax = sc->hInts[5];
+  int tb = sc->p.tight_border, exn = sc->p.extrapolation_cells;
+  d->tmin[0] = std::max(xmin - tb, 0);
+  d->tmin[1] = std::max(ymin - tb, 0);
+  d->tmin[2] = std::max(zmin - tb, 0);
+  d->tmax[0] = std::min(xmax + tb, G.X);
+  d->tmax[1] = std::min(ymax + tb, G.Y);
+  d->tmax[2] = std::min(zmax + tb, G.Z);
+  d->ex[0] = std::max(xmin - exn, 0);
+  d->ex[1] = std::max(ymin - exn, 0);
+  d->ex[2] = std::max(zmin - exn, 0);
+  d->ex[3] = std::min(xmax + exn, G.X);
+  d->ex[4] = std::min(ymax + exn, G.Y);
+  d->ex[5] = std::min(zmax + exn, G.Z);
+  Box ex = mkbox(d->ex[0], d->ex[1], d->ex[2], d->ex[3], d->ex[4], d->ex[5]);
+  k_sweep_phi<<<1, 1024, 0, st>>>(G, d->d, ex, 2);
+  ESF_LAUNCH_CHECK();
+  return ESF_OK;
+}
+
+// MT19937 stream shared by every initMaterialParticles call (the reference
+// re-seeds a fresh MERSENNETWISTER with 123456 each time, MERSENNETWISTER.h:259-262).
+static esf_status ensure_mt(esf_scene* sc, long long need) {
+  if (need <= sc->mtLen) return ESF_OK;
+  long long len = need + need / 2 + 1024;
+  std::vector<uint32_t> h(len);
+  uint32_t mt[624];
+  mt[0] = 123456u;
+  for (int i = 1; i < 624; i++) mt[i] = 1812433253u * (mt[i - 1] ^ (mt[i - 1] >> 30)) + (uint32_t)i;
+  int idx = 624;
+  for (long long k = 0; k < len; k++) {
+    if (idx >= 624) {
+      for (int i = 0; i < 624; i++) {
+        uint32_t y = (mt[i] & 0x80000000u) | (mt[(i + 1) % 624] & 0x7fffffffu);
+        mt[i] = mt[(i + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+      }
+      idx = 0;
+    }
+    uint32_t y = mt[idx++];
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= y >> 18;
+    h[k] = y;
+  }
+  TRY(sc->mt.ensure(len * 4));
+  ESF_CUDA(cudaMemcpyAsync(sc->mt.p, h.data(), len * 4, cudaMemcpyHostToDevice, sc->stream));
+  ESF_CUDA(cudaStreamSynchronize(sc->stream));
+  sc->mtLen = len;
+  return ESF_OK;
+}
+
+// valid==1 cells of the tight box in z,y,x order (list + per-cell ordinal)
+static esf_status collect_valid_cells(esf_scene* sc, Solid* d) {
+  const GridDev& G = sc->g;
+  cudaStream_t st = sc->stream;
+  Box cells = mkbox(d->tmin[0], d->tmin[1], d->tmin[2], d->tmax[0] - 1, d->tmax[1] - 1, d->tmax[2] - 1);
+  long long nc = boxn(cells);
+  d->nValid = 0;
+  if (nc <= 0) return ESF_OK;
+  TRY(d->cellFlag.ensure(nc * 4));
+  TRY(d->cellScan.ensure((nc + 1) * 4));
+  k_flag_valid_cells<<<kblocks(nc), KT, 0, st>>>(G, d->d, cells, d->cellFlag.as<int>());
+  size_t tb = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, tb, d->cellFlag.as<int>(), d->cellScan.as<int>(), (int)nc, st);
+  TRY(sc->cubTmp.ensure(tb));
+  cub::DeviceScan::ExclusiveSum(sc->cubTmp.p, tb, d->cellFlag.as<int>(), d->cellScan.as<int>(), (int)nc, st);
+  ESF_CUDA(cudaMemcpyAsync(&sc->hInts[0], d->cellScan.as<int>() + nc - 1, 4, cudaMemcpyDeviceToHost, st));
+  ESF_CUDA(cudaMemcpyAsync(&sc->hInts[1], d->cellFlag.as<int>() + nc - 1, 4, cudaMemcpyDeviceToHost, st));
+  ESF_CUDA(cudaStreamSynchronize(st));
+  d->nValid = (long long)sc->hInts[0] + sc->hInts[1];
+  TRY(d->cellList.ensure((d->nValid + 1) * 8));
+  k_collect_valid_cells<<<kblocks(nc), KT, 0, st>>>(G, cells, d->cellFlag.as<int>(), d->cellScan.as<int>(),
+                                                    d->cellList.as<long long>());
+  ESF_LAUNCH_CHECK();
+  return ESF_OK;
+}
+
+// initMaterialParticles (DEFOR_SOLID_3D.cpp:333-367)
+static esf_status init_particles(esf_scene* sc, Solid* d) {
+  TRY(collect_valid_cells(sc, d));
+  const int ppc = sc->p.particles_per_cell;
+  d->np = d->nValid * ppc;
+  if (d->np == 0) return ESF_OK;
+  TRY(ensure_mt(sc, 3 * d->np));
+  TRY(d->part.ensure(d->np * 80));
+  k_seed_particles<<<kblocks(d->np), KT, 0, sc->stream>>>(sc->g, d->d, d->cellList.as<long long>(),
+                                                           d->nValid, ppc, sc->mt.as<uint32_t>(),
+                                                           d->pmass, d->part.as<double>());
+  ESF_LAUNCH_CHECK();
+  return ESF_OK;
+}
+
+static esf_status advect_mesh(esf_scene* sc, Solid* d) {
+  k_advect_mesh<<<kblocks(d->nv), KT, 0, sc->stream>>>(sc->g, d->d, d->nv, d->dVerts, d->dRest);
+  ESF_LAUNCH_CHECK();
+  return ESF_OK;
+}
+
+// gatherSolidMasses (COUPLED_INTEGRATOR_3D.cpp:327-375)
+static esf_status gather_solid_masses(esf_scene* sc) {
+  const GridDev& G = sc->g;
+  cudaStream_t st = sc->stream;
+  for (int i = 0; i < sc->ns; i++)
+    k_gather_accumulate<<<kblocks(G.T), KT, 0, st>>>(G, sc->s[i]->d, i == 0, sc->solidMass, sc->quarter);
+  k_node_vf<<<kblocks(G.T), KT, 0, st>>>(G, sc->quarter, sc->solidMass, sc->nodeVF, sc->nodeFlag);
+  size_t tb = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, tb, sc->nodeFlag, sc->nodeScan, (int)G.T, st);
+  TRY(sc->cubTmp.ensure(tb));
+  cub::DeviceScan::ExclusiveSum(sc->cubTmp.p, tb, sc->nodeFlag, sc->nodeScan, (int)G.T, st);
+  ESF_CUDA(cudaMemcpyAsync(&sc->hInts[0], sc->nodeScan + G.T - 1, 4, cudaMemcpyDeviceToHost, st));
+  ESF_CUDA(cudaMemcpyAsync(&sc->hInts[1], sc->nodeFlag + G.T - 1, 4, cudaMemcpyDeviceToHost, st));
+  ESF_CUDA(cudaStreamSynchronize(st));
+  long long S = (long long)sc->hInts[0] + sc->hInts[1];
+  TRY(sc->sNode.ensure((S + 1) * 8));
+  k_sdof<<<kblocks(G.T), KT, 0, st>>>(G, sc->nodeFlag, sc->nodeScan, sc->sdof, sc->sNode.as<long long>());
+  ESF_LAUNCH_CHECK();
+  sc->S = S;
+  return ESF_OK;
+}
+
+static esf_status recover_velocity(esf_scene* sc) {
+  for (int i = 0; i < sc->ns; i++) {
+    Solid* d = sc->s[i];
+    Box b = mkbox(d->ex[0], d->ex[1], d->ex[2], d->ex[3] - 1, d->ex[4] - 1, d->ex[5] - 1);
+    if (boxn(b) > 0)
+      k_recover_velocity<<<kblocks(boxn(b)), KT, 0, sc->stream>>>(sc->g, d->d, b, sc->vel);
+  }
+  ESF_LAUNCH_CHECK();
+  return ESF_OK;
+}
+
+extern "C" esf_status esf_init(esf_scene* sc) {
+  if (!sc) return ESF_ERR_INVALID_ARG;
+  if (sc->inited || sc->ns == 0) {
+    set_error("esf_init: needs at least one solid and may run once");
+    return ESF_ERR_STATE;
+  }
+  if (!(sc->p.mass_sample_dh > 0) || (int)(sc->g.dh / sc->p.mass_sample_dh) < 1 ||
+      sc->p.particles_per_cell < 1) {
+    set_error("esf_init: invalid mass sample dh or particle count");
+    return ESF_ERR_INVALID_ARG;
+  }
+  cudaSetDevice(sc->device);
+  const GridDev& G = sc->g;
+  // DEFOR_SOLID_3D::init (DEFOR_SOLID_3D.cpp:269-331)
+  for (int i = 0; i < sc->ns; i++) {
+    Solid* d = sc->s[i];
+    d->ex[0] = d->ex[1] = d->ex[2] = 0;
+    d->ex[3] = G.X;
+    d->ex[4] = G.Y;
+    d->ex[5] = G.Z;
+    d->tmin[0] = d->tmin[1] = d->tmin[2] = 0;
+    d->tmax[0] = G.X;
+    d->tmax[1] = G.Y;
+    d->tmax[2] = G.Z;
+    TRY(compute_solid_mass(sc, d, 0));
+    TRY(compute_sdf(sc, d));
+    TRY(init_particles(sc, d));
+    TRY(advect_mesh(sc, d));
+  }
+  TRY(gather_solid_masses(sc));
+  TRY(recover_velocity(sc));
+  ESF_CUDA(cudaStreamSynchronize(sc->stream));
+  sc->inited = true;
+  return ESF_OK;
+}
+
+static double u64_to_double(unsigned long long b) {
+  b = (b >> 63) ? (b & 0x7fffffffffffffffull) : ~b;
+  double d;
+  memcpy(&d, &b, 8);
+  return d;
+}
+
+// stiffness + computeMV + assembly (DEFOR_SOLID_3D.cpp:697-889;
+// COUPLED_INTEGRATOR_3D.cpp:432-437, 609-620 for the assembly)
+static esf_status solid_system(esf_scene* sc, double* energyOut) {
+  const GridDev& G = sc->g;
+  cudaStream_t st = sc->stream;
+  const long long S = sc->S;
+  TRY(sc->solidF.ensure((3 * S + 1) * 8));
+  TRY(sc->solidMv.ensure((3 * S + 1) * 8));
+  TRY(sc->damped.ensure((3 * S + 1) * 8));
+  TRY(sc->solidV0.ensure((3 * S + 1) * 8));
+  TRY(sc->solidPC.ensure((3 * S + 1) * 8));
+  TRY(sc->solidB1.ensure((3 * S + 1) * 8));
+  TRY(sc->sysDiag.ensure((3 * S + 1) * 8));
+  TRY(sc->blocks.ensure((243 * S + 1) * 8));
+  TRY(sc->nbr.ensure((27 * S + 1) * 4));
+  TRY(sc->mask.ensure((S + 1) * 4));
+  ESF_CUDA(cudaMemsetAsync(sc->solidF.p, 0, 3 * S * 8 + 8, st));
+  ESF_CUDA(cudaMemsetAsync(sc->solidMv.p, 0, 3 * S * 8 + 8, st));
+  ESF_CUDA(cudaMemsetAsync(sc->damped.p, 0, 3 * S * 8 + 8, st));
+  ESF_CUDA(cudaMemsetAsync(sc->mask.p, 0, S * 4 + 4, st));
+  const int EB = 4096;
+  TRY(sc->energy.ensure(EB * 3 * 8));
+  ESF_CUDA(cudaMemsetAsync(sc->energy.p, 0, EB * 3 * 8, st));
+  double* ePart = sc->energy.as<double>();
+  // one solid: its valid-cell list is the one the particles were seeded from
+  if (sc->ns != 1 && S > 0) {
+    set_error("solid_system: scenes with more than one solid are not supported yet");
+    return ESF_ERR_UNSUPPORTED;
+  }
+  for (int i = 0; i < sc->ns; i++) {
+    Solid* d = sc->s[i];
+    ESF_CUDA(cudaMemsetAsync(sc->cellOrd, 0xff, G.R * 4, st));
+    long long nc = d->nValid;
+    TRY(sc->Ke.ensure((576 * nc + 1) * 8));
+    TRY(sc->nf.ensure((24 * nc + 1) * 8));
+    if (nc > 0) {
+      k_element_stiffness<<<kblocks(nc, 128), 128, 0, st>>>(G, d->d, d->cellList.as<long long>(), nc,
+                                                             sc->Ke.as<double>(), sc->nf.as<double>(),
+                                                             ePart);
+      // cell -> ordinal in the valid list
+      k_cell_ord_fill<<<kblocks(nc), KT, 0, st>>>(G, d->cellList.as<long long>(), nc, sc->cellOrd);
+    }
+    Box b = mkbox(d->ex[0], d->ex[1], d->ex[2], d->ex[3] - 1, d->ex[4] - 1, d->ex[5] - 1);
+    if (boxn(b) > 0 && S > 0)
+      k_compute_mv<<<std::min(kblocks(boxn(b)), EB), KT, 0, st>>>(G, d->d, b, sc->sdof,
+                                                                  sc->solidMv.as<double>(), ePart + EB);
+    ESF_LAUNCH_CHECK();
+  }
+  *energyOut = 0;
+  return ESF_OK;
+}
+
+static double sum_partials(esf_scene* sc, int n) {
+  std::vector<double> h(n);
+  // the scene stream is non-blocking: copy on it, then wait for it
+  cudaMemcpyAsync(h.data(), sc->energy.p, n * 8, cudaMemcpyDeviceToHost, sc->stream);
+  cudaStreamSynchronize(sc->stream);
+  double a = 0;
+  for (double v : h) a += v;
+  return a;
+}
+
+extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
+  if (!sc) return ESF_ERR_INVALID_ARG;
+  if (!sc->inited) {
+    set_error("esf_step: call esf_init first");
+    return ESF_ERR_STATE;
+  }
+  cudaSetDevice(sc->device);
+  const GridDev& G = sc->g;
+  cudaStream_t st = sc->stream;
+  sc->status = ESF_OK;
+  ESF_CUDA(cudaEventRecord(sc->e0, st));
+  // ---- broad phase (COUPLED_INTEGRATOR_3D.cpp:378-411)
+  int prone = 0;
+  for (int i = 0; i < sc->ns && !prone; i++) {
+    Solid* d = sc->s[i];
+    unsigned long long init[6] = {~0ull, ~0ull, ~0ull, 0, 0, 0};
+    memcpy(sc->hU64, init, sizeof init);
+    ESF_CUDA(cudaMemcpyAsync(sc->dU64, sc->hU64, sizeof init, cudaMemcpyHostToDevice, st));
+    k_mesh_aabb<<<kblocks(3LL * d->ntri), KT, 0, st>>>(d->ntri, d->dTris, d->dVerts, sc->dU64);
+    ESF_CUDA(cudaMemcpyAsync(sc->hU64, sc->dU64, sizeof init, cudaMemcpyDeviceToHost, st));
+    ESF_CUDA(cudaStreamSynchronize(st));
+    double mn[3], mx[3];
+    for (int k = 0; k < 3; k++) {
+      mn[k] = u64_to_double(sc->hU64[k]);
+      mx[k] = u64_to_double(sc->hU64[3 + k]);
+    }
+    bool inside = true;
+    for (int k = 0; k < 3; k++)
+      if (mn[k] < d->safeMin[k] || mn[k] > d->safeMax[k] || mx[k] < d->safeMin[k] || mx[k] > d->safeMax[k])
+        inside = false;
+    if (!inside) prone = 1;
+  }
+  if (!prone && sc->ns > 1) {
+    set_error("esf_step: solid-solid broad phase is not supported yet");
+    return ESF_ERR_UNSUPPORTED;
+  }
+  // CFL (:88-102)
+  sc->hU64[0] = 0;
+  ESF_CUDA(cudaMemcpyAsync(sc->dU64, sc->hU64, 8, cudaMemcpyHostToDevice, st));
+  k_cfl_vmax<<<kblocks(G.T), KT, 0, st>>>(G, sc->vel, sc->solidMass, sc->dU64);
+  ESF_CUDA(cudaMemcpyAsync(sc->hU64, sc->dU64, 8, cudaMemcpyDeviceToHost, st));
+  ESF_CUDA(cudaStreamSynchronize(st));
+  {
+    double vm;
+    memcpy(&vm, sc->hU64, 8);
+    double alpha = prone ? 0.6 : 1.8;
+    double dt = 1e9;
+    if (sc->S > 0) {
+      double vmax = vm * G.dhInv;
+      double c = alpha / vmax;
+      dt = (c < dt) ? c : dt;
+    }
+    sc->dt = (sc->defaultDt < dt) ? sc->defaultDt : dt;
+  }
+  const double dt = sc->dt;
+  const long long S = sc->S;
+  // ---- solid forces, stiffness, mv
+  double e_unused;
+  TRY(solid_system(sc, &e_unused));
+  const int EB = 4096;
+  double* ePart = sc->energy.as<double>();
+  // ---- vorticity + body forces (:442-606)
+  ESF_CUDA(cudaMemsetAsync(sc->ws, 0, G.T * 8, st));
+  if (sc->vortEps > 0) k_vorticity<<<kblocks(G.T), KT, 0, st>>>(G, sc->nodeVF, sc->vel, sc->vort, sc->ws);
+  // The reference adds the stiffness forces before the body forces, so the
+  // block/force gather runs first; the damped mass it needs for the diagonal
+  // comes from the body-force kernel and is added afterwards.
+  BodyParams bp;
+  bp.fluidDensity = sc->fluidDensity;
+  bp.gravity = sc->p.gravity;
+  bp.buoyancy = sc->p.buoyancy;
+  bp.damp = 1 + dt * sc->p.rayleigh_alpha;
+  bp.vortEps = sc->vortEps;
+  bp.dt = dt;
+  const double scale = dt * dt + sc->p.rayleigh_beta * dt;
+  if (S > 0) {
+    // forces + blocks (diagonal mass added in a second pass, below)
+    k_assemble<<<kblocks(S * 27), KT, 0, st>>>(G, sc->s[0]->d, sc->sdof, sc->sNode.as<long long>(), S,
+                                                sc->cellOrd, sc->Ke.as<double>(), sc->nf.as<double>(), scale,
+                                                sc->blocks.as<double>(),
+                                                sc->nbr.as<int>(), sc->mask.as<int>(), sc->solidF.as<double>());
+  }
+  k_body_forces<<<EB, KT, 0, st>>>(G, bp, sc->nodeVF, sc->solidMass, sc->vel, sc->intensity, sc->vort,
+                                   sc->ws, sc->sdof, sc->uf, sc->mvf, sc->minv, sc->damped.as<double>(),
+                                   sc->solidMv.as<double>(), sc->solidF.as<double>(), ePart + 2 * EB);
+  ESF_LAUNCH_CHECK();
+  if (S > 0) {
+    k_add_diag<<<kblocks(S), KT, 0, st>>>(S, sc->damped.as<double>(), sc->blocks.as<double>(),
+                                          sc->sysDiag.as<double>());
+    ESF_LAUNCH_CHECK();
+  }
+  double energy = sum_partials(sc, 3 * EB);
+  // ---- pcrImplicitSolve (:662-764)
+  int it[3] = {0, 0, 0}, cv[3] = {0, 0, 0}, rf[3] = {0, 0, 0};
+  double rr[3] = {0, 0, 0};
+  const int prec = sc->p.precision;
+  if (!sc->sw || solid_work_capacity(sc->sw) < S) {
+    solid_work_free(sc->sw);
+    sc->sw = nullptr;
+    TRY(solid_work_alloc(&sc->sw, S + S / 4 + 16, prec == ESF_MIXED));
+  }
+  esf_status es = ESF_OK;
+  if (S > 0) {
+    es = solid_solve(sc->sw, S, sc->blocks.as<double>(), sc->nbr.as<int>(), sc->sysDiag.as<double>(),
+                     sc->solidF.as<double>(), sc->solidV0.as<double>(), sc->p.implicit_solver_eps,
+                     sc->p.cr_max_iterations, prec, sc->p.inner_eps, sc->p.max_refinements, &it[0],
+                     &rr[0], &rf[0], &cv[0], st);
+    if (es == ESF_ERR_NUMERIC) sc->status = es;
+    else if (es) return es;
+  }
+  k_vstar<<<kblocks(G.T), KT, 0, st>>>(G, sc->sdof, sc->uf, sc->minv, sc->solidV0.as<double>(), sc->vstar);
+  k_cell_rhs<<<kblocks(G.R), KT, 0, st>>>(G, sc->vel, sc->vstar, sc->minv, sc->rhs, sc->jdiag, sc->b1);
+  ESF_LAUNCH_CHECK();
+  es = pressure_solve(sc->pw, G, sc->minv, sc->jdiag, sc->b1, sc->lambda, sc->p.div_free_solver_eps,
+                      sc->p.cr_max_iterations, prec, sc->p.inner_eps, sc->p.max_refinements, &it[1],
+                      &rr[1], &rf[1], &cv[1], st);
+  if (es == ESF_ERR_NUMERIC) sc->status = es;
+  else if (es) return es;
+  if (S > 0) {
+    k_solid_b1<<<kblocks(S), KT, 0, st>>>(G, sc->sNode.as<long long>(), S, sc->lambda, sc->solidB1.as<double>());
+    ESF_LAUNCH_CHECK();
+    es = solid_solve(sc->sw, S, sc->blocks.as<double>(), sc->nbr.as<int>(), sc->sysDiag.as<double>(),
+                     sc->solidB1.as<double>(), sc->solidPC.as<double>(), sc->p.implicit_solver_eps,
+                     sc->p.cr_max_iterations, prec, sc->p.inner_eps, sc->p.max_refinements, &it[2],
+                     &rr[2], &rf[2], &cv[2], st);
+    if (es == ESF_ERR_NUMERIC) sc->status = es;
+    else if (es) return es;
+  }
+  k_velocity_update<<<kblocks(G.T), KT, 0, st>>>(G, sc->sdof, sc->lambda, sc->minv, sc->solidPC.as<double>(),
+                                                 sc->vstar, sc->pc, sc->v1, sc->vel);
+  ESF_LAUNCH_CHECK();
+  // ---- finalizeSolution (:828-917)
+  ContactParams cp;
+  cp.wallThickness = sc->p.wall_thickness;
+  cp.spring = sc->p.contact_spring_stiffness;
+  cp.friction = sc->p.friction;
+  cp.alpha = sc->p.flip_alpha;
+  cp.bnd[0] = G.o[0];
+  cp.bnd[1] = G.o[1];
+  cp.bnd[2] = G.o[2];
+  cp.bnd[3] = G.o[0] + G.dh * (G.X - 1);
+  cp.bnd[4] = G.o[1] + G.dh * (G.Y - 1);
+  cp.bnd[5] = G.o[2] + G.dh * (G.Z - 1);
+  for (int i = 0; i < sc->ns; i++) {  // DEFOR_SOLID_3D::finalizeSolution(v, dt) (:1182-1197)
+    Solid* d = sc->s[i];
+    Box ex = mkbox(d->ex[0], d->ex[1], d->ex[2], d->ex[3], d->ex[4], d->ex[5]);
+    if (boxn(ex) > 0) k_copy_grid_velocity<<<kblocks(boxn(ex)), KT, 0, st>>>(G, d->d, ex, sc->vel);
+    d->d.dt = dt;
+  }
+  for (int i = 0; i < sc->ns; i++) {  // gridToParticle
+    Solid* d = sc->s[i];
+    if (d->np > 0)
+      k_grid_to_particle<<<kblocks(d->np), KT, 0, st>>>(G, d->d, d->np, d->part.as<double>(), cp, nullptr, 0,
+                                                        sc->dInts + 32);
+  }
+  for (int i = 0; i < sc->ns; i++) {  // particleToGrid
+    Solid* d = sc->s[i];
+    ESF_CUDA(cudaMemsetAsync(d->d.mass, 0, G.T * 8, st));
+    if (d->np == 0) continue;
+    const long long np = d->np;
+    const unsigned int nkeys = (unsigned int)((long long)(G.X + 3) * (G.Y + 3) * (G.Z + 3));
+    TRY(sc->keys.ensure(np * 4));
+    TRY(sc->vals.ensure(np * 4));
+    TRY(sc->skeys.ensure(np * 4));
+    TRY(sc->svals.ensure(np * 4));
+    TRY(sc->bstart.ensure((size_t)nkeys * 4));
+    TRY(sc->bend.ensure((size_t)nkeys * 4));
+    int pinit[6] = {1 << 30, 1 << 30, 1 << 30, -(1 << 30), -(1 << 30), -(1 << 30)};
+    memcpy(sc->hInts, pinit, sizeof pinit);
+    ESF_CUDA(cudaMemcpyAsync(sc->dInts, sc->hInts, sizeof pinit, cudaMemcpyHostToDevice, st));
+    k_p2g_keys<<<kblocks(np), KT, 0, st>>>(G, np, d->part.as<double>(), sc->keys.as<unsigned int>(),
+                                           sc->vals.as<unsigned int>(), sc->dInts);
+    int bits = 1;
+    while (bits < 32 && (1ull << bits) <= nkeys) bits++;
+    size_t tb = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, tb, sc->keys.as<unsigned int>(), sc->skeys.as<unsigned int>(),
+                                    sc->vals.as<unsigned int>(), sc->svals.as<unsigned int>(), (int)np, 0, bits, st);
+    TRY(sc->cubTmp.ensure(tb));
+    cub::DeviceRadixSort::SortPairs(sc->cubTmp.p, tb, sc->keys.as<unsigned int>(), sc->skeys.as<unsigned int>(),
+                                    sc->vals.as<unsigned int>(), sc->svals.as<unsigned int>(), (int)np, 0, bits, st);
+    ESF_CUDA(cudaMemsetAsync(sc->bstart.p, 0, (size_t)nkeys * 4, st));
+    ESF_CUDA(cudaMemsetAsync(sc->bend.p, 0, (size_t)nkeys * 4, st));
+    k_bucket_bounds<<<kblocks(np), KT, 0, st>>>(np, sc->skeys.as<unsigned int>(), sc->bstart.as<int>(),
+                                                sc->bend.as<int>(), nkeys);
+    ESF_CUDA(cudaMemcpyAsync(sc->hInts, sc->dInts, sizeof pinit, cudaMemcpyDeviceToHost, st));
+    ESF_CUDA(cudaStreamSynchronize(st));
+    Box nb = mkbox(std::max(sc->hInts[0], 0), std::max(sc->hInts[1], 0), std::max(sc->hInts[2], 0),
+                   std::min(sc->hInts[3] + 4, G.X), std::min(sc->hInts[4] + 4, G.Y), std::min(sc->hInts[5] + 4, G.Z));
+    if (boxn(nb) > 0)
+      k_p2g_gather<<<kblocks(boxn(nb)), KT, 0, st>>>(G, d->d, nb, d->part.as<double>(), sc->svals.as<unsigned int>(),
+                                                     sc->bstart.as<int>(), sc->bend.as<int>(), sc->p.flip_cutoff);
+    ESF_LAUNCH_CHECK();
+  }
+  for (int i = 0; i < sc->ns; i++) {  // extendVectorField
+    Solid* d = sc->s[i];
+    Box ex = mkbox(d->ex[0], d->ex[1], d->ex[2], d->ex[3], d->ex[4], d->ex[5]);
+    if (ex.hi[0] - ex.lo[0] >= 3 && ex.hi[1] - ex.lo[1] >= 3 && ex.hi[2] - ex.lo[2] >= 3)
+      k_extend_velocity<<<1, 1024, 0, st>>>(G, d->d, ex);
+    ESF_LAUNCH_CHECK();
+  }
+  for (int i = 0; i < sc->ns; i++) {  // DEFOR_SOLID_3D::finalizeSolution() (:1198-1233)
+    Solid* d = sc->s[i];
+    k_u_add<<<kblocks(3 * G.T), KT, 0, st>>>(G, d->d);
+    k_u_advect<<<kblocks(G.T), KT, 0, st>>>(G, d->d);
+    std::swap(d->d.u, d->d.tmp3);
+    Box ex = mkbox(d->ex[0], d->ex[1], d->ex[2], d->ex[3], d->ex[4], d->ex[5]);
+    // the face extrapolation reads two layers inward: boxes thinner than 3
+    // nodes (a vanished solid) are left as advected
+    if (ex.hi[0] - ex.lo[0] >= 3 && ex.hi[1] - ex.lo[1] >= 3 && ex.hi[2] - ex.lo[2] >= 3)
+      for (int axis = 2; axis >= 0; axis--)
+        k_u_extrapolate<<<kblocks(boxn(ex)), KT, 0, st>>>(G, d->d.u, ex, axis);
+    k_recover_X<<<kblocks(G.T), KT, 0, st>>>(G, d->d);
+    ESF_LAUNCH_CHECK();
+  }
+  for (int i = 0; i < sc->ns; i++) TRY(compute_solid_mass(sc, sc->s[i], 1));
+  for (int i = 0; i < sc->ns; i++) TRY(advect_mesh(sc, sc->s[i]));
+  for (int i = 0; i < sc->ns; i++) {
+    TRY(compute_sdf(sc, sc->s[i]));
+    TRY(init_particles(sc, sc->s[i]));
+  }
+  TRY(gather_solid_masses(sc));
+  k_advect_velocity<<<kblocks(G.T), KT, 0, st>>>(G, sc->solidMass, sc->vel, sc->vws, dt);
+  std::swap(sc->vel, sc->vws);
+  k_advect_scalar<<<kblocks(G.T), KT, 0, st>>>(G, sc->solidMass, sc->vel, sc->intensity, sc->ws, dt);
+  std::swap(sc->intensity, sc->ws);
+  TRY(recover_velocity(sc));
+  k_dirichlet<<<kblocks(G.T), KT, 0, st>>>(G, sc->vel, sc->intensity);
+  ESF_LAUNCH_CHECK();
+  ESF_CUDA(cudaEventRecord(sc->e1, st));
+  ESF_CUDA(cudaStreamSynchronize(st));
+  if (rep) {
+    memset(rep, 0, sizeof *rep);
+    rep->dt = dt;
+    rep->energy = energy;
+    for (int k = 0; k < 3; k++) {
+      rep->iterations[k] = it[k];
+      rep->converged[k] = cv[k];
+      rep->rel_residual[k] = rr[k];
+      rep->refinements[k] = rf[k];
+    }
+    rep->prone_to_contact = prone;
+    long long np = 0;
+    for (int i = 0; i < sc->ns; i++) np += sc->s[i]->np;
+    rep->num_particles = (int)np;
+    rep->status = sc->status;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, sc->e0, sc->e1);
+    rep->device_ms = ms;
+  }
+  return (esf_status)sc->status;
+}
+
+// ------------------------------------------------------------ field access
+namespace {
+struct FieldRef {
+  void* dev = nullptr;     // device source (node/cell/solid layouts)
+  size_t count = 0;        // elements exposed
+  size_t eb = 8;
+  int kind = 0;            // 0 direct, 1 node3->dof3, 2 node1->dof3, 3 host ints, 4 dof map
+  bool writable = false;
+};
+}  // namespace
+
+static esf_status field_ref(esf_scene* s, int f, int si, FieldRef& r) {
+  const GridDev& G = s->g;
+  const size_t T = G.T, R = G.R, D = 3ull * (G.X - 2) * (G.Y - 2) * (G.Z - 2), S3 = 3ull * s->S;
+  Solid* d = (si >= 0 && si < s->ns) ? s->s[si] : nullptr;
+  switch (f) {
+    case ESF_F_VELOCITY: r = {s->vel, T * 3, 8, 0, true}; return ESF_OK;
+    case ESF_F_INTENSITY: r = {s->intensity, T, 8, 0, true}; return ESF_OK;
+    case ESF_F_SOLID_MASS: r = {s->solidMass, T, 8, 0, false}; return ESF_OK;
+    case ESF_F_NODE_SOLID_VF: r = {s->nodeVF, T, 8, 0, false}; return ESF_OK;
+    case ESF_F_DOF_MAP: r = {nullptr, T, 4, 4, false}; return ESF_OK;
+    case ESF_F_SOLID_DOF_MAP: r = {s->sdof, T, 4, 0, false}; return ESF_OK;
+    case ESF_F_PRESSURE: r = {s->lambda, R, 8, 0, true}; return ESF_OK;
+    case ESF_F_JMINVJT_DIAG: r = {s->jdiag, R, 8, 0, false}; return ESF_OK;
+    case ESF_F_DIV_RHS: r = {s->rhs, R, 8, 0, false}; return ESF_OK;
+    case ESF_F_B1: r = {s->b1, R, 8, 0, false}; return ESF_OK;
+    case ESF_F_NZ_MASS_INV: r = {s->minv, D, 8, 2, false}; return ESF_OK;
+    case ESF_F_VELOCITY_DT0: r = {s->vstar, D, 8, 1, false}; return ESF_OK;
+    case ESF_F_VELOCITY_DT1: r = {s->v1, D, 8, 1, false}; return ESF_OK;
+    case ESF_F_UNIT_FORCE: r = {s->uf, D, 8, 1, false}; return ESF_OK;
+    case ESF_F_SOLID_UNIT_FORCE: r = {s->solidF.p, S3, 8, 0, false}; return ESF_OK;
+    case ESF_F_SOLID_VELOCITY_DT0: r = {s->solidV0.p, S3, 8, 0, false}; return ESF_OK;
+    case ESF_F_SOLID_PRESSURE_CORRECTION: r = {s->solidPC.p, S3, 8, 0, false}; return ESF_OK;
+    case ESF_F_DAMPED_SOLID_MASS: r = {s->damped.p, S3, 8, 0, false}; return ESF_OK;
+    case ESF_F_SYSTEM_DIAG: r = {s->sysDiag.p, S3, 8, 0, false}; return ESF_OK;
+    case ESF_F_SYSTEM_BLOCKS: r = {s->blocks.p, 243ull * s->S, 8, 0, false}; return ESF_OK;
+    case ESF_F_SYSTEM_MASK: r = {s->mask.p, (size_t)s->S, 4, 0, false}; return ESF_OK;
+    default: break;
+  }
+  if (!d) {
+    set_error("field %d: invalid solid index %d", f, si);
+    return ESF_ERR_INVALID_ARG;
+  }
+  switch (f) {
+    case ESF_F_S_U: r = {d->d.u, T * 3, 8, 0, true}; return ESF_OK;
+    case ESF_F_S_X: r = {d->d.X, T * 3, 8, 0, true}; return ESF_OK;
+    case ESF_F_S_VELOCITY: r = {d->d.vel, T * 3, 8, 0, true}; return ESF_OK;
+    case ESF_F_S_VEC_WORKSPACE: r = {d->d.vws, T * 3, 8, 0, true}; return ESF_OK;
+    case ESF_F_S_MASS: r = {d->d.mass, T, 8, 0, true}; return ESF_OK;
+    case ESF_F_S_PHI: r = {d->d.phi, T, 8, 0, true}; return ESF_OK;
+    case ESF_F_S_DET_FINV: r = {d->d.detFInv, T, 8, 0, false}; return ESF_OK;
+    case ESF_F_S_VALID: r = {d->d.valid, R, 1, 0, false}; return ESF_OK;
+    case ESF_F_S_QUARTER_FRACTIONS: r = {d->d.quarter, T * 8, 8, 0, false}; return ESF_OK;
+    case ESF_F_S_PARTICLES: r = {d->part.p, (size_t)d->np * 10, 8, 0, false}; return ESF_OK;
+    case ESF_F_S_MESH_VERTICES: r = {d->dVerts, (size_t)d->nv * 3, 8, 0, false}; return ESF_OK;
+    case ESF_F_S_BOXES: r = {nullptr, 12, 4, 3, false}; return ESF_OK;
+    default: break;
+  }
+  set_error("unknown field id %d", f);
+  return ESF_ERR_INVALID_ARG;
+}
+
+extern "C" esf_status esf_field_info(const esf_scene* s, esf_field f, int si, size_t* count,
+                                     size_t* eb) {
+  if (!s || !count || !eb) return ESF_ERR_INVALID_ARG;
+  FieldRef r;
+  TRY(field_ref((esf_scene*)s, f, si, r));
+  *count = r.count;
+  *eb = r.eb;
+  return ESF_OK;
+}
+
+extern "C" esf_status esf_get_field(esf_scene* s, esf_field f, int si, void* host, size_t bytes) {
+  if (!s || (!host && bytes)) return ESF_ERR_INVALID_ARG;
+  FieldRef r;
+  TRY(field_ref(s, f, si, r));
+  if (bytes != r.count * r.eb) {
+    set_error("esf_get_field(%d): %zu bytes given, %zu expected", (int)f, bytes, r.count * r.eb);
+    return ESF_ERR_INVALID_ARG;
+  }
+  const GridDev& G = s->g;
+  ESF_CUDA(cudaStreamSynchronize(s->stream));
+  if (r.kind == 0) {
+    if (bytes) ESF_CUDA(cudaMemcpy(host, r.dev, bytes, cudaMemcpyDeviceToHost));
+    return ESF_OK;
+  }
+  if (r.kind == 3) {
+    Solid* d = s->s[si];
+    int b[12] = {d->ex[0], d->ex[1], d->ex[2], d->ex[3], d->ex[4], d->ex[5],
+                 d->tmin[0], d->tmin[1], d->tmin[2], d->tmax[0], d->tmax[1], d->tmax[2]};
+    memcpy(host, b, 48);
+    return ESF_OK;
+  }
+  if (r.kind == 4) {  // _gridIdxToSolutionIdx (COUPLED_INTEGRATOR_3D.cpp:123-131)
+    int* o = (int*)host;
+    int idx = 0;
+    for (long long n = 0; n < G.T; n++) o[n] = -1;
+    for (int z = 1; z < G.Z - 1; z++)
+      for (int y = 1; y < G.Y - 1; y++)
+        for (int x = 1; x < G.X - 1; x++) o[x + (long long)y * G.X + z * G.slab] = idx++;
+    return ESF_OK;
+  }
+  // node-indexed -> compacted DOF order
+  const int comp = (r.kind == 1) ? 3 : 1;
+  std::vector<double> tmp(G.T * comp);
+  ESF_CUDA(cudaMemcpy(tmp.data(), r.dev, tmp.size() * 8, cudaMemcpyDeviceToHost));
+  double* o = (double*)host;
+  long long k = 0;
+  for (int z = 1; z < G.Z - 1; z++)
+    for (int y = 1; y < G.Y - 1; y++)
+      for (int x = 1; x < G.X - 1; x++, k++) {
+        long long n = x + (long long)y * G.X + z * G.slab;
+        for (int q = 0; q < 3; q++) o[3 * k + q] = (comp == 3) ? tmp[3 * n + q] : tmp[n];
+      }
+  return ESF_OK;
+}
+
+extern "C" esf_status esf_set_field(esf_scene* s, esf_field f, int si, const void* host,
+                                    size_t bytes) {
+  if (!s || (!host && bytes)) return ESF_ERR_INVALID_ARG;
+  FieldRef r;
+  TRY(field_ref(s, f, si, r));
+  if (!r.writable || r.kind != 0) {
+    set_error("esf_set_field(%d): field is read-only", (int)f);
+    return ESF_ERR_INVALID_ARG;
+  }
+  if (bytes != r.count * r.eb) {
+    set_error("esf_set_field(%d): %zu bytes given, %zu expected", (int)f, bytes, r.count * r.eb);
+    return ESF_ERR_INVALID_ARG;
+  }
+  ESF_CUDA(cudaStreamSynchronize(s->stream));
+  if (bytes) ESF_CUDA(cudaMemcpy(r.dev, host, bytes, cudaMemcpyHostToDevice));
+  return ESF_OK;
+}
+
+// ------------------------------------------------------- operator seam
+static GridDev grid_dev(const esf_grid* g) {
+  GridDev G;
+  G.X = g->xRes;
+  G.Y = g->yRes;
+  G.Z = g->zRes;
+  G.slab = (long long)G.X * G.Y;
+  G.T = G.slab * G.Z;
+  G.cX = G.X - 1;
+  G.cY = G.Y - 1;
+  G.cZ = G.Z - 1;
+  G.cslab = (long long)G.cX * G.cY;
+  G.R = G.cslab * G.cZ;
+  G.dh = g->dh;
+  G.dhInv = 1.0 / g->dh;
+  for (int k = 0; k < 3; k++) G.o[k] = g->origin[k];
+  return G;
+}
+
+extern "C" esf_status esf_pressure_apply(const esf_grid* g, const double* minv, const double* in,
+                                         double* out, void* stream) {
+  if (!g || !minv || !in || !out || g->xRes < 3 || g->yRes < 3 || g->zRes < 3) {
+    set_error("esf_pressure_apply: invalid argument");
+    return ESF_ERR_INVALID_ARG;
+  }
+  GridDev G = grid_dev(g);
+  return pressure_apply<double>(G, minv, in, out, (cudaStream_t)stream);
+}
+
+extern "C" esf_status esf_pressure_solve(const esf_grid* g, const double* minv, const double* diag,
+                                         const double* b, double* x, double eps, int maxIt,
+                                         int precision, int* iters, double* relres, void* stream) {
+  if (!g || !minv || !diag || !b || !x || g->xRes < 3 || g->yRes < 3 || g->zRes < 3 || maxIt < 0 ||
+      (precision != ESF_FP64 && precision != ESF_MIXED)) {
+    set_error("esf_pressure_solve: invalid argument");
+    return ESF_ERR_INVALID_ARG;
+  }
+  GridDev G = grid_dev(g);
+  PressureWork* w = nullptr;
+  TRY(pressure_work_alloc(&w, G, precision == ESF_MIXED));
+  int it = 0, rf = 0, cv = 0;
+  double rr = 0;
+  esf_status e = pressure_solve(w, G, minv, diag, b, x, eps, maxIt, precision, 1e-4, 50, &it, &rr, &rf,
+                                &cv, (cudaStream_t)stream);
+  cudaStreamSynchronize((cudaStream_t)stream);
+  pressure_work_free(w);
+  if (iters) *iters = it;
+  if (relres) *relres = rr;
+  return e;
+}
+
+extern "C" esf_status esf_write_frame(esf_scene* s, const char* path, int frame, int debug) {
+  (void)s; (void)path; (void)frame; (void)debug;
+  set_error("esf_write_frame: frame I/O is not implemented yet");
+  return ESF_ERR_UNSUPPORTED;
+}
+extern "C" esf_status esf_read_frame(esf_scene* s, const char* path, int frame, int debug) {
+  (void)s; (void)path; (void)frame; (void)debug;
+  set_error("esf_read_frame: frame I/O is not implemented yet");
+  return ESF_ERR_UNSUPPORTED;
+}

@@ -1,0 +1,119 @@
+"""The solver seam through the C ABI: esf_pressure_apply / esf_pressure_solve
+(getMatVecMult and solvePCR of the reference) against the oracle, the
+mixed-precision refinement against FP64, and error handling."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from common import rel_err
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(a):
+    import torch
+    return torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def _jacobi_diag(X, Y, Z, minv):
+    """diag(J M^-1 J^T): 3 m^-1 summed over the DOF corners of each cell."""
+    m = minv.reshape(Z, Y, X).copy()
+    m[0, :, :] = m[-1, :, :] = 0
+    m[:, 0, :] = m[:, -1, :] = 0
+    m[:, :, 0] = m[:, :, -1] = 0
+    d = np.zeros((Z - 1, Y - 1, X - 1))
+    for i in range(8):
+        dx, dy, dz = i & 1, (i >> 1) & 1, (i >> 2) & 1
+        d += 3 * m[dz:dz + Z - 1, dy:dy + Y - 1, dx:dx + X - 1]
+    return d.reshape(-1)
+
+
+@pytest.mark.parametrize("shape", [(21, 17, 13), (34, 9, 40), (4, 4, 4)])
+def test_pressure_apply_matches_oracle(shape, gpu_lib):
+    import torch
+    X, Y, Z = shape
+    rng = np.random.default_rng(X * Y * Z)
+    g = oracle.grid(X, 0.05)
+    g.yRes, g.zRes = Y, Z
+    minv = rng.uniform(0.5, 2.0, X * Y * Z)
+    x = rng.standard_normal((X - 1) * (Y - 1) * (Z - 1))
+    ref = oracle.pressure_apply(g, minv, x)
+    dm, dx, do = _dev(minv), _dev(x), _dev(np.zeros_like(x))
+    assert gpu_lib.esf_pressure_apply(C.byref(g), _ptr(dm), _ptr(dx), _ptr(do), None) == 0
+    torch.cuda.synchronize()
+    assert rel_err(do.cpu().numpy(), ref) <= 1e-13
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_pressure_solve_matches_oracle(precision, gpu_lib):
+    import torch
+    X = Y = Z = 25
+    rng = np.random.default_rng(7)
+    g = oracle.grid(X, 0.04)
+    minv = rng.uniform(50.0, 300.0, X * Y * Z)
+    diag = _jacobi_diag(X, Y, Z, minv)
+    b = oracle.pressure_apply(g, minv, rng.standard_normal((X - 1) ** 3))
+    x0 = 0.1 * rng.standard_normal(len(b))  # warm start
+    xr, itr, rrr, st = oracle.pressure_solve(g, minv, diag, b, x0, 1e-8, 20000)
+    assert st == 0 and rrr < 1e-8
+    dm, dd, db, dx = _dev(minv), _dev(diag), _dev(b), _dev(x0)
+    it, rr = C.c_int(), C.c_double()
+    s = gpu_lib.esf_pressure_solve(C.byref(g), _ptr(dm), _ptr(dd), _ptr(db), _ptr(dx), 1e-8, 20000,
+                                   precision, C.byref(it), C.byref(rr), None)
+    torch.cuda.synchronize()
+    assert s == 0
+    assert rr.value < 1e-8
+    x = dx.cpu().numpy()
+    # independent residual of the GPU answer with the oracle operator
+    res = np.linalg.norm(oracle.pressure_apply(g, minv, x) - b) / np.linalg.norm(b)
+    assert res < 1e-8
+    if precision == 0:
+        assert abs(it.value - itr) <= 5
+    assert rel_err(x, xr) <= 1e-5
+
+
+def test_mixed_step_close_to_fp64(gpu_lib):
+    """Mixed-precision refinement reaches the same 1e-8 relative residual;
+    velocity and pressure stay close to the FP64 GPU step."""
+    import eulersf_gb300 as E
+    from eulersf_gb300.scene import SceneDesc
+    desc = SceneDesc(N=32, mass_sample_dh=(1 / 32) / 4, noise_seed=7)
+    A, B = E.make_scene(desc, precision=0), E.make_scene(desc, precision=1)
+    for _ in range(3):
+        ra, rb = A.stepImplicit(), B.stepImplicit()
+        assert all(rb["converged"]) and max(rb["rel_residual"]) < 1e-8, rb
+        assert rel_err(B.get("velocity"), A.get("velocity")) < 1e-5
+        assert rel_err(B.get("lambda1"), A.get("lambda1")) < 1e-5
+        assert np.array_equal(B.get("gridIdxToSolidIdx"), A.get("gridIdxToSolidIdx"))
+
+
+def test_error_paths(gpu_lib):
+    import eulersf_gb300 as E
+    from eulersf_gb300 import abi
+    from eulersf_gb300.scene import SceneDesc
+    g = abi.Grid(10, 10, 10, 0.1, (C.c_double * 3)(0, 0, 0))
+    p = abi.Params()
+    assert gpu_lib.esf_params_default(C.byref(g), C.byref(p)) == 0
+    h = C.c_void_p()
+    assert gpu_lib.esf_create(C.byref(g), C.byref(p), None, C.byref(h)) == 0
+    rep = abi.StepReport()
+    assert gpu_lib.esf_step(h, C.byref(rep)) == 2           # before init
+    assert gpu_lib.esf_init(h) == 2                          # no solid
+    buf = np.zeros(5)
+    assert gpu_lib.esf_set_field(h, 0, 0, buf.ctypes.data_as(C.c_void_p), 40) == 1  # size
+    assert gpu_lib.esf_set_field(h, 2, 0, buf.ctypes.data_as(C.c_void_p), 40) == 1  # read-only
+    assert gpu_lib.esf_get_field(h, 54, 3, buf.ctypes.data_as(C.c_void_p), 40) == 1  # no solid 3
+    assert gpu_lib.esf_destroy(h) == 0
+    I = E.make_scene(SceneDesc(N=12, mass_sample_dh=(1 / 12) / 4))
+    with pytest.raises(abi.EsfError):
+        I.set("velocity", np.zeros(7))
+    it, rr = C.c_int(), C.c_double()
+    assert gpu_lib.esf_pressure_solve(C.byref(g), None, None, None, None, 1e-8, 10, 0,
+                                      C.byref(it), C.byref(rr), None) == 1

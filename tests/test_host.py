@@ -1,0 +1,111 @@
+"""CPU-only checks: the C-ABI library loads and exports every declared
+symbol, host-side argument checks, the cfg reader, and the scene generator.
+No kernel is launched."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from common import ROOT
+
+from eulersf_gb300 import abi, scene
+
+
+def _declared():
+    text = open(os.path.join(ROOT, "include", "eulersf.h")).read()
+    return sorted(set(re.findall(r"\b(esf_[a-z_0-9]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import eulersf_gb300 as E
+    return E.load(build_if_missing=True)
+
+
+def test_exports_every_declared_symbol(lib):
+    import eulersf_gb300 as E
+    names = _declared()
+    assert set(names) == set(E.EXPORTS)
+    for n in names:
+        assert hasattr(lib, n), n
+    assert lib.esf_abi_version() == 1
+
+
+def test_oracle_exports():
+    import oracle
+    o = oracle.load()
+    for n in ("esfo_create", "esfo_step", "esfo_pressure_apply", "esfo_pressure_solve"):
+        assert hasattr(o, n)
+
+
+def test_invalid_arguments_need_no_gpu(lib):
+    g = abi.Grid(2, 10, 10, 0.1, (C.c_double * 3)(0, 0, 0))
+    p = abi.Params()
+    assert lib.esf_params_default(C.byref(g), C.byref(p)) == 0
+    assert p.cr_max_iterations == 10 and p.particles_per_cell == 8 and p.flip_alpha == 0.95
+    h = C.c_void_p()
+    assert lib.esf_create(C.byref(g), C.byref(p), None, C.byref(h)) == 1
+    assert b"grid" in lib.esf_last_error()
+    assert lib.esf_create(None, C.byref(p), None, C.byref(h)) == 1
+    assert lib.esf_step(None, None) == 1
+    assert lib.esf_destroy(None) == 0
+
+
+def test_parse_config_reads_reference_keys(lib, tmp_path):
+    desc = scene.SceneDesc(N=48, vorticity_eps=1.5, buoyancy=0.2, eps=1e-6, max_iters=1234,
+                           solids=[scene.SolidDesc(center=(0.4, 0.6, 0.5), radius=0.12, E=3e5)])
+    cfg = scene.write_scene(desc, str(tmp_path / "s"))
+    g, p, n = abi.Grid(), abi.Params(), C.c_int()
+    paths = C.create_string_buffer(4 * 256)
+    solids = (abi.SolidDesc * 4)()
+    st = lib.esf_parse_config(cfg.encode(), C.byref(g), C.byref(p), C.byref(n), paths, 256, solids, 4)
+    assert st == 0
+    assert (g.xRes, g.yRes, g.zRes) == (49, 49, 49) and g.dh == 1.0 / 48
+    assert p.dt == 1.0 / 240 and p.gravity == 9.8 and p.vorticity_eps == 1.5 and p.buoyancy == 0.2
+    assert p.div_free_solver_eps == 1e-6 and p.cr_max_iterations == 1234
+    assert p.particles_per_cell == 32 and p.mass_sample_dh == 0.00125 and p.tight_border == 5
+    assert n.value == 1
+    lam, mu = scene.lame(3e5, 0.45)
+    assert solids[0].lambda_ == pytest.approx(lam, rel=1e-15) and solids[0].mu == pytest.approx(mu, rel=1e-15)
+    assert tuple(solids[0].translation) == (0.4, 0.6, 0.5)
+    assert paths.raw[:256].split(b"\0")[0].decode().endswith("sphere0")
+    assert list(solids[0].rotation) == [1, 0, 0, 0, 1, 0, 0, 0, 1]
+    # the Python reader agrees (SIMPLE_PARSER lowercases keys and values)
+    vals = scene.parse_cfg(cfg)
+    assert float(vals["dt"]) == p.dt and vals["xres"] == "49"
+    assert lib.esf_parse_config(b"/nonexistent.cfg", C.byref(g), C.byref(p), None, None, 0,
+                                None, 0) == 5
+
+
+def test_noise_field():
+    a = scene.noise_field(9, 0)
+    b = scene.noise_field(9, 0)
+    c = scene.noise_field(9, 1)
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    assert np.abs(a).max() <= 1e-3
+    v = a.reshape(9, 9, 9, 3)
+    for face in (v[0], v[-1], v[:, 0], v[:, -1], v[:, :, 0], v[:, :, -1]):
+        assert not face.any()
+    assert abs(a[a != 0].mean()) < 2e-4
+
+
+def test_rest_mass_and_mesh(tmp_path):
+    res, mdh, orig, data = scene.rest_mass_field(0.15)
+    assert mdh == 0.0015 and all(r >= 219 for r in res)
+    # volume of the rasterised sphere ~ 4/3 pi r^3 (density 1000)
+    vol = (data > 0).sum() * mdh ** 3
+    assert abs(vol - 4 / 3 * np.pi * 0.15 ** 3) / vol < 0.02
+    p = str(tmp_path / "m.mass")
+    scene.write_field_gz(p, res, mdh, orig, data)
+    r2, d2, o2, data2 = scene.read_field_gz(p)
+    assert tuple(r2) == tuple(res) and d2 == mdh and np.array_equal(data2, data)
+    v, f = scene.icosphere(3, 0.2)
+    assert len(v) == 642 and len(f) == 1280
+    assert np.allclose(np.linalg.norm(v, axis=1), 0.2)
+
+
+def test_lame():
+    lam, mu = scene.lame(2e5, 0.45)
+    assert lam == pytest.approx(620689.6551724138) and mu == pytest.approx(68965.51724137931)
