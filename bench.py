@@ -1,0 +1,347 @@
+"""Benchmark of the coupled solid-fluid step on GB300.
+
+Workload (one "step" = one stepImplicit of the scene): the rubber-ball scene
+at 256^3 cells (257^3 nodes, dx = 1/256), sphere r = 0.15 at (0.5, 0.65, 0.5),
+density 1100, E = 2e5, nu = 0.45, fluid density 1000, gravity 9.8,
+dt = 1/240, all solves to 1e-8 relative residual, seeded fluid noise
+(seed 7), mixed precision (FP32 inner PCR in FP64 refinement). Synthetic
+input: the scene generator of eulersf_gb300/scene.py. Every working array
+(>= 135 MB each, ~2 GB in all) is larger than the 129 MB L2, so no flush is
+needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs N independent replicas (one scene per GPU): the step does not
+shard. Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "coupled steps/s at 256^3 (mixed precision; CG iters/s reported beside it)"
+UNIT = "steps/s"
+# Pressure PCR iterations of the reference's FP64 algorithm per step of this
+# workload, measured with the FP64 GPU path (its counts match the reference's
+# to within one 5-iteration check interval): profiles/pressure_fp64_256.md.
+FP64_ITERS_PER_STEP_256 = 18025
+
+
+def workload(N=256, seed=7):
+    from eulersf_gb300.scene import SceneDesc, SolidDesc
+    return SceneDesc(N=N, noise_seed=seed,
+                     solids=[SolidDesc(center=(0.5, 0.65, 0.5), radius=0.15, density=1100.0,
+                                       E=2e5, nu=0.45)])
+
+
+def config_dict(desc, precision, n_gpus):
+    return {"workload": f"rubber ball {desc.N}^3 cells ({desc.res}^3 nodes), r=0.15, E=2e5, nu=0.45, "
+                        f"fluid 1000 / solid 1100, dt=1/240, tol 1e-8, seed {desc.noise_seed}",
+            "grid_cells": desc.N ** 3, "precision": precision, "parallelism": f"replicas x{n_gpus}",
+            "l2": "inputs larger than L2 (no flush)"}
+
+
+def read_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        cmd = ["nvidia-smi", "-i", str(self.gpu),
+               "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+               "--format=csv,noheader,nounits", "-lms", "200"]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def dist_setup(n_gpus):
+    rank, world = int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("ESF_BENCH_GLOO") is None else "gloo")
+        pg = dist
+    return rank, world, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    pg.all_reduce(t)
+    return float(t.item())
+
+
+# --------------------------------------------------------- CPU baseline
+def synthetic_pressure_problem(desc, seed=0):
+    """A pressure problem of the workload's size: m^-1 of fluid nodes
+    (rho_f dh^3) with the ball's nodes also carrying solid mass, its Jacobi
+    diagonal and a smooth right-hand side. The cost of a PCR iteration
+    depends only on the grid, not on these values."""
+    import numpy as np
+    res, N, dh = desc.res, desc.N, desc.dh
+    s = desc.solids[0]
+    z, y, x = np.meshgrid(*(np.arange(res) * dh,) * 3, indexing="ij")
+    fluid = desc.fluid_density * dh ** 3
+    inside = (x - s.center[0]) ** 2 + (y - s.center[1]) ** 2 + (z - s.center[2]) ** 2 <= s.radius ** 2
+    mass = fluid + np.where(inside, s.density * dh ** 3, 0.0)
+    minv = (1.0 / mass).reshape(-1)
+    m = minv.reshape(res, res, res).copy()
+    m[0], m[-1], m[:, 0], m[:, -1], m[:, :, 0], m[:, :, -1] = 0, 0, 0, 0, 0, 0
+    diag = np.zeros((N, N, N))
+    for i in range(8):
+        dx, dy, dz = i & 1, (i >> 1) & 1, (i >> 2) & 1
+        diag += 3 * m[dz:dz + N, dy:dy + N, dx:dx + N]
+    rng = np.random.default_rng(seed)
+    b = rng.standard_normal(N ** 3)
+    return minv, diag.reshape(-1), b
+
+
+def cpu_pressure_sample(desc, iters, threads=None):
+    """Time `iters` FP64 pressure-PCR iterations at the workload's size with
+    the CPU oracle (the reference's algorithm restated in C, OpenMP on the
+    operator and the elementwise updates)."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    import oracle
+    minv, diag, b = synthetic_pressure_problem(desc)
+    g = oracle.grid(desc.res, desc.dh)
+    oracle.pressure_apply(g, minv, b)  # load + first touch
+    t0 = time.perf_counter()
+    _, it, _, _ = oracle.pressure_solve(g, minv, diag, b, np.zeros_like(b), 1e-30, iters)
+    return it, time.perf_counter() - t0
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def reference_arm(args):
+    """--impl reference: the reference algorithm on the host cores (the
+    oracle port; the reference's own binaries are built for this machine
+    only), same workload, metric and unit."""
+    rank, world, pg = dist_setup(args.gpus)
+    if rank != 0:
+        return 0
+    desc = workload(args.size)
+    threads = cpu_threads()
+    per_step = []
+    sample_iters = max(2, args.cpu_iters)
+    for _ in range(args.warmup):
+        cpu_pressure_sample(desc, 1, threads)
+    for _ in range(args.steps):
+        it, t = cpu_pressure_sample(desc, sample_iters, threads)
+        per_step.append(t / max(it, 1) * FP64_ITERS_PER_STEP_256)
+    t_step = statistics.mean(per_step)
+    value = 1.0 / t_step
+    sample = (f"{sample_iters} FP64 pressure-PCR iterations at {desc.N}^3 per timed step "
+              f"(oracle port, {threads} threads); steps/s = iterations/s / "
+              f"{FP64_ITERS_PER_STEP_256} iterations per step (the reference algorithm's count); "
+              f"the non-solver part of the step (<2% at this tolerance) is not counted")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config_dict(desc, "fp64 (reference algorithm)", args.gpus),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------- our arm
+def ours(args):
+    import numpy as np
+    import torch
+    rank, world, pg = dist_setup(args.gpus)
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(local)
+    import eulersf_gb300 as E
+    from eulersf_gb300 import abi
+    lib = E.load()
+    prec = abi.ESF_MIXED if args.precision == "mixed" else abi.ESF_FP64
+    desc = workload(args.size)
+    stream = torch.cuda.current_stream()
+    I = E.make_scene(desc, precision=prec, stream=stream.cuda_stream)
+    for _ in range(args.warmup):
+        I.stepImplicit()
+    # ---- timed region: device time, inputs resident in HBM
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(pg)
+    torch.cuda.synchronize()
+    l0 = lib.esf_kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    reports = [I.stepImplicit() for _ in range(args.steps)]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(pg)
+    launches = lib.esf_kernel_launches() - l0
+    clk = clocks.stop()
+    t = e0.elapsed_time(e1) / 1e3
+    t_max = max_over_ranks(pg, t)
+    steps_all = sum_over_ranks(pg, args.steps)
+    value = steps_all / t_max
+    piters = sum(r["iterations"][1] for r in reports)
+    cg_rate = sum_over_ranks(pg, piters) / t_max
+    # ---- dominant kernel: fused update + stencil + dot of the pressure PCR
+    upd, axpy = C.c_double(), C.c_double()
+    st = lib.esf_time_pressure_kernels(I._h, 20, C.byref(upd), C.byref(axpy))
+    R = desc.N ** 3
+    w = 4 if prec == abi.ESF_MIXED else 8
+    peak, peak_kind = read_peaks()
+    algo = 10 * w * R  # P2 + P3 of the per-iteration byte model: 10 words per row
+    achieved = algo / (upd.value * 1e-3) / 1e9 if st == 0 and upd.value > 0 else None
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "pressure_update_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            tj = json.load(f)
+        key = f"{'fp32' if w == 4 else 'fp64'}_{desc.N}"
+        if key in tj:
+            traffic = tj[key]
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                "peak_kind": peak_kind, "kernel": f"pressure_stencil<{'float' if w == 4 else 'double'}, update>",
+                "kernel_ms": upd.value, "axpy_kernel_ms": axpy.value,
+                "algorithmic_bytes_per_launch": algo}
+    # ---- e2e: public API with host buffers (pinned), copies in the timed region
+    e2e = None
+    if args.e2e_steps > 0:
+        res = desc.res
+        inten = I.get("intensity")
+        h_in = torch.from_numpy(inten).pin_memory()
+        h_out = torch.empty(res ** 3 * 3, dtype=torch.float64).pin_memory()
+        fid_in, fid_out = abi.FIELDS["intensity"][0], abi.FIELDS["velocity"][0]
+        barrier(pg)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            lib.esf_set_field(I._h, fid_in, 0, C.c_void_p(h_in.data_ptr()), h_in.numel() * 8)
+            lib.esf_step(I._h, None)
+            lib.esf_get_field(I._h, fid_out, 0, C.c_void_p(h_out.data_ptr()), h_out.numel() * 8)
+        torch.cuda.synchronize()
+        te = max_over_ranks(pg, time.perf_counter() - t0)
+        e2e = {"value": sum_over_ranks(pg, args.e2e_steps) / te, "unit": UNIT,
+               "h2d_bytes_per_step": int(h_in.numel() * 8), "d2h_bytes_per_step": int(h_out.numel() * 8),
+               "what": "per step: intensity field H2D, esf_step, velocity field D2H (pinned host buffers)"}
+    # ---- CPU baseline (rank 0, N=1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = cpu_threads()
+        it, tc = cpu_pressure_sample(desc, args.cpu_iters, threads)
+        t_step = tc / max(it, 1) * FP64_ITERS_PER_STEP_256
+        cpu = {"value": 1.0 / t_step, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{it} FP64 pressure-PCR iterations of this {desc.N}^3 step on the oracle port "
+                         f"({tc:.1f} s); steps/s = iterations/s / {FP64_ITERS_PER_STEP_256} iterations per "
+                         f"step of the reference algorithm; non-solver work not counted"}
+    if rank == 0:
+        last = reports[-1]
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer" if w == 4 else "f64",
+            "data": "synthetic (seeded scene generator)", "config": config_dict(desc, args.precision, world),
+            "cg_iters_per_s": cg_rate, "pressure_iters_per_step": piters / args.steps,
+            "solid_iters_per_step": [r["iterations"][0] + r["iterations"][2] for r in reports],
+            "refinements_last_step": last["refinements"], "rel_residual_last_step": last["rel_residual"],
+            "phase_ms_last_step": last["phase_ms"], "roofline": roofline, "cpu_baseline": cpu,
+            "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    I.close()
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-iters", type=int, default=10)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -23,7 +23,8 @@ EXPORTS = [
     "esf_abi_version", "esf_last_error", "esf_params_default", "esf_parse_config", "esf_create",
     "esf_destroy", "esf_add_solid", "esf_set_fluid", "esf_init", "esf_set_max_dt", "esf_step",
     "esf_dt", "esf_field_info", "esf_get_field", "esf_set_field", "esf_pressure_apply",
-    "esf_pressure_solve", "esf_write_frame", "esf_read_frame",
+    "esf_pressure_solve", "esf_write_frame", "esf_read_frame", "esf_kernel_launches",
+    "esf_time_pressure_kernels",
 ]
 
 
@@ -50,6 +51,9 @@ def load(build_if_missing: bool = False) -> C.CDLL:
     lib.esf_parse_config.argtypes = [C.c_char_p, C.POINTER(abi.Grid), C.POINTER(abi.Params),
                                      C.POINTER(C.c_int), C.c_char_p, C.c_size_t,
                                      C.POINTER(abi.SolidDesc), C.c_int]
+    lib.esf_kernel_launches.restype = C.c_uint64
+    lib.esf_time_pressure_kernels.argtypes = [vp, C.c_int, C.POINTER(C.c_double),
+                                              C.POINTER(C.c_double)]
     lib.esf_write_frame.argtypes = [vp, C.c_char_p, C.c_int, C.c_int]
     lib.esf_read_frame.argtypes = [vp, C.c_char_p, C.c_int, C.c_int]
     _lib = lib

@@ -57,17 +57,24 @@ class StepReport(C.Structure):
     _fields_ = [
         ("dt", C.c_double), ("energy", C.c_double), ("iterations", C.c_int * 3),
         ("converged", C.c_int * 3), ("rel_residual", C.c_double * 3),
-        ("refinements", C.c_int * 3), ("prone_to_contact", C.c_int),
+        ("refinements", C.c_int * 3), ("fp64_iterations", C.c_int), ("prone_to_contact", C.c_int),
         ("num_particles", C.c_int), ("status", C.c_int), ("device_ms", C.c_double),
+        ("phase_ms", C.c_double * 13),
     ]
+    PHASES = ["broad_phase_cfl", "solid_forces_stiffness", "body_forces", "solid_solve_1",
+              "pressure_solve", "solid_solve_2", "grid_to_particle", "particle_to_grid",
+              "velocity_extension", "solid_displacement", "solid_mass", "mesh_sdf_particles",
+              "fluid_advection"]
 
     def as_dict(self) -> dict:
         return {
             "dt": self.dt, "energy": self.energy, "iterations": list(self.iterations),
             "converged": list(self.converged), "rel_residual": list(self.rel_residual),
-            "refinements": list(self.refinements), "prone_to_contact": self.prone_to_contact,
+            "refinements": list(self.refinements), "fp64_iterations": self.fp64_iterations,
+            "prone_to_contact": self.prone_to_contact,
             "num_particles": self.num_particles, "status": self.status,
             "device_ms": self.device_ms,
+            "phase_ms": dict(zip(self.PHASES, list(self.phase_ms))),
         }
 
 

@@ -106,7 +106,10 @@ struct PcrState {
   int setup;         // 1: next phase-B reduction initialises delta
   int status;        // 0 ok, 6 numeric (NaN met)
   int inner;         // 1: inner solve of a refinement, stops on delta/delta0
-  double delta0;     // delta after set-up
+  double delta0;     // delta after set-up or after the last residual replacement
+  int rebase;        // 1: next update reduction replaces the residual (keeps d)
+  int iter0;         // iteration of the last replacement
+  int cap;           // inner mode: iterations between replacements (0 = none)
   unsigned int ticket[4];
 };
 
@@ -118,7 +121,13 @@ struct PcrState {
 namespace esf {
 void set_error(const char* fmt, ...);
 const char* cuda_err(cudaError_t e);
+// kernel-launch accounting: direct launches count once; launches made while
+// a graph is being captured are counted per replay instead
+void note_launch();
+void note_graph_replay(unsigned long long kernels);
+void set_capturing(bool on, unsigned long long* counter);
 }  // namespace esf
+#define ESF_COUNTED esf::note_launch(),
 
 #define ESF_CUDA(call)                                                                  \
   do {                                                                                  \
@@ -152,7 +161,15 @@ void pressure_work_free(PressureWork* w);
 esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv64,
                           const double* diag64, const double* b, double* x, double eps, int maxIt,
                           int precision, double innerEps, int maxRefine, int* iters,
-                          double* relres, int* refinements, int* converged, cudaStream_t st);
+                          double* relres, int* refinements, int* converged, cudaStream_t st,
+                          int* fp64Iters = nullptr);
+
+// Average device time of the fused update kernel and of the axpy+norm kernel
+// on scratch copies of the pressure problem (state untouched).
+esf_status pressure_time_kernels(PressureWork* w, const GridDev& g, const double* minv64,
+                                 const double* diag64, const double* b, const double* x,
+                                 int precision, int reps, double* update_ms, double* axpy_ms,
+                                 cudaStream_t st);
 
 // Solid system in node-block form: for solid node a, 27 neighbour blocks of
 // 3x3 (neighbour j = (dx+1) + 3(dy+1) + 9(dz+1)), nbr[a*27+j] = solid index

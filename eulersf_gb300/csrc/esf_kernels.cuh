@@ -336,6 +336,22 @@ __device__ void sweep_phi_pass(const GridDev& g, double* ph, const double* ms, c
   }
 }
 
+// One hyperplane a+b+c = p of a sweepPhi pass, all blocks in parallel.
+__global__ void k_sweep_phi_plane(GridDev g, double* ph, const double* ms, Sweep w, int p) {
+  const long long nab = (long long)w.ni * w.nj;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nab;
+       t += (long long)gridDim.x * blockDim.x) {
+    int a = (int)(t % w.ni), b = (int)(t / w.ni);
+    int c = p - a - b;
+    if (c < 0 || c >= w.nk) continue;
+    int i = w.i0 + a * w.di, j = w.j0 + b * w.dj, k = w.k0 + c * w.dk;
+    long long n = nidx(g, i, j, k);
+    if (ms[n] == 0)
+      solve_distance(ph[nidx(g, i - w.di, j, k)], ph[nidx(g, i, j - w.dj, k)],
+                     ph[nidx(g, i, j, k - w.dk)], &ph[n]);
+  }
+}
+
 // DEFOR_SOLID_3D::sweepPhi x2 (DEFOR_SOLID_3D.cpp:397-455, 267).
 __global__ void k_sweep_phi(GridDev g, SolidDev s, Box ex, int repeats) {
   for (int rep = 0; rep < repeats; rep++)
@@ -444,6 +460,113 @@ __device__ void sweep_vec_pass(const GridDev& g, double* f, const double* ph, co
   }
 }
 
+// First trigger rank of the three pass-long flags of sweepOnePass, by
+// atomicMin over all nodes of the pass (ranks: long long loop order).
+__global__ void k_sweep_vec_ranks(GridDev g, const double* ph, const double* ms, Sweep w,
+                                  unsigned long long* ranks) {
+  __shared__ unsigned long long sm[3];
+  if (threadIdx.x < 3) sm[threadIdx.x] = ~0ull;
+  __syncthreads();
+  unsigned long long r0 = ~0ull, r1 = ~0ull, r2 = ~0ull;
+  const long long nij = (long long)w.ni * w.nj, total = nij * w.nk;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    int a = (int)(t % w.ni), b = (int)((t / w.ni) % w.nj), c = (int)(t / nij);
+    int i = w.i0 + a * w.di, j = w.j0 + b * w.dj, k = w.k0 + c * w.dk;
+    long long n = nidx(g, i, j, k);
+    if (ms[n] != 0) continue;
+    double pn = ph[n];
+    double dp = pn - ph[nidx(g, i - w.di, j, k)], dpn = pn - ph[nidx(g, i + w.di, j, k)];
+    if (dp < 0 && dpn >= 0) continue;
+    if (dp < 0 && dpn < 0 && (unsigned long long)t < r0) r0 = t;
+    double dq = pn - ph[nidx(g, i, j - w.dj, k)], dqn = pn - ph[nidx(g, i, j + w.dj, k)];
+    if (dq < 0 && dqn >= 0) continue;
+    if (dq < 0 && dqn < 0 && (unsigned long long)t < r1) r1 = t;
+    double dr = pn - ph[nidx(g, i, j, k - w.dk)], drn = pn - ph[nidx(g, i, j, k + w.dk)];
+    if (dr < 0 && drn >= 0) continue;
+    if (dr < 0 && drn < 0 && (unsigned long long)t < r2) r2 = t;
+  }
+  // one shared-memory and one global atomic per block and flag
+  if (r0 != ~0ull) atomicMin(&sm[0], r0);
+  if (r1 != ~0ull) atomicMin(&sm[1], r1);
+  if (r2 != ~0ull) atomicMin(&sm[2], r2);
+  __syncthreads();
+  if (threadIdx.x < 3 && sm[threadIdx.x] != ~0ull) atomicMin(&ranks[threadIdx.x], sm[threadIdx.x]);
+}
+// One hyperplane of a sweepOnePass pass (flags resolved from the ranks).
+__global__ void k_sweep_vec_plane(GridDev g, double* f, const double* ph, const double* ms, Sweep w,
+                                  int p, const unsigned long long* ranks) {
+  const long long nij = (long long)w.ni * w.nj;
+  const unsigned long long rx = ranks[0], ry = ranks[1], rz = ranks[2];
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nij;
+       t += (long long)gridDim.x * blockDim.x) {
+    int a = (int)(t % w.ni), b = (int)(t / w.ni);
+    int c = p - a - b;
+    if (c < 0 || c >= w.nk) continue;
+    int i = w.i0 + a * w.di, j = w.j0 + b * w.dj, k = w.k0 + c * w.dk;
+    long long n = nidx(g, i, j, k);
+    if (ms[n] != 0) continue;
+    unsigned long long rank = (unsigned long long)(a + (long long)b * w.ni + (long long)c * nij);
+    double pn = ph[n];
+    double dp = pn - ph[nidx(g, i - w.di, j, k)], dpn = pn - ph[nidx(g, i + w.di, j, k)];
+    if (dp < 0 && dpn >= 0) continue;
+    double dq = pn - ph[nidx(g, i, j - w.dj, k)], dqn = pn - ph[nidx(g, i, j + w.dj, k)];
+    if (dq < 0 && dqn >= 0) continue;
+    double dr = pn - ph[nidx(g, i, j, k - w.dk)], drn = pn - ph[nidx(g, i, j, k + w.dk)];
+    if (dr < 0 && drn >= 0) continue;
+    if (rank >= rx) dp = 0;
+    if (rank >= ry) dq = 0;
+    if (rank >= rz) dr = 0;
+    double alpha, beta;
+    if (dp + dq + dr < 1e-3) {
+      alpha = 0.333;
+      beta = 0.333;
+    } else {
+      alpha = dp / (dp + dq + dr);
+      beta = dq / (dp + dq + dr);
+    }
+    long long ea = nidx(g, i - w.di, j, k), eb = nidx(g, i, j - w.dj, k), ec = nidx(g, i, j, k - w.dk);
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+      f[3 * n + q] = (alpha * f[3 * ea + q] + beta * f[3 * eb + q]) + (1 - alpha - beta) * f[3 * ec + q];
+  }
+}
+// Face copies of sweepVectorField (DEFOR_SOLID_3D.cpp:544-563), one axis
+// per launch, in the order z, y, x.
+__global__ void k_extend_faces(GridDev g, double* f, const double* ms, Box ex, int axis) {
+  int a0, a1;
+  if (axis == 2) {
+    a0 = 0;
+    a1 = 1;
+  } else if (axis == 1) {
+    a0 = 0;
+    a1 = 2;
+  } else {
+    a0 = 1;
+    a1 = 2;
+  }
+  const long long n0 = ex.hi[a0] - ex.lo[a0], n1 = ex.hi[a1] - ex.lo[a1];
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n0 * n1;
+       t += (long long)gridDim.x * blockDim.x) {
+    int c[3];
+    c[a0] = ex.lo[a0] + (int)(t % n0);
+    c[a1] = ex.lo[a1] + (int)(t / n0);
+    int cc[3] = {c[0], c[1], c[2]};
+    cc[axis] = ex.lo[axis];
+    long long A = nidx(g, cc[0], cc[1], cc[2]);
+    cc[axis] = ex.lo[axis] + 1;
+    long long B = nidx(g, cc[0], cc[1], cc[2]);
+    if (ms[A] == 0)
+      for (int q = 0; q < 3; q++) f[3 * A + q] = f[3 * B + q];
+    cc[axis] = ex.hi[axis] - 1;
+    A = nidx(g, cc[0], cc[1], cc[2]);
+    cc[axis] = ex.hi[axis] - 2;
+    B = nidx(g, cc[0], cc[1], cc[2]);
+    if (ms[A] == 0)
+      for (int q = 0; q < 3; q++) f[3 * A + q] = f[3 * B + q];
+  }
+}
+
 // extendVectorField = 4 x sweepVectorField (DEFOR_SOLID_3D.cpp:521-574).
 __global__ void __launch_bounds__(1024) k_extend_velocity(GridDev g, SolidDev s, Box ex) {
   __shared__ long long sh[32];
@@ -548,13 +671,27 @@ __global__ void k_seed_particles(GridDev g, SolidDev s, const long long* cellLis
   }
 }
 
-// cubic B-spline weight of gridToParticle/particleToGrid (DEFOR_SOLID_3D.cpp:928-935)
+// cubic B-spline weight of gridToParticle/particleToGrid
+// (DEFOR_SOLID_3D.cpp:928-935); |d|^3 as a product (the reference's
+// pow(d, 3) agrees to an ulp).
 __device__ __forceinline__ double bspline(double d) {
   double a = fabs(d);
-  double c = fabs(pow(d, 3.0));
+  double c = a * a * a;
   if (a < 1) return 0.5 * c - d * d + 2.0 / 3;
   if (a < 2) return -1.0 / 6 * c + d * d - 2 * a + 4.0 / 3;
   return 0;
+}
+// The 4 weights per axis of a particle's 4^3 stencil, whose first node is
+// floor((p - o)/dh) - 1 on each axis: w[4*axis + k] for node base + k.
+__device__ __forceinline__ void stencil_weights(const GridDev& g, const double* pos, int base[3],
+                                                double w[12]) {
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    base[q] = (int)floor((pos[q] - g.o[q]) / g.dh) - 1;
+    const double f = g.dhInv * (pos[q] - g.o[q]);
+#pragma unroll
+    for (int k = 0; k < 4; k++) w[4 * q + k] = bspline(f - (base[q] + k));
+  }
 }
 
 struct ContactParams {
@@ -574,15 +711,16 @@ __global__ void k_grid_to_particle(GridDev g, SolidDev s, long long np, double* 
     int j = (int)floor((pos[1] - g.o[1]) / g.dh) - 1;
     int k = (int)floor((pos[2] - g.o[2]) / g.dh) - 1;
     double pic[3] = {0, 0, 0}, flip[3] = {0, 0, 0};
-    double base[3];
-    for (int q = 0; q < 3; q++) base[q] = g.dhInv * (pos[q] - g.o[q]);
+    int bb[3];
+    double wt[12];
+    stencil_weights(g, pos, bb, wt);
     for (int r = k; r < k + 4; r++)
       for (int t = j; t < j + 4; t++)
         for (int sx = i; sx < i + 4; sx++) {
           if (sx < 0 || t < 0 || r < 0 || sx > g.X - 1 || t > g.Y - 1 || r > g.Z - 1) continue;
           long long n = nidx(g, sx, t, r);
           if (s.mass[n] == 0) continue;
-          double w = bspline(base[0] - sx) * bspline(base[1] - t) * bspline(base[2] - r);
+          double w = wt[sx - i] * wt[4 + t - j] * wt[8 + r - k];
           for (int q = 0; q < 3; q++) {
             double v = s.vel[3 * n + q];
             pic[q] += v * w;
@@ -643,13 +781,15 @@ __global__ void k_grid_to_particle(GridDev g, SolidDev s, long long np, double* 
 // (X+3)(Y+3)(Z+3) lattice; particles whose stencil misses the grid get the
 // key `nkeys` (sorted last, never gathered).
 __global__ void k_p2g_keys(GridDev g, long long np, const double* part, unsigned int* keys,
-                           unsigned int* vals, int* pbox) {
+                           unsigned int* vals, int* pbox, double* pw) {
   const long long KX = g.X + 3, KY = g.Y + 3, KZ = g.Z + 3;
   FOR_N(np, c) {
     const double* P = part + 10 * c;
-    int i = (int)floor((P[0] - g.o[0]) / g.dh) - 1;
-    int j = (int)floor((P[1] - g.o[1]) / g.dh) - 1;
-    int k = (int)floor((P[2] - g.o[2]) / g.dh) - 1;
+    int bb[3];
+    double wt[12];
+    stencil_weights(g, P, bb, wt);
+    for (int q = 0; q < 12; q++) pw[12 * c + q] = wt[q];
+    int i = bb[0], j = bb[1], k = bb[2];
     unsigned int key = (unsigned int)(KX * KY * KZ);
     if (i >= -3 && i <= g.X - 1 && j >= -3 && j <= g.Y - 1 && k >= -3 && k <= g.Z - 1) {
       key = (unsigned int)((i + 3) + KX * ((j + 3) + KY * (k + 3)));
@@ -677,8 +817,8 @@ __global__ void k_bucket_bounds(long long np, const unsigned int* skeys, int* bs
 // per-node gather over the 4^3 buckets whose stencils reach the node, in
 // bucket order then particle order (deterministic).
 __global__ void k_p2g_gather(GridDev g, SolidDev s, Box nodes, const double* part,
-                             const unsigned int* sval, const int* bstart, const int* bend,
-                             int cutoff) {
+                             const double* pw, const unsigned int* sval, const int* bstart,
+                             const int* bend, int cutoff) {
   const long long KX = g.X + 3, KY = g.Y + 3;
   FOR_BOX(nodes, x, y, z) {
     double acc[4] = {0, 0, 0, 0};
@@ -689,10 +829,12 @@ __global__ void k_p2g_gather(GridDev g, SolidDev s, Box nodes, const double* par
           if (bx < -3 || by < -3 || bz < -3) continue;
           long long key = (bx + 3) + KX * ((by + 3) + KY * (long long)(bz + 3));
           int b0 = bstart[key], b1 = bend[key];
+          const int ox = x - bx, oy = 4 + y - by, oz = 8 + z - bz;
           for (int e = b0; e < b1; e++) {
-            const double* P = part + 10 * (long long)sval[e];
-            double w = bspline(g.dhInv * (P[0] - g.o[0]) - x) * bspline(g.dhInv * (P[1] - g.o[1]) - y) *
-                       bspline(g.dhInv * (P[2] - g.o[2]) - z);
+            const long long pi = sval[e];
+            const double* P = part + 10 * pi;
+            const double* W = pw + 12 * pi;
+            double w = W[ox] * W[oy] * W[oz];
             touched = true;
             acc[0] += w * P[3];
             acc[1] += w * P[4];
@@ -1186,8 +1328,8 @@ __global__ void k_assemble(GridDev g, SolidDev s, const int* sdof, const long lo
         }
       }
     }
-    double* B = blocks + 243 * a + 9 * j;
-    for (int e = 0; e < 9; e++) B[e] = present ? blk[e] * scale : 0.0;
+    // entry-major layout: blocks[(j * 9 + e) * S + a]
+    for (int e = 0; e < 9; e++) blocks[((long long)j * 9 + e) * S + a] = present ? blk[e] * scale : 0.0;
     if (j == 13) {
       present = true;  // coeffRef(i, i) creates the diagonal entries
       // force: cells containing n in increasing index, corner ia
@@ -1201,7 +1343,7 @@ __global__ void k_assemble(GridDev g, SolidDev s, const int* sdof, const long lo
       }
       for (int r = 0; r < 3; r++) force[3 * a + r] = f[r];
     }
-    nbr[t] = present ? mdof : -1;
+    nbr[(long long)j * S + a] = present ? mdof : -1;
     unsigned int bit = present ? (1u << j) : 0u;
     if (bit) atomicOr((unsigned int*)&mask[a], bit);
   }
@@ -1221,7 +1363,7 @@ __global__ void k_add_diag(long long S, const double* damped, double* blocks, do
   FOR_N(3 * S, i) {
     long long a = i / 3;
     int r = (int)(i % 3);
-    double* e = blocks + 243 * a + 9 * 13 + 4 * r;
+    double* e = blocks + (13LL * 9 + 4 * r) * S + a;
     *e = *e + damped[i];
     diag[i] = *e;
   }

@@ -10,7 +10,9 @@
 //  * FP32 inner solves inside FP64 iterative refinement (ESF_MIXED);
 //  * the solid system (M + dt^2 K) in 27-neighbour 3x3 block rows.
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
+#include <chrono>
 
 #include <vector>
 
@@ -65,11 +67,19 @@ __device__ bool last_block_sum(double mine, double* partial, unsigned int* ticke
 // every 5th iteration; inner solves of a refinement stop as soon as the
 // preconditioned residual's energy r.Ar has fallen by eps^2.
 __device__ __forceinline__ void finish_update(PcrState* st, double total) {
-  if (st->setup) {
+  if (st->rebase) {
+    // residual replaced by an FP64 recompute: the direction is kept
+    st->beta = total / st->delta;
+    st->delta = total;
+    st->delta0 = total;
+    st->rebase = 0;
+    st->iter0 = st->iter;
+  } else if (st->setup) {
     st->delta = total;
     st->delta0 = total;
     st->beta = 0.0;
     st->setup = 0;
+    st->iter0 = st->iter;
     if (st->inner && !(total > 0.0)) {  // zero right-hand side: nothing to do
       st->converged = 1;
       st->done = 1;
@@ -79,7 +89,8 @@ __device__ __forceinline__ void finish_update(PcrState* st, double total) {
     st->delta = total;
     if (st->inner) {
       st->iter++;
-      if (total <= st->eps * st->eps * st->delta0) {
+      if (total <= st->eps * st->eps * st->delta0 ||
+          (st->cap > 0 && st->iter - st->iter0 >= st->cap)) {
         st->converged = 1;
         st->done = 1;
       }
@@ -173,9 +184,13 @@ __global__ void __launch_bounds__(NT) pressure_stencil(GridDev g, StencilArgs<T>
   const bool cin = cgx < g.cX && cgy < g.cY;
   const long long ccol = cgx + (long long)cgy * g.cX;
   double acc = 0.0;
+  // r.s of this thread's cells: at most 32 terms, kept in T (the FP64 pipe
+  // is a small fraction of the FP32 one) and widened once per thread
+  T accT = 0;
 
-  // register prefetch of one layer: stencil input pieces + node m^-1
-  T pr[2], pa[2], pi[2], pm[2];
+  // register prefetch of one layer: stencil input pieces, x and d of the
+  // tile's own cells, node m^-1
+  T pr[2], pa[2], pi[2], pm[2], px[2], pd[2];
   auto fetch = [&](int kk) {
     const bool layerOk = kk >= 0 && kk < g.cZ;
 #pragma unroll
@@ -183,12 +198,18 @@ __global__ void __launch_bounds__(NT) pressure_stencil(GridDev g, StencilArgs<T>
       pr[q] = 0;
       pa[q] = 0;
       pi[q] = 0;
+      px[q] = 0;
+      pd[q] = 0;
       if (hin[q] && layerOk) {
         const long long c = hc[q] + (long long)kk * g.cslab;
         if (MODE == S_UPDATE) {
           pr[q] = a.r[c];
           pa[q] = a.Ap[c];
           pi[q] = a.invd[c];
+          if (hown[q] && kk >= z0 && kk < z1) {
+            px[q] = a.x[c];
+            pd[q] = a.d[c];
+          }
         } else {
           pr[q] = a.in[c];
         }
@@ -200,13 +221,15 @@ __global__ void __launch_bounds__(NT) pressure_stencil(GridDev g, StencilArgs<T>
   fetch(z0 - 1);
   for (int kk = z0 - 1; kk <= z1; kk++) {
     const int vb = kk & 1;
-    T cr[2], ca[2], ci[2], cm[2];
+    T cr[2], ca[2], ci[2], cm[2], cxv[2], cdv[2];
 #pragma unroll
     for (int q = 0; q < 2; q++) {
       cr[q] = pr[q];
       ca[q] = pa[q];
       ci[q] = pi[q];
       cm[q] = pm[q];
+      cxv[q] = px[q];
+      cdv[q] = pd[q];
     }
     if (kk < z1) fetch(kk + 1);  // in flight while this layer computes
     // (a) stencil input of cell layer kk
@@ -220,7 +243,7 @@ __global__ void __launch_bounds__(NT) pressure_stencil(GridDev g, StencilArgs<T>
         v = upd_r(cr[q], alpha, ca[q], ci[q]);
         if (hown[q] && kk >= z0 && kk < z1) {
           const long long c = hc[q] + (long long)kk * g.cslab;
-          a.x[c] = a.x[c] + alpha * a.d[c];
+          a.x[c] = cxv[q] + alpha * cdv[q];
         }
       }
       const int hs = tid + q * NT;
@@ -266,7 +289,7 @@ __global__ void __launch_bounds__(NT) pressure_stencil(GridDev g, StencilArgs<T>
       } else if (MODE == S_UPDATE) {
         a.out[c] = o;
         T rv = sV[vb][(ccx + 1) + (ccy + 1) * HX];
-        acc += (double)(rv * o);
+        accT += rv * o;
       } else if (MODE == S_CHECK) {
         double t = (double)o - (double)a.b[c];
         acc += t * t;
@@ -277,12 +300,13 @@ __global__ void __launch_bounds__(NT) pressure_stencil(GridDev g, StencilArgs<T>
       } else if (MODE == S_RESID64) {
         T rr = a.b[c] - o;
         a.r[c] = rr;
-        a.out32[c] = (float)rr;
+        a.out32[c] = a.invd ? (float)(rr * a.invd[c]) : (float)rr;
         acc += (double)rr * (double)rr;
       }
     }
   }
   if (MODE == S_APPLY) return;
+  if (MODE == S_UPDATE) acc = (double)accT;
   __syncthreads();
   double bs = block_sum<NT>(acc, sred);
   const int nblocks = gridDim.x * gridDim.y * gridDim.z;
@@ -331,7 +355,35 @@ __global__ void __launch_bounds__(VT) pcr_phase_a(long long n, T* d, T* r, T* Ap
   const T beta = (T)st->beta;
   const T alpha = (T)st->alpha;
   T acc = 0;
-  for (long long i = blockIdx.x * (long long)VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT) {
+  // four independent element chains per thread keep enough loads in flight
+  const long long stride = (long long)gridDim.x * VT;
+  long long i = blockIdx.x * (long long)VT + threadIdx.x;
+  for (; i + 3 * stride < n; i += 4 * stride) {
+    T a[4], iv[4], rv[4], dv[4], sv[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const long long j = i + u * stride;
+      a[u] = Ap[j];
+      iv[u] = invd[j];
+      rv[u] = r[j];
+      dv[u] = d[j];
+      sv[u] = s[j];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const long long j = i + u * stride;
+      if (UPDR) {
+        rv[u] = upd_r(rv[u], alpha, a[u], iv[u]);
+        r[j] = rv[u];
+      }
+      T dn = beta * dv[u] + rv[u];
+      T an = beta * a[u] + sv[u];
+      d[j] = dn;
+      Ap[j] = an;
+      acc += an * (an * iv[u]);
+    }
+  }
+  for (; i < n; i += stride) {
     T a = Ap[i], iv = invd[i], rv = r[i];
     if (UPDR) {
       rv = upd_r(rv, alpha, a, iv);
@@ -418,7 +470,7 @@ __global__ void add_correction(long long n, double* x, const float* e) {
 
 static int vec_blocks(long long n) {
   long long b = (n + VT - 1) / VT;
-  int cap = 152 * 8;
+  int cap = 152 * 8;  // 8 resident blocks of 256 threads per SM
   return (int)(b < cap ? (b > 0 ? b : 1) : cap);
 }
 
@@ -440,6 +492,8 @@ struct PressureWork {
   const void* keyB[8];
   cudaStream_t capStream;
   cudaEvent_t ev[4];
+  unsigned long long kFirst, kChunk, kFirst32, kChunk32;  // kernels per graph
+  PcrState* stT;  // state used by the kernel timer
 };
 
 // z-chunk depth: deep enough to amortise the two halo layers, shallow
@@ -466,7 +520,7 @@ esf_status pressure_apply(const GridDev& g, const T* minv, const T* in, T* out, 
   a.in = in;
   a.minv = minv;
   a.out = out;
-  pressure_stencil<T, S_APPLY><<<stencil_grid<T>(g), NT, 0, st>>>(g, a, stencil_cz(g));
+  ESF_COUNTED pressure_stencil<T, S_APPLY><<<stencil_grid<T>(g), NT, 0, st>>>(g, a, stencil_cz(g));
   ESF_LAUNCH_CHECK();
   return ESF_OK;
 }
@@ -500,6 +554,7 @@ esf_status pressure_work_alloc(PressureWork** out, const GridDev& g, int mixed) 
   ESF_CUDA(cudaMalloc(&w->partial, ESF_MAX_PARTIALS * 8));
   ESF_CUDA(cudaMalloc(&w->st, sizeof(PcrState)));
   ESF_CUDA(cudaMalloc(&w->st32, sizeof(PcrState)));
+  ESF_CUDA(cudaMalloc(&w->stT, sizeof(PcrState)));
   ESF_CUDA(cudaMemset(w->st, 0, sizeof(PcrState)));
   ESF_CUDA(cudaMemset(w->st32, 0, sizeof(PcrState)));
   ESF_CUDA(cudaMallocHost(&w->hst, 8 * sizeof(PcrState)));
@@ -514,7 +569,7 @@ void pressure_work_free(PressureWork* w) {
   cudaFree(w->r); cudaFree(w->d); cudaFree(w->Ap); cudaFree(w->s); cudaFree(w->invd);
   cudaFree(w->x32); cudaFree(w->r32); cudaFree(w->d32); cudaFree(w->Ap32); cudaFree(w->s32);
   cudaFree(w->invd32); cudaFree(w->b32); cudaFree(w->minv32);
-  cudaFree(w->partial); cudaFree(w->st); cudaFree(w->st32);
+  cudaFree(w->partial); cudaFree(w->st); cudaFree(w->st32); cudaFree(w->stT);
   if (w->hst) cudaFreeHost(w->hst);
   if (w->gFirst) cudaGraphExecDestroy(w->gFirst);
   if (w->gChunk) cudaGraphExecDestroy(w->gChunk);
@@ -538,29 +593,29 @@ struct PressureKernels {
     StencilArgs<T> a;
     memset(&a, 0, sizeof a);
     a.in = x; a.b = b; a.r = r; a.invd = invd; a.minv = minv; a.partial = partial; a.st = st;
-    pressure_stencil<T, S_RESID_INIT><<<stencil_grid<T>(g), NT, 0, cs>>>(g, a, stencil_cz(g));
-    zero2<T><<<vec_blocks(g.R), VT, 0, cs>>>(g.R, d, Ap);
+    ESF_COUNTED pressure_stencil<T, S_RESID_INIT><<<stencil_grid<T>(g), NT, 0, cs>>>(g, a, stencil_cz(g));
+    ESF_COUNTED zero2<T><<<vec_blocks(g.R), VT, 0, cs>>>(g.R, d, Ap);
     update(cs);
   }
   void setup_zero(cudaStream_t cs) const {
-    pcr_zero_start<T><<<vec_blocks(g.R), VT, 0, cs>>>(g.R, b, invd, x, r, d, Ap, partial, st);
+    ESF_COUNTED pcr_zero_start<T><<<vec_blocks(g.R), VT, 0, cs>>>(g.R, b, invd, x, r, d, Ap, partial, st);
     update(cs);
   }
   void phase_a(cudaStream_t cs) const {
-    pcr_phase_a<T, true><<<vec_blocks(g.R), VT, 0, cs>>>(g.R, d, r, Ap, s, invd, partial, st);
+    ESF_COUNTED pcr_phase_a<T, true><<<vec_blocks(g.R), VT, 0, cs>>>(g.R, d, r, Ap, s, invd, partial, st);
   }
   void update(cudaStream_t cs) const {
     StencilArgs<T> a;
     memset(&a, 0, sizeof a);
     a.x = x; a.d = d; a.r = r; a.Ap = Ap; a.invd = invd; a.minv = minv; a.out = s;
     a.partial = partial; a.st = st;
-    pressure_stencil<T, S_UPDATE><<<stencil_grid<T>(g), NT, 0, cs>>>(g, a, stencil_cz(g));
+    ESF_COUNTED pressure_stencil<T, S_UPDATE><<<stencil_grid<T>(g), NT, 0, cs>>>(g, a, stencil_cz(g));
   }
   void check(cudaStream_t cs) const {
     StencilArgs<T> a;
     memset(&a, 0, sizeof a);
     a.in = x; a.b = b; a.minv = minv; a.partial = partial; a.st = st;
-    pressure_stencil<T, S_CHECK><<<stencil_grid<T>(g), NT, 0, cs>>>(g, a, stencil_cz(g));
+    ESF_COUNTED pressure_stencil<T, S_CHECK><<<stencil_grid<T>(g), NT, 0, cs>>>(g, a, stencil_cz(g));
   }
   // iterations [i0, i0+n) followed by the residual check of iteration
   // i0+n-1 (reference solves only; inner solves stop on delta)
@@ -574,9 +629,16 @@ struct PressureKernels {
 };
 
 template <typename K>
-static esf_status capture(cudaStream_t cs, const K& k, bool first, bool warm, cudaGraphExec_t* exec) {
+static esf_status capture(cudaStream_t cs, const K& k, bool first, bool warm, cudaGraphExec_t* exec,
+                          unsigned long long* kernels) {
   cudaGraph_t graph;
-  ESF_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+  *kernels = 0;
+  set_capturing(true, kernels);
+  cudaError_t ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (ce != cudaSuccess) {
+    set_capturing(false, nullptr);
+    ESF_CUDA(ce);
+  }
   // reference solves warm-start and check every 5th iteration; inner solves
   // of a refinement start from zero and stop on delta
   if (first) {
@@ -586,6 +648,7 @@ static esf_status capture(cudaStream_t cs, const K& k, bool first, bool warm, cu
   } else {
     k.chunk(cs, 5, warm);  // iterations 5j+1 .. 5j+5
   }
+  set_capturing(false, nullptr);
   ESF_CUDA(cudaStreamEndCapture(cs, &graph));
   if (*exec) cudaGraphExecDestroy(*exec);
   ESF_CUDA(cudaGraphInstantiate(exec, graph, 0));
@@ -596,7 +659,8 @@ static esf_status capture(cudaStream_t cs, const K& k, bool first, bool warm, cu
 // Runs one PCR solve from graphs; keeps up to 3 chunks in flight and polls
 // pinned copies of the device state.
 static esf_status run_graph_solve(PressureWork* w, PcrState* dst, cudaGraphExec_t gFirst,
-                                  cudaGraphExec_t gChunk, int maxIt, cudaStream_t st,
+                                  cudaGraphExec_t gChunk, unsigned long long kFirst,
+                                  unsigned long long kChunk, int maxIt, cudaStream_t st,
                                   PcrState* out) {
   const int inflight = 3;
   int launched = 0, waited = 0;
@@ -604,7 +668,9 @@ static esf_status run_graph_solve(PressureWork* w, PcrState* dst, cudaGraphExec_
   bool done = false;
   while (!done) {
     if (launched < maxChunks) {
-      ESF_CUDA(cudaGraphLaunch(launched == 0 ? gFirst : gChunk, st));
+      const bool first = launched == 0 && gFirst;
+      ESF_CUDA(cudaGraphLaunch(first ? gFirst : gChunk, st));
+      note_graph_replay(first ? kFirst : kChunk);
       ESF_CUDA(cudaMemcpyAsync(&w->hst[launched % 4], dst, sizeof(PcrState), cudaMemcpyDeviceToHost, st));
       ESF_CUDA(cudaEventRecord(w->ev[launched % 4], st));
       launched++;
@@ -644,29 +710,36 @@ static esf_status init_state(PcrState* d, double eps, int maxIt, cudaStream_t st
 esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv64,
                           const double* diag64, const double* b, double* x, double eps, int maxIt,
                           int precision, double innerEps, int maxRefine, int* iters,
-                          double* relres, int* refinements, int* converged, cudaStream_t st) {
+                          double* relres, int* refinements, int* converged, cudaStream_t st,
+                          int* fp64Iters) {
+  if (fp64Iters) *fp64Iters = 0;
   {
     dim3 gr = stencil_grid<double>(g);
     if ((long long)gr.x * gr.y * gr.z > ESF_MAX_PARTIALS) return ESF_ERR_UNSUPPORTED;
   }
-  inv_vec<<<vec_blocks(g.R), VT, 0, st>>>(g.R, diag64, w->invd, w->invd32);
+  ESF_COUNTED inv_vec<<<vec_blocks(g.R), VT, 0, st>>>(g.R, diag64, w->invd, w->invd32);
   ESF_LAUNCH_CHECK();
-  if (precision == ESF_FP64) {
+  // FP64 PCR from the warm start x (the reference's solvePCR): two kernels
+  // per iteration replayed as graphs, true-residual check every 5th.
+  auto fp64_solve = [&](int itCap, PcrState* out) -> esf_status {
     PressureKernels<double> k{g, minv64, w->invd, b, x, w->r, w->d, w->Ap, w->s, w->partial, w->st};
     const void* key[8] = {minv64, diag64, b, x, nullptr, nullptr, nullptr, nullptr};
     bool rebuild = !w->graphsFor64 || memcmp(key, w->keyA, sizeof key) != 0;
     if (rebuild) {
-      esf_status e = capture(w->capStream, k, true, true, &w->gFirst);
+      esf_status e = capture(w->capStream, k, true, true, &w->gFirst, &w->kFirst);
       if (e) return e;
-      e = capture(w->capStream, k, false, true, &w->gChunk);
+      e = capture(w->capStream, k, false, true, &w->gChunk, &w->kChunk);
       if (e) return e;
       memcpy(w->keyA, key, sizeof key);
       w->graphsFor64 = true;
     }
-    esf_status e = init_state(w->st, eps, maxIt, st);
+    esf_status e = init_state(w->st, eps, itCap, st);
     if (e) return e;
+    return run_graph_solve(w, w->st, w->gFirst, w->gChunk, w->kFirst, w->kChunk, itCap, st, out);
+  };
+  if (precision == ESF_FP64) {
     PcrState h;
-    e = run_graph_solve(w, w->st, w->gFirst, w->gChunk, maxIt, st, &h);
+    esf_status e = fp64_solve(maxIt, &h);
     if (e) return e;
     if (iters) *iters = h.iter;
     if (converged) *converged = h.converged;
@@ -674,70 +747,224 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
     if (relres) *relres = h.bnorm2 > 0 ? sqrt(h.resid2 / h.bnorm2) : sqrt(h.resid2);
     return h.status ? (esf_status)h.status : ESF_OK;
   }
-  // ---- mixed: FP32 inner PCR inside FP64 iterative refinement
-  convert_vec<double, float><<<vec_blocks(g.T), VT, 0, st>>>(g.T, minv64, w->minv32);
+  // ---- mixed: FP32 inner CR solves (stencil, vectors and updates in FP32,
+  // dot products and alpha/beta in FP64) inside FP64 iterative refinement:
+  // r = b - A x in FP64; solve A e = r in FP32 from e = 0 until the inner
+  // residual energy r.Ar has fallen by innerEps^2, or by the smaller ratio
+  // that predicts the outer tolerance; x += e in FP64; repeat until
+  // ||b - A x|| < eps ||b||. Capping the inner solves does not work here:
+  // short restarted solves stall near 2e-8 on a 256^3 scene, because the
+  // slow modes of this operator need long Krylov runs. If the refinements run
+  // out before the tolerance is met, FP64 PCR finishes from the refined x.
+  // Each inner solve restarts its Krylov space: carrying the direction across
+  // the FP64 residual replacement stalls near 1e-7, because FP32 rounding
+  // feeds the operator's near-null checkerboard modes (J J^T on the
+  // node-collocated grid).
+  ESF_COUNTED convert_vec<double, float><<<vec_blocks(g.T), VT, 0, st>>>(g.T, minv64, w->minv32);
   PressureKernels<float> k32{g, w->minv32, w->invd32, w->b32, w->x32, w->r32, w->d32, w->Ap32,
                              w->s32, w->partial, w->st32};
   const void* key[8] = {w->minv32, w->invd32, w->b32, w->x32, nullptr, nullptr, nullptr, nullptr};
   if (!w->graphsFor32 || memcmp(key, w->keyB, sizeof key) != 0) {
-    esf_status e = capture(w->capStream, k32, true, false, &w->gFirst32);
-    if (e) return e;
-    e = capture(w->capStream, k32, false, false, &w->gChunk32);
+    esf_status e = capture(w->capStream, k32, false, false, &w->gChunk32, &w->kChunk32);
     if (e) return e;
     memcpy(w->keyB, key, sizeof key);
     w->graphsFor32 = true;
   }
-  int total = 0, ref = 0, conv = 0;
-  double bnorm2 = -1, rel = 0;
-  esf_status status = ESF_OK;
-  for (ref = 0; ref <= maxRefine; ref++) {
-    // r = b - A x in FP64 (also ||b||^2 the first time)
+  // ||b||
+  {
     esf_status e = init_state(w->st, eps, maxIt, st);
     if (e) return e;
+  }
+  ESF_COUNTED vec_norm2<double><<<vec_blocks(g.R), VT, 0, st>>>(g.R, b, w->partial + ESF_MAX_PARTIALS / 2,
+                                                    &w->st->ticket[3], &w->st->bnorm2);
+  ESF_LAUNCH_CHECK();
+  // r64 = b - A x (FP64), r32 = (b - A x)/diag in FP32, ||r64||^2
+  auto true_residual = [&](double* resid2, double* bnorm2) -> esf_status {
     StencilArgs<double> a;
     memset(&a, 0, sizeof a);
-    a.in = x; a.b = b; a.r = w->r; a.out32 = w->b32; a.minv = minv64; a.partial = w->partial;
-    a.st = w->st;
-    pressure_stencil<double, S_RESID64><<<stencil_grid<double>(g), NT, 0, st>>>(g, a, stencil_cz(g));
+    a.in = x; a.b = b; a.r = w->r; a.out32 = w->r32; a.invd = w->invd; a.minv = minv64;
+    a.partial = w->partial; a.st = w->st;
+    ESF_COUNTED pressure_stencil<double, S_RESID64><<<stencil_grid<double>(g), NT, 0, st>>>(g, a, stencil_cz(g));
     ESF_LAUNCH_CHECK();
-    if (bnorm2 < 0) {
-      vec_norm2<double><<<vec_blocks(g.R), VT, 0, st>>>(g.R, b, w->partial + ESF_MAX_PARTIALS / 2,
-                                                      &w->st->ticket[3], &w->st->bnorm2);
-      ESF_LAUNCH_CHECK();
-    }
     PcrState h;
     ESF_CUDA(cudaMemcpyAsync(&h, w->st, sizeof h, cudaMemcpyDeviceToHost, st));
     ESF_CUDA(cudaStreamSynchronize(st));
-    if (bnorm2 < 0) bnorm2 = h.bnorm2;
-    rel = bnorm2 > 0 ? sqrt(h.resid2 / bnorm2) : sqrt(h.resid2);
-    if (!(h.resid2 == h.resid2)) {
-      status = ESF_ERR_NUMERIC;
-      break;
-    }
-    if (sqrt(h.resid2) < eps * sqrt(bnorm2)) {
-      conv = 1;
-      break;
-    }
-    if (ref == maxRefine || total >= maxIt) break;
-    // inner FP32 solve of A e = r from e = 0
-    e = init_state(w->st32, innerEps, maxIt - total, st, 1);
+    *resid2 = h.resid2;
+    *bnorm2 = h.bnorm2;
+    return ESF_OK;
+  };
+  double resid2 = 0, bnorm2 = 0;
+  {
+    esf_status e = true_residual(&resid2, &bnorm2);
     if (e) return e;
-    PcrState hi;
-    e = run_graph_solve(w, w->st32, w->gFirst32, w->gChunk32, maxIt - total, st, &hi);
-    if (e) return e;
-    total += hi.iter + (hi.converged ? 0 : 0);
-    if (hi.status) {
-      status = (esf_status)hi.status;
-      break;
+  }
+  const double bnorm = sqrt(bnorm2);
+  double rel = bnorm > 0 ? sqrt(resid2) / bnorm : sqrt(resid2);
+  int total = 0, ref = 0, conv = 0;
+  esf_status status = ESF_OK;
+  // inner stopping ratio on delta/delta0 for the next inner solve
+  auto trigger = [&](double r2) {
+    double t = innerEps;
+    double target = (r2 > 0) ? 0.5 * eps * bnorm / sqrt(r2) : 0.0;  // predicted convergence
+    return (target > t) ? target : t;
+  };
+  if (!(resid2 == resid2)) {
+    status = ESF_ERR_NUMERIC;
+  } else if (sqrt(resid2) < eps * bnorm) {
+    conv = 1;
+  } else {
+    ESF_CUDA(cudaMemsetAsync(w->x32, 0, g.R * 4, st));
+    ESF_CUDA(cudaMemsetAsync(w->d32, 0, g.R * 4, st));
+    ESF_CUDA(cudaMemsetAsync(w->Ap32, 0, g.R * 4, st));
+    {
+      PcrState h;
+      memset(&h, 0, sizeof h);
+      h.eps = trigger(resid2);
+      h.maxIt = maxIt;
+      h.setup = 1;
+      h.inner = 1;
+      ESF_CUDA(cudaMemcpyAsync(w->st32, &h, sizeof h, cudaMemcpyHostToDevice, st));
+      ESF_CUDA(cudaStreamSynchronize(st));
     }
-    add_correction<<<vec_blocks(g.R), VT, 0, st>>>(g.R, x, w->x32);
+    k32.update(st);  // s = A r, delta (set-up: alpha = 0)
     ESF_LAUNCH_CHECK();
+    const bool trace = getenv("ESF_TRACE") != nullptr;
+    auto t0 = std::chrono::steady_clock::now();
+    for (ref = 0; ref < maxRefine; ref++) {
+      if (trace) {
+        double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        fprintf(stderr, "[esf] refine %d at %.2f ms: iters %d rel %.3e\n", ref, ms, total, rel);
+      }
+      PcrState hi;
+      esf_status e = run_graph_solve(w, w->st32, nullptr, w->gChunk32, 0, w->kChunk32,
+                                     maxIt, st, &hi);
+      if (e) return e;
+      total = hi.iter;
+      if (hi.status) {
+        status = (esf_status)hi.status;
+        break;
+      }
+      // refinement: fold the FP32 partial solution into x, recompute r
+      ESF_COUNTED add_correction<<<vec_blocks(g.R), VT, 0, st>>>(g.R, x, w->x32);
+      ESF_CUDA(cudaMemsetAsync(w->x32, 0, g.R * 4, st));
+      e = true_residual(&resid2, &bnorm2);
+      if (e) return e;
+      rel = bnorm > 0 ? sqrt(resid2) / bnorm : sqrt(resid2);
+      if (!(resid2 == resid2)) {
+        status = ESF_ERR_NUMERIC;
+        break;
+      }
+      if (sqrt(resid2) < eps * bnorm) {
+        conv = 1;
+        ref++;
+        break;
+      }
+      if (total >= maxIt) break;
+      // restart the inner recurrence from the new residual (iteration count
+      // carries over)
+      ESF_CUDA(cudaMemsetAsync(w->d32, 0, g.R * 4, st));
+      ESF_CUDA(cudaMemsetAsync(w->Ap32, 0, g.R * 4, st));
+      hi.done = 0;
+      hi.converged = 0;
+      hi.alpha = 0.0;
+      hi.beta = 0.0;
+      hi.setup = 1;
+      hi.eps = trigger(resid2);
+      memset(hi.ticket, 0, sizeof hi.ticket);
+      ESF_CUDA(cudaMemcpyAsync(w->st32, &hi, sizeof hi, cudaMemcpyHostToDevice, st));
+      ESF_CUDA(cudaStreamSynchronize(st));
+      k32.update(st);
+      ESF_LAUNCH_CHECK();
+    }
+  }
+  if (!conv && ref >= maxRefine && status == ESF_OK && total < maxIt) {
+    // FP64 finish from the refined iterate
+    PcrState h;
+    esf_status e = fp64_solve(maxIt - total, &h);
+    if (e) return e;
+    total += h.iter;
+    conv = h.converged;
+    rel = h.bnorm2 > 0 ? sqrt(h.resid2 / h.bnorm2) : sqrt(h.resid2);
+    if (h.status) status = (esf_status)h.status;
+    if (fp64Iters) *fp64Iters = h.iter;
   }
   if (iters) *iters = total;
   if (refinements) *refinements = ref;
   if (relres) *relres = rel;
   if (converged) *converged = conv;
   return status;
+}
+
+// Kernel timer: the two per-iteration kernels of the scene's precision on
+// scratch vectors seeded from b (the solution x and the solve state are not
+// touched), averaged over `reps` launches with CUDA events on `st`.
+template <typename T>
+static esf_status time_kernels_t(PressureWork* w, const GridDev& g, const T* minv, const T* invd,
+                                 const T* bsrc, T* x, T* r, T* d, T* Ap, T* s, int reps,
+                                 double* upd, double* ax, cudaStream_t st) {
+  const long long R = g.R;
+  ESF_CUDA(cudaMemcpyAsync(r, bsrc, R * sizeof(T), cudaMemcpyDeviceToDevice, st));
+  ESF_CUDA(cudaMemcpyAsync(d, bsrc, R * sizeof(T), cudaMemcpyDeviceToDevice, st));
+  ESF_CUDA(cudaMemcpyAsync(Ap, bsrc, R * sizeof(T), cudaMemcpyDeviceToDevice, st));
+  ESF_CUDA(cudaMemcpyAsync(s, bsrc, R * sizeof(T), cudaMemcpyDeviceToDevice, st));
+  ESF_CUDA(cudaMemsetAsync(x, 0, R * sizeof(T), st));
+  PcrState h;
+  memset(&h, 0, sizeof h);
+  h.alpha = 1e-3;
+  h.beta = 1e-3;
+  h.delta = 1.0;
+  h.iter = 1;
+  h.maxIt = 1 << 30;
+  h.eps = 0;
+  h.inner = 1;
+  ESF_CUDA(cudaMemcpyAsync(w->stT, &h, sizeof h, cudaMemcpyHostToDevice, st));
+  ESF_CUDA(cudaStreamSynchronize(st));
+  PressureKernels<T> k{g, minv, invd, bsrc, x, r, d, Ap, s, w->partial, w->stT};
+  cudaEvent_t e0, e1, e2;
+  ESF_CUDA(cudaEventCreate(&e0));
+  ESF_CUDA(cudaEventCreate(&e1));
+  ESF_CUDA(cudaEventCreate(&e2));
+  k.update(st);  // warm-up
+  k.phase_a(st);
+  ESF_CUDA(cudaEventRecord(e0, st));
+  for (int i = 0; i < reps; i++) k.update(st);
+  ESF_CUDA(cudaEventRecord(e1, st));
+  for (int i = 0; i < reps; i++) k.phase_a(st);
+  ESF_CUDA(cudaEventRecord(e2, st));
+  ESF_CUDA(cudaEventSynchronize(e2));
+  float t1 = 0, t2 = 0;
+  cudaEventElapsedTime(&t1, e0, e1);
+  cudaEventElapsedTime(&t2, e1, e2);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  *upd = t1 / reps;
+  *ax = t2 / reps;
+  return ESF_OK;
+}
+
+esf_status pressure_time_kernels(PressureWork* w, const GridDev& g, const double* minv64,
+                                 const double* diag64, const double* b, const double* x,
+                                 int precision, int reps, double* update_ms, double* axpy_ms,
+                                 cudaStream_t st) {
+  (void)x;
+  ESF_COUNTED inv_vec<<<vec_blocks(g.R), VT, 0, st>>>(g.R, diag64, w->invd, w->invd32);
+  if (precision == ESF_MIXED) {
+    if (!w->x32) return ESF_ERR_STATE;
+    ESF_COUNTED convert_vec<double, float><<<vec_blocks(g.T), VT, 0, st>>>(g.T, minv64, w->minv32);
+    ESF_COUNTED convert_vec<double, float><<<vec_blocks(g.R), VT, 0, st>>>(g.R, b, w->b32);
+    ESF_LAUNCH_CHECK();
+    return time_kernels_t<float>(w, g, w->minv32, w->invd32, w->b32, w->x32, w->r32, w->d32,
+                                 w->Ap32, w->s32, reps, update_ms, axpy_ms, st);
+  }
+  // FP64: x scratch is w->s's neighbour; use the FP64 work arrays only
+  double* xs = nullptr;
+  ESF_CUDA(cudaMalloc(&xs, g.R * 8));
+  esf_status e = time_kernels_t<double>(w, g, minv64, w->invd, b, xs, w->r, w->d, w->Ap, w->s, reps,
+                                        update_ms, axpy_ms, st);
+  cudaStreamSynchronize(st);
+  cudaFree(xs);
+  return e;
 }
 
 // -------------------------------------------------------- solid solver
@@ -751,19 +978,21 @@ __global__ void __launch_bounds__(VT) solid_spmv(long long S, const T* __restric
   __shared__ double sred[32];
   if (MODE != S_APPLY && st->done) return;
   double acc = 0;
+  T accT = 0;
   for (long long a = blockIdx.x * (long long)VT + threadIdx.x; a < S; a += (long long)gridDim.x * VT) {
     T y0 = 0, y1 = 0, y2 = 0;
-    const T* B = blocks + a * 243;
-    const int* nb = nbr + a * 27;
+    // blocks are stored entry-major, B[(j * 9 + e) * S + a]: consecutive
+    // threads read consecutive words
+    const int* nb = nbr + a;
 #pragma unroll 1
     for (int j = 0; j < 27; j++) {
-      int m = nb[j];
+      int m = nb[(long long)j * S];
       if (m < 0) continue;
       T v0 = in[3 * (long long)m], v1 = in[3 * (long long)m + 1], v2 = in[3 * (long long)m + 2];
-      const T* Bj = B + 9 * j;
-      y0 += Bj[0] * v0 + Bj[1] * v1 + Bj[2] * v2;
-      y1 += Bj[3] * v0 + Bj[4] * v1 + Bj[5] * v2;
-      y2 += Bj[6] * v0 + Bj[7] * v1 + Bj[8] * v2;
+      const T* Bj = blocks + (long long)j * 9 * S + a;
+      y0 += Bj[0] * v0 + Bj[S] * v1 + Bj[2 * S] * v2;
+      y1 += Bj[3 * S] * v0 + Bj[4 * S] * v1 + Bj[5 * S] * v2;
+      y2 += Bj[6 * S] * v0 + Bj[7 * S] * v1 + Bj[8 * S] * v2;
     }
     T y[3] = {y0, y1, y2};
 #pragma unroll
@@ -773,7 +1002,7 @@ __global__ void __launch_bounds__(VT) solid_spmv(long long S, const T* __restric
         out[i] = y[c];
       } else if (MODE == S_UPDATE) {
         out[i] = y[c];
-        acc += (double)(in[i] * y[c]);
+        accT += in[i] * y[c];
       } else if (MODE == S_CHECK) {
         double t = (double)y[c] - (double)b[i];
         acc += t * t;
@@ -786,6 +1015,7 @@ __global__ void __launch_bounds__(VT) solid_spmv(long long S, const T* __restric
     }
   }
   if (MODE == S_APPLY) return;
+  if (MODE == S_UPDATE) acc = (double)accT;
   double bs = block_sum<VT>(acc, sred);
   double total;
   if (last_block_sum<VT>(bs, partial, &st->ticket[1], gridDim.x, &total, sred) &&
@@ -824,6 +1054,8 @@ __global__ void __launch_bounds__(VT) pcr_update_xr(long long n, T* x, const T* 
 
 struct SolidWork {
   long long S;
+  PcrState* hst;      // pinned state copies [4]
+  cudaEvent_t ev[4];
   double *r, *d, *Ap, *s, *invd, *partial;
   float *blocks32, *x32, *r32, *d32, *Ap32, *s32, *invd32, *b32;
   PcrState *st, *st32;
@@ -844,6 +1076,8 @@ esf_status solid_work_alloc(SolidWork** out, long long S, int mixed) {
   ESF_CUDA(cudaMalloc(&w->partial, ESF_MAX_PARTIALS * 8));
   ESF_CUDA(cudaMalloc(&w->st, sizeof(PcrState)));
   ESF_CUDA(cudaMalloc(&w->st32, sizeof(PcrState)));
+  ESF_CUDA(cudaMallocHost(&w->hst, 4 * sizeof(PcrState)));
+  for (int i = 0; i < 4; i++) ESF_CUDA(cudaEventCreateWithFlags(&w->ev[i], cudaEventDisableTiming));
   if (mixed) {
     ESF_CUDA(cudaMalloc(&w->blocks32, w->cap * 243 * 4));
     ESF_CUDA(cudaMalloc(&w->x32, n * 4));
@@ -864,6 +1098,9 @@ void solid_work_free(SolidWork* w) {
   cudaFree(w->partial); cudaFree(w->st); cudaFree(w->st32); cudaFree(w->blocks32);
   cudaFree(w->x32); cudaFree(w->r32); cudaFree(w->d32); cudaFree(w->Ap32); cudaFree(w->s32);
   cudaFree(w->invd32); cudaFree(w->b32);
+  if (w->hst) cudaFreeHost(w->hst);
+  for (int i = 0; i < 4; i++)
+    if (w->ev[i]) cudaEventDestroy(w->ev[i]);
   delete w;
 }
 
@@ -871,35 +1108,50 @@ template <typename T>
 static esf_status solid_pcr(long long S, const T* blocks, const int* nbr, const T* invd,
                             const T* b, T* x, T* r, T* d, T* Ap, T* s, double* partial,
                             PcrState* dst, double eps, int maxIt, cudaStream_t st, PcrState* out,
-                            int inner) {
+                            int inner, PcrState* hbuf, cudaEvent_t* evs) {
   const long long n = 3 * S;
   const int vb = vec_blocks(n), sb = vec_blocks(S);
   esf_status e = init_state(dst, eps, maxIt, st, inner);
   if (e) return e;
   // assembled variant: x = 0, r = b/diag (CONJUGATE_RESIDUAL.inl:196-205)
-  pcr_zero_start<T><<<vb, VT, 0, st>>>(n, b, invd, x, r, d, Ap, partial, dst);
-  solid_spmv<T, S_UPDATE><<<sb, VT, 0, st>>>(S, blocks, nbr, r, nullptr, nullptr, s, nullptr,
+  ESF_COUNTED pcr_zero_start<T><<<vb, VT, 0, st>>>(n, b, invd, x, r, d, Ap, partial, dst);
+  ESF_COUNTED solid_spmv<T, S_UPDATE><<<sb, VT, 0, st>>>(S, blocks, nbr, r, nullptr, nullptr, s, nullptr,
                                              partial, dst);
   ESF_LAUNCH_CHECK();
+  // chunks of 5 iterations (the first 6) each followed by an async copy of
+  // the state into pinned memory; up to 3 chunks in flight, then poll
   PcrState h;
   memset(&h, 0, sizeof h);
   const int maxChunks = maxIt / 5 + 3;
-  for (int chunk = 0; chunk < maxChunks; chunk++) {
-    const int nIt = (chunk == 0) ? 6 : 5;  // iterations 0..5, then 5j+1..5j+5
-    for (int k = 0; k < nIt; k++) {
-      pcr_phase_a<T, false><<<vb, VT, 0, st>>>(n, d, r, Ap, s, invd, partial, dst);
-      pcr_update_xr<T><<<vb, VT, 0, st>>>(n, x, d, r, Ap, invd, dst);
-      solid_spmv<T, S_UPDATE><<<sb, VT, 0, st>>>(S, blocks, nbr, r, nullptr, nullptr, s, nullptr,
-                                                 partial, dst);
+  const int inflight = 3;
+  int launched = 0, waited = 0;
+  bool done = false;
+  while (!done) {
+    if (launched < maxChunks) {
+      const int nIt = (launched == 0) ? 6 : 5;  // iterations 0..5, then 5j+1..5j+5
+      for (int k = 0; k < nIt; k++) {
+        ESF_COUNTED pcr_phase_a<T, false><<<vb, VT, 0, st>>>(n, d, r, Ap, s, invd, partial, dst);
+        ESF_COUNTED pcr_update_xr<T><<<vb, VT, 0, st>>>(n, x, d, r, Ap, invd, dst);
+        ESF_COUNTED solid_spmv<T, S_UPDATE><<<sb, VT, 0, st>>>(S, blocks, nbr, r, nullptr, nullptr, s,
+                                                               nullptr, partial, dst);
+      }
+      if (!inner)
+        ESF_COUNTED solid_spmv<T, S_CHECK><<<sb, VT, 0, st>>>(S, blocks, nbr, x, b, nullptr, nullptr,
+                                                              nullptr, partial, dst);
+      ESF_LAUNCH_CHECK();
+      ESF_CUDA(cudaMemcpyAsync(&hbuf[launched % 4], dst, sizeof(PcrState), cudaMemcpyDeviceToHost, st));
+      ESF_CUDA(cudaEventRecord(evs[launched % 4], st));
+      launched++;
     }
-    if (!inner)
-      solid_spmv<T, S_CHECK><<<sb, VT, 0, st>>>(S, blocks, nbr, x, b, nullptr, nullptr, nullptr,
-                                                partial, dst);
-    ESF_LAUNCH_CHECK();
-    ESF_CUDA(cudaMemcpyAsync(&h, dst, sizeof h, cudaMemcpyDeviceToHost, st));
-    ESF_CUDA(cudaStreamSynchronize(st));
-    if (h.done) break;
+    if (launched - waited >= inflight || launched >= maxChunks) {
+      ESF_CUDA(cudaEventSynchronize(evs[waited % 4]));
+      h = hbuf[waited % 4];
+      waited++;
+      if (h.done || waited >= maxChunks) done = true;
+    }
   }
+  ESF_CUDA(cudaStreamSynchronize(st));
+  ESF_CUDA(cudaMemcpy(&h, dst, sizeof h, cudaMemcpyDeviceToHost));
   *out = h;
   return ESF_OK;
 }
@@ -917,12 +1169,12 @@ esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const in
   }
   const long long n = 3 * S;
   if ((n + VT - 1) / VT > ESF_MAX_PARTIALS * 64LL) return ESF_ERR_UNSUPPORTED;
-  inv_vec<<<vec_blocks(n), VT, 0, st>>>(n, diag, w->invd, w->invd32);
+  ESF_COUNTED inv_vec<<<vec_blocks(n), VT, 0, st>>>(n, diag, w->invd, w->invd32);
   ESF_LAUNCH_CHECK();
   if (precision == ESF_FP64) {
     PcrState h;
     esf_status e = solid_pcr<double>(S, blocks, nbr, w->invd, b, x, w->r, w->d, w->Ap, w->s,
-                                     w->partial, w->st, eps, maxIt, st, &h, 0);
+                                     w->partial, w->st, eps, maxIt, st, &h, 0, w->hst, w->ev);
     if (e) return e;
     if (iters) *iters = h.iter;
     if (converged) *converged = h.converged;
@@ -931,13 +1183,13 @@ esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const in
     return h.status ? (esf_status)h.status : ESF_OK;
   }
   // mixed: FP32 blocks; x starts at 0 as in the assembled reference variant
-  convert_vec<double, float><<<vec_blocks(S * 243), VT, 0, st>>>(S * 243, blocks, w->blocks32);
+  ESF_COUNTED convert_vec<double, float><<<vec_blocks(S * 243), VT, 0, st>>>(S * 243, blocks, w->blocks32);
   ESF_CUDA(cudaMemsetAsync(x, 0, n * 8, st));
   double bnorm2 = 0;
   {
     esf_status e0 = init_state(w->st, eps, maxIt, st);
     if (e0) return e0;
-    vec_norm2<double><<<vec_blocks(n), VT, 0, st>>>(n, b, w->partial, &w->st->ticket[3],
+    ESF_COUNTED vec_norm2<double><<<vec_blocks(n), VT, 0, st>>>(n, b, w->partial, &w->st->ticket[3],
                                                     &w->st->bnorm2);
     PcrState hb;
     ESF_CUDA(cudaMemcpyAsync(&hb, w->st, sizeof hb, cudaMemcpyDeviceToHost, st));
@@ -949,7 +1201,7 @@ esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const in
   esf_status status = ESF_OK;
   for (ref = 0; ref <= maxRefine; ref++) {
     init_state(w->st, eps, maxIt, st);
-    solid_spmv<double, S_RESID64><<<vec_blocks(S), VT, 0, st>>>(S, blocks, nbr, x, b, w->r,
+    ESF_COUNTED solid_spmv<double, S_RESID64><<<vec_blocks(S), VT, 0, st>>>(S, blocks, nbr, x, b, w->r,
                                                                 nullptr, w->b32, w->partial,
                                                                 w->st);
     ESF_LAUNCH_CHECK();
@@ -969,14 +1221,14 @@ esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const in
     PcrState hi;
     esf_status e = solid_pcr<float>(S, w->blocks32, nbr, w->invd32, w->b32, w->x32, w->r32, w->d32,
                                     w->Ap32, w->s32, w->partial, w->st32, innerEps, maxIt - total,
-                                    st, &hi, 1);
+                                    st, &hi, 1, w->hst, w->ev);
     if (e) return e;
     total += hi.iter;
     if (hi.status) {
       status = (esf_status)hi.status;
       break;
     }
-    add_correction<<<vec_blocks(n), VT, 0, st>>>(n, x, w->x32);
+    ESF_COUNTED add_correction<<<vec_blocks(n), VT, 0, st>>>(n, x, w->x32);
   }
   if (iters) *iters = total;
   if (refinements) *refinements = ref;

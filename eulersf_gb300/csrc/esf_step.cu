@@ -19,6 +19,14 @@
 namespace esf {
 
 static thread_local char g_err[1024] = "";
+static unsigned long long g_launches = 0;
+static thread_local unsigned long long* g_capture = nullptr;
+void note_launch() {
+  if (g_capture) (*g_capture)++;
+  else __atomic_add_fetch(&g_launches, 1ull, __ATOMIC_RELAXED);
+}
+void note_graph_replay(unsigned long long kernels) { __atomic_add_fetch(&g_launches, kernels, __ATOMIC_RELAXED); }
+void set_capturing(bool on, unsigned long long* counter) { g_capture = on ? counter : nullptr; }
 void set_error(const char* fmt, ...) {
   va_list ap;
   va_start(ap, fmt);
@@ -106,7 +114,7 @@ struct esf_scene {
   esf::DBuf sNode, solidF, solidMv, damped, solidV0, solidPC, solidB1, sysDiag, blocks, nbr, mask;
   esf::DBuf Ke, nf, energy;
   // scratch
-  esf::DBuf cubTmp, keys, vals, skeys, svals, bstart, bend, mt;
+  esf::DBuf cubTmp, keys, vals, skeys, svals, bstart, bend, mt, pweights;
   long long mtLen = 0;
   int *dInts = nullptr, *hInts = nullptr;
   unsigned long long* dU64 = nullptr;
@@ -114,6 +122,7 @@ struct esf_scene {
   esf::PressureWork* pw = nullptr;
   esf::SolidWork* sw = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEvent_t ph[14] = {};
   int status = 0;
 };
 
@@ -128,6 +137,7 @@ using namespace esf;
 extern "C" {
 
 int esf_abi_version(void) { return ESF_ABI_VERSION; }
+uint64_t esf_kernel_launches(void) { return __atomic_load_n(&esf::g_launches, __ATOMIC_RELAXED); }
 const char* esf_last_error(void) { return esf::g_err; }
 
 esf_status esf_params_default(const esf_grid* g, esf_params* p) {
@@ -273,6 +283,8 @@ extern "C" esf_status esf_create(const esf_grid* g, const esf_params* p, void* s
   }
   if (!e && cudaEventCreate(&s->e0) != cudaSuccess) e = ESF_ERR_CUDA;
   if (!e && cudaEventCreate(&s->e1) != cudaSuccess) e = ESF_ERR_CUDA;
+  for (int i = 0; i < 14 && !e; i++)
+    if (cudaEventCreate(&s->ph[i]) != cudaSuccess) e = ESF_ERR_CUDA;
   if (e) {
     esf_destroy(s);
     return e;
@@ -305,12 +317,14 @@ extern "C" esf_status esf_destroy(esf_scene* s) {
   DBuf* bufs[] = {&s->sNode, &s->solidF, &s->solidMv, &s->damped, &s->solidV0, &s->solidPC,
                   &s->solidB1, &s->sysDiag, &s->blocks, &s->nbr, &s->mask, &s->Ke, &s->nf,
                   &s->energy, &s->cubTmp, &s->keys, &s->vals, &s->skeys, &s->svals, &s->bstart,
-                  &s->bend, &s->mt};
+                  &s->bend, &s->mt, &s->pweights};
   for (DBuf* b : bufs) b->release();
   pressure_work_free(s->pw);
   solid_work_free(s->sw);
   if (s->e0) cudaEventDestroy(s->e0);
   if (s->e1) cudaEventDestroy(s->e1);
+  for (int i = 0; i < 14; i++)
+    if (s->ph[i]) cudaEventDestroy(s->ph[i]);
   if (s->ownStream && s->stream) cudaStreamDestroy(s->stream);
   delete s;
   return ESF_OK;
@@ -410,7 +424,7 @@ extern "C" esf_status esf_add_solid(esf_scene* sc, const esf_solid_desc* dd) {
   ESF_CUDA(cudaMemsetAsync(x.detFInv, 0, T * 8, st));
   ESF_CUDA(cudaMemsetAsync(x.quarter, 0, T * 64, st));
   ESF_CUDA(cudaMemsetAsync(x.valid, 0, G.R, st));
-  k_initial_state<<<kblocks(G.T), KT, 0, st>>>(G, x, d->dRot, d->trans[0], d->trans[1], d->trans[2],
+  ESF_COUNTED k_initial_state<<<kblocks(G.T), KT, 0, st>>>(G, x, d->dRot, d->trans[0], d->trans[1], d->trans[2],
                                                d->scale[0], d->scale[1], d->scale[2], d->v0[0],
                                                d->v0[1], d->v0[2]);
   ESF_LAUNCH_CHECK();
@@ -464,9 +478,9 @@ static esf_status compute_solid_mass(esf_scene* sc, Solid* d, int usesdf) {
   if (nc <= 0) return ESF_OK;
   const double subDh = sc->p.mass_sample_dh;
   const int res = (int)(G.dh / subDh);
-  k_det_finv<<<kblocks(nc), KT, 0, st>>>(G, x, cells);
-  k_mass_subsample<<<kblocks(nc, 128), 128, 0, st>>>(G, x, cells, usesdf, subDh, res);
-  k_mass_gather<<<kblocks(boxn(nodes)), KT, 0, st>>>(G, x, cells, nodes);
+  ESF_COUNTED k_det_finv<<<kblocks(nc), KT, 0, st>>>(G, x, cells);
+  ESF_COUNTED k_mass_subsample<<<kblocks(nc, 128), 128, 0, st>>>(G, x, cells, usesdf, subDh, res);
+  ESF_COUNTED k_mass_gather<<<kblocks(boxn(nodes)), KT, 0, st>>>(G, x, cells, nodes);
   ESF_LAUNCH_CHECK();
   return ESF_OK;
 }
@@ -479,7 +493,7 @@ static esf_status compute_sdf(esf_scene* sc, Solid* d) {
   memcpy(sc->hInts, init, sizeof init);
   ESF_CUDA(cudaMemcpyAsync(sc->dInts, sc->hInts, sizeof init, cudaMemcpyHostToDevice, st));
   double large = G.X + G.Y + G.Z + 2;
-  k_phi_init<<<kblocks(G.T), KT, 0, st>>>(G, d->d, large, sc->dInts);
+  ESF_COUNTED k_phi_init<<<kblocks(G.T), KT, 0, st>>>(G, d->d, large, sc->dInts);
   ESF_LAUNCH_CHECK();
   ESF_CUDA(cudaMemcpyAsync(sc->hInts, sc->dInts, sizeof init, cudaMemcpyDeviceToHost, st));
   ESF_CUDA(cudaStreamSynchronize(st));
@@ -499,7 +513,25 @@ static esf_status compute_sdf(esf_scene* sc, Solid* d) {
   d->ex[4] = std::min(ymax + exn, G.Y);
   d->ex[5] = std::min(zmax + exn, G.Z);
   Box ex = mkbox(d->ex[0], d->ex[1], d->ex[2], d->ex[3], d->ex[4], d->ex[5]);
-  k_sweep_phi<<<1, 1024, 0, st>>>(G, d->d, ex, 2);
+  // 2 x sweepPhi: 8 passes each, every pass a sequence of hyperplanes
+  for (int rep = 0; rep < 2; rep++)
+    for (int dir = 0; dir < 8; dir++) {
+      Sweep w;
+      w.dj = (dir & 1) ? -1 : 1;
+      w.di = (dir & 2) ? -1 : 1;
+      w.dk = (dir & 4) ? -1 : 1;
+      w.i0 = w.di > 0 ? ex.lo[0] + 1 : ex.hi[0] - 2;
+      w.j0 = w.dj > 0 ? ex.lo[1] + 1 : ex.hi[1] - 2;
+      w.k0 = w.dk > 0 ? ex.lo[2] + 1 : ex.hi[2] - 2;
+      w.ni = ex.hi[0] - ex.lo[0] - 1;
+      w.nj = ex.hi[1] - ex.lo[1] - 1;
+      w.nk = ex.hi[2] - ex.lo[2] - 1;
+      if (w.ni <= 0 || w.nj <= 0 || w.nk <= 0) continue;
+      const int planes = w.ni + w.nj + w.nk - 2;
+      const int blocks = kblocks((long long)w.ni * w.nj);
+      for (int pl = 0; pl < planes; pl++)
+        ESF_COUNTED k_sweep_phi_plane<<<blocks, KT, 0, st>>>(G, d->d.phi, d->d.mass, w, pl);
+    }
   ESF_LAUNCH_CHECK();
   return ESF_OK;
 }
@@ -546,7 +578,7 @@ static esf_status collect_valid_cells(esf_scene* sc, Solid* d) {
   if (nc <= 0) return ESF_OK;
   TRY(d->cellFlag.ensure(nc * 4));
   TRY(d->cellScan.ensure((nc + 1) * 4));
-  k_flag_valid_cells<<<kblocks(nc), KT, 0, st>>>(G, d->d, cells, d->cellFlag.as<int>());
+  ESF_COUNTED k_flag_valid_cells<<<kblocks(nc), KT, 0, st>>>(G, d->d, cells, d->cellFlag.as<int>());
   size_t tb = 0;
   cub::DeviceScan::ExclusiveSum(nullptr, tb, d->cellFlag.as<int>(), d->cellScan.as<int>(), (int)nc, st);
   TRY(sc->cubTmp.ensure(tb));
@@ -556,7 +588,7 @@ static esf_status collect_valid_cells(esf_scene* sc, Solid* d) {
   ESF_CUDA(cudaStreamSynchronize(st));
   d->nValid = (long long)sc->hInts[0] + sc->hInts[1];
   TRY(d->cellList.ensure((d->nValid + 1) * 8));
-  k_collect_valid_cells<<<kblocks(nc), KT, 0, st>>>(G, cells, d->cellFlag.as<int>(), d->cellScan.as<int>(),
+  ESF_COUNTED k_collect_valid_cells<<<kblocks(nc), KT, 0, st>>>(G, cells, d->cellFlag.as<int>(), d->cellScan.as<int>(),
                                                     d->cellList.as<long long>());
   ESF_LAUNCH_CHECK();
   return ESF_OK;
@@ -570,7 +602,7 @@ static esf_status init_particles(esf_scene* sc, Solid* d) {
   if (d->np == 0) return ESF_OK;
   TRY(ensure_mt(sc, 3 * d->np));
   TRY(d->part.ensure(d->np * 80));
-  k_seed_particles<<<kblocks(d->np), KT, 0, sc->stream>>>(sc->g, d->d, d->cellList.as<long long>(),
+  ESF_COUNTED k_seed_particles<<<kblocks(d->np), KT, 0, sc->stream>>>(sc->g, d->d, d->cellList.as<long long>(),
                                                            d->nValid, ppc, sc->mt.as<uint32_t>(),
                                                            d->pmass, d->part.as<double>());
   ESF_LAUNCH_CHECK();
@@ -578,7 +610,7 @@ static esf_status init_particles(esf_scene* sc, Solid* d) {
 }
 
 static esf_status advect_mesh(esf_scene* sc, Solid* d) {
-  k_advect_mesh<<<kblocks(d->nv), KT, 0, sc->stream>>>(sc->g, d->d, d->nv, d->dVerts, d->dRest);
+  ESF_COUNTED k_advect_mesh<<<kblocks(d->nv), KT, 0, sc->stream>>>(sc->g, d->d, d->nv, d->dVerts, d->dRest);
   ESF_LAUNCH_CHECK();
   return ESF_OK;
 }
@@ -588,8 +620,8 @@ static esf_status gather_solid_masses(esf_scene* sc) {
   const GridDev& G = sc->g;
   cudaStream_t st = sc->stream;
   for (int i = 0; i < sc->ns; i++)
-    k_gather_accumulate<<<kblocks(G.T), KT, 0, st>>>(G, sc->s[i]->d, i == 0, sc->solidMass, sc->quarter);
-  k_node_vf<<<kblocks(G.T), KT, 0, st>>>(G, sc->quarter, sc->solidMass, sc->nodeVF, sc->nodeFlag);
+    ESF_COUNTED k_gather_accumulate<<<kblocks(G.T), KT, 0, st>>>(G, sc->s[i]->d, i == 0, sc->solidMass, sc->quarter);
+  ESF_COUNTED k_node_vf<<<kblocks(G.T), KT, 0, st>>>(G, sc->quarter, sc->solidMass, sc->nodeVF, sc->nodeFlag);
   size_t tb = 0;
   cub::DeviceScan::ExclusiveSum(nullptr, tb, sc->nodeFlag, sc->nodeScan, (int)G.T, st);
   TRY(sc->cubTmp.ensure(tb));
@@ -599,7 +631,7 @@ static esf_status gather_solid_masses(esf_scene* sc) {
   ESF_CUDA(cudaStreamSynchronize(st));
   long long S = (long long)sc->hInts[0] + sc->hInts[1];
   TRY(sc->sNode.ensure((S + 1) * 8));
-  k_sdof<<<kblocks(G.T), KT, 0, st>>>(G, sc->nodeFlag, sc->nodeScan, sc->sdof, sc->sNode.as<long long>());
+  ESF_COUNTED k_sdof<<<kblocks(G.T), KT, 0, st>>>(G, sc->nodeFlag, sc->nodeScan, sc->sdof, sc->sNode.as<long long>());
   ESF_LAUNCH_CHECK();
   sc->S = S;
   return ESF_OK;
@@ -610,7 +642,7 @@ static esf_status recover_velocity(esf_scene* sc) {
     Solid* d = sc->s[i];
     Box b = mkbox(d->ex[0], d->ex[1], d->ex[2], d->ex[3] - 1, d->ex[4] - 1, d->ex[5] - 1);
     if (boxn(b) > 0)
-      k_recover_velocity<<<kblocks(boxn(b)), KT, 0, sc->stream>>>(sc->g, d->d, b, sc->vel);
+      ESF_COUNTED k_recover_velocity<<<kblocks(boxn(b)), KT, 0, sc->stream>>>(sc->g, d->d, b, sc->vel);
   }
   ESF_LAUNCH_CHECK();
   return ESF_OK;
@@ -695,15 +727,15 @@ static esf_status solid_system(esf_scene* sc, double* energyOut) {
     TRY(sc->Ke.ensure((576 * nc + 1) * 8));
     TRY(sc->nf.ensure((24 * nc + 1) * 8));
     if (nc > 0) {
-      k_element_stiffness<<<kblocks(nc, 128), 128, 0, st>>>(G, d->d, d->cellList.as<long long>(), nc,
+      ESF_COUNTED k_element_stiffness<<<kblocks(nc, 128), 128, 0, st>>>(G, d->d, d->cellList.as<long long>(), nc,
                                                              sc->Ke.as<double>(), sc->nf.as<double>(),
                                                              ePart);
       // cell -> ordinal in the valid list
-      k_cell_ord_fill<<<kblocks(nc), KT, 0, st>>>(G, d->cellList.as<long long>(), nc, sc->cellOrd);
+      ESF_COUNTED k_cell_ord_fill<<<kblocks(nc), KT, 0, st>>>(G, d->cellList.as<long long>(), nc, sc->cellOrd);
     }
     Box b = mkbox(d->ex[0], d->ex[1], d->ex[2], d->ex[3] - 1, d->ex[4] - 1, d->ex[5] - 1);
     if (boxn(b) > 0 && S > 0)
-      k_compute_mv<<<std::min(kblocks(boxn(b)), EB), KT, 0, st>>>(G, d->d, b, sc->sdof,
+      ESF_COUNTED k_compute_mv<<<std::min(kblocks(boxn(b)), EB), KT, 0, st>>>(G, d->d, b, sc->sdof,
                                                                   sc->solidMv.as<double>(), ePart + EB);
     ESF_LAUNCH_CHECK();
   }
@@ -732,6 +764,7 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
   cudaStream_t st = sc->stream;
   sc->status = ESF_OK;
   ESF_CUDA(cudaEventRecord(sc->e0, st));
+  ESF_CUDA(cudaEventRecord(sc->ph[0], st));
   // ---- broad phase (COUPLED_INTEGRATOR_3D.cpp:378-411)
   int prone = 0;
   for (int i = 0; i < sc->ns && !prone; i++) {
@@ -739,7 +772,7 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     unsigned long long init[6] = {~0ull, ~0ull, ~0ull, 0, 0, 0};
     memcpy(sc->hU64, init, sizeof init);
     ESF_CUDA(cudaMemcpyAsync(sc->dU64, sc->hU64, sizeof init, cudaMemcpyHostToDevice, st));
-    k_mesh_aabb<<<kblocks(3LL * d->ntri), KT, 0, st>>>(d->ntri, d->dTris, d->dVerts, sc->dU64);
+    ESF_COUNTED k_mesh_aabb<<<kblocks(3LL * d->ntri), KT, 0, st>>>(d->ntri, d->dTris, d->dVerts, sc->dU64);
     ESF_CUDA(cudaMemcpyAsync(sc->hU64, sc->dU64, sizeof init, cudaMemcpyDeviceToHost, st));
     ESF_CUDA(cudaStreamSynchronize(st));
     double mn[3], mx[3];
@@ -760,7 +793,7 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
   // CFL (:88-102)
   sc->hU64[0] = 0;
   ESF_CUDA(cudaMemcpyAsync(sc->dU64, sc->hU64, 8, cudaMemcpyHostToDevice, st));
-  k_cfl_vmax<<<kblocks(G.T), KT, 0, st>>>(G, sc->vel, sc->solidMass, sc->dU64);
+  ESF_COUNTED k_cfl_vmax<<<kblocks(G.T), KT, 0, st>>>(G, sc->vel, sc->solidMass, sc->dU64);
   ESF_CUDA(cudaMemcpyAsync(sc->hU64, sc->dU64, 8, cudaMemcpyDeviceToHost, st));
   ESF_CUDA(cudaStreamSynchronize(st));
   {
@@ -777,6 +810,7 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
   }
   const double dt = sc->dt;
   const long long S = sc->S;
+  ESF_CUDA(cudaEventRecord(sc->ph[1], st));
   // ---- solid forces, stiffness, mv
   double e_unused;
   TRY(solid_system(sc, &e_unused));
@@ -784,7 +818,7 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
   double* ePart = sc->energy.as<double>();
   // ---- vorticity + body forces (:442-606)
   ESF_CUDA(cudaMemsetAsync(sc->ws, 0, G.T * 8, st));
-  if (sc->vortEps > 0) k_vorticity<<<kblocks(G.T), KT, 0, st>>>(G, sc->nodeVF, sc->vel, sc->vort, sc->ws);
+  if (sc->vortEps > 0) ESF_COUNTED k_vorticity<<<kblocks(G.T), KT, 0, st>>>(G, sc->nodeVF, sc->vel, sc->vort, sc->ws);
   // The reference adds the stiffness forces before the body forces, so the
   // block/force gather runs first; the damped mass it needs for the diagonal
   // comes from the body-force kernel and is added afterwards.
@@ -798,23 +832,24 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
   const double scale = dt * dt + sc->p.rayleigh_beta * dt;
   if (S > 0) {
     // forces + blocks (diagonal mass added in a second pass, below)
-    k_assemble<<<kblocks(S * 27), KT, 0, st>>>(G, sc->s[0]->d, sc->sdof, sc->sNode.as<long long>(), S,
+    ESF_COUNTED k_assemble<<<kblocks(S * 27), KT, 0, st>>>(G, sc->s[0]->d, sc->sdof, sc->sNode.as<long long>(), S,
                                                 sc->cellOrd, sc->Ke.as<double>(), sc->nf.as<double>(), scale,
                                                 sc->blocks.as<double>(),
                                                 sc->nbr.as<int>(), sc->mask.as<int>(), sc->solidF.as<double>());
   }
-  k_body_forces<<<EB, KT, 0, st>>>(G, bp, sc->nodeVF, sc->solidMass, sc->vel, sc->intensity, sc->vort,
+  ESF_CUDA(cudaEventRecord(sc->ph[2], st));
+  ESF_COUNTED k_body_forces<<<EB, KT, 0, st>>>(G, bp, sc->nodeVF, sc->solidMass, sc->vel, sc->intensity, sc->vort,
                                    sc->ws, sc->sdof, sc->uf, sc->mvf, sc->minv, sc->damped.as<double>(),
                                    sc->solidMv.as<double>(), sc->solidF.as<double>(), ePart + 2 * EB);
   ESF_LAUNCH_CHECK();
   if (S > 0) {
-    k_add_diag<<<kblocks(S), KT, 0, st>>>(S, sc->damped.as<double>(), sc->blocks.as<double>(),
+    ESF_COUNTED k_add_diag<<<kblocks(S), KT, 0, st>>>(S, sc->damped.as<double>(), sc->blocks.as<double>(),
                                           sc->sysDiag.as<double>());
     ESF_LAUNCH_CHECK();
   }
   double energy = sum_partials(sc, 3 * EB);
   // ---- pcrImplicitSolve (:662-764)
-  int it[3] = {0, 0, 0}, cv[3] = {0, 0, 0}, rf[3] = {0, 0, 0};
+  int it[3] = {0, 0, 0}, cv[3] = {0, 0, 0}, rf[3] = {0, 0, 0}, it64 = 0;
   double rr[3] = {0, 0, 0};
   const int prec = sc->p.precision;
   if (!sc->sw || solid_work_capacity(sc->sw) < S) {
@@ -823,6 +858,7 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     TRY(solid_work_alloc(&sc->sw, S + S / 4 + 16, prec == ESF_MIXED));
   }
   esf_status es = ESF_OK;
+  ESF_CUDA(cudaEventRecord(sc->ph[3], st));
   if (S > 0) {
     es = solid_solve(sc->sw, S, sc->blocks.as<double>(), sc->nbr.as<int>(), sc->sysDiag.as<double>(),
                      sc->solidF.as<double>(), sc->solidV0.as<double>(), sc->p.implicit_solver_eps,
@@ -831,16 +867,18 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     if (es == ESF_ERR_NUMERIC) sc->status = es;
     else if (es) return es;
   }
-  k_vstar<<<kblocks(G.T), KT, 0, st>>>(G, sc->sdof, sc->uf, sc->minv, sc->solidV0.as<double>(), sc->vstar);
-  k_cell_rhs<<<kblocks(G.R), KT, 0, st>>>(G, sc->vel, sc->vstar, sc->minv, sc->rhs, sc->jdiag, sc->b1);
+  ESF_CUDA(cudaEventRecord(sc->ph[4], st));
+  ESF_COUNTED k_vstar<<<kblocks(G.T), KT, 0, st>>>(G, sc->sdof, sc->uf, sc->minv, sc->solidV0.as<double>(), sc->vstar);
+  ESF_COUNTED k_cell_rhs<<<kblocks(G.R), KT, 0, st>>>(G, sc->vel, sc->vstar, sc->minv, sc->rhs, sc->jdiag, sc->b1);
   ESF_LAUNCH_CHECK();
   es = pressure_solve(sc->pw, G, sc->minv, sc->jdiag, sc->b1, sc->lambda, sc->p.div_free_solver_eps,
                       sc->p.cr_max_iterations, prec, sc->p.inner_eps, sc->p.max_refinements, &it[1],
-                      &rr[1], &rf[1], &cv[1], st);
+                      &rr[1], &rf[1], &cv[1], st, &it64);
   if (es == ESF_ERR_NUMERIC) sc->status = es;
   else if (es) return es;
+  ESF_CUDA(cudaEventRecord(sc->ph[5], st));
   if (S > 0) {
-    k_solid_b1<<<kblocks(S), KT, 0, st>>>(G, sc->sNode.as<long long>(), S, sc->lambda, sc->solidB1.as<double>());
+    ESF_COUNTED k_solid_b1<<<kblocks(S), KT, 0, st>>>(G, sc->sNode.as<long long>(), S, sc->lambda, sc->solidB1.as<double>());
     ESF_LAUNCH_CHECK();
     es = solid_solve(sc->sw, S, sc->blocks.as<double>(), sc->nbr.as<int>(), sc->sysDiag.as<double>(),
                      sc->solidB1.as<double>(), sc->solidPC.as<double>(), sc->p.implicit_solver_eps,
@@ -849,9 +887,10 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     if (es == ESF_ERR_NUMERIC) sc->status = es;
     else if (es) return es;
   }
-  k_velocity_update<<<kblocks(G.T), KT, 0, st>>>(G, sc->sdof, sc->lambda, sc->minv, sc->solidPC.as<double>(),
+  ESF_COUNTED k_velocity_update<<<kblocks(G.T), KT, 0, st>>>(G, sc->sdof, sc->lambda, sc->minv, sc->solidPC.as<double>(),
                                                  sc->vstar, sc->pc, sc->v1, sc->vel);
   ESF_LAUNCH_CHECK();
+  ESF_CUDA(cudaEventRecord(sc->ph[6], st));
   // ---- finalizeSolution (:828-917)
   ContactParams cp;
   cp.wallThickness = sc->p.wall_thickness;
@@ -867,15 +906,16 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
   for (int i = 0; i < sc->ns; i++) {  // DEFOR_SOLID_3D::finalizeSolution(v, dt) (:1182-1197)
     Solid* d = sc->s[i];
     Box ex = mkbox(d->ex[0], d->ex[1], d->ex[2], d->ex[3], d->ex[4], d->ex[5]);
-    if (boxn(ex) > 0) k_copy_grid_velocity<<<kblocks(boxn(ex)), KT, 0, st>>>(G, d->d, ex, sc->vel);
+    if (boxn(ex) > 0) ESF_COUNTED k_copy_grid_velocity<<<kblocks(boxn(ex)), KT, 0, st>>>(G, d->d, ex, sc->vel);
     d->d.dt = dt;
   }
   for (int i = 0; i < sc->ns; i++) {  // gridToParticle
     Solid* d = sc->s[i];
     if (d->np > 0)
-      k_grid_to_particle<<<kblocks(d->np), KT, 0, st>>>(G, d->d, d->np, d->part.as<double>(), cp, nullptr, 0,
+      ESF_COUNTED k_grid_to_particle<<<kblocks(d->np), KT, 0, st>>>(G, d->d, d->np, d->part.as<double>(), cp, nullptr, 0,
                                                         sc->dInts + 32);
   }
+  ESF_CUDA(cudaEventRecord(sc->ph[7], st));
   for (int i = 0; i < sc->ns; i++) {  // particleToGrid
     Solid* d = sc->s[i];
     ESF_CUDA(cudaMemsetAsync(d->d.mass, 0, G.T * 8, st));
@@ -888,11 +928,12 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     TRY(sc->svals.ensure(np * 4));
     TRY(sc->bstart.ensure((size_t)nkeys * 4));
     TRY(sc->bend.ensure((size_t)nkeys * 4));
+    TRY(sc->pweights.ensure((size_t)np * 96));
     int pinit[6] = {1 << 30, 1 << 30, 1 << 30, -(1 << 30), -(1 << 30), -(1 << 30)};
     memcpy(sc->hInts, pinit, sizeof pinit);
     ESF_CUDA(cudaMemcpyAsync(sc->dInts, sc->hInts, sizeof pinit, cudaMemcpyHostToDevice, st));
-    k_p2g_keys<<<kblocks(np), KT, 0, st>>>(G, np, d->part.as<double>(), sc->keys.as<unsigned int>(),
-                                           sc->vals.as<unsigned int>(), sc->dInts);
+    ESF_COUNTED k_p2g_keys<<<kblocks(np), KT, 0, st>>>(G, np, d->part.as<double>(), sc->keys.as<unsigned int>(),
+                                           sc->vals.as<unsigned int>(), sc->dInts, sc->pweights.as<double>());
     int bits = 1;
     while (bits < 32 && (1ull << bits) <= nkeys) bits++;
     size_t tb = 0;
@@ -903,52 +944,84 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
                                     sc->vals.as<unsigned int>(), sc->svals.as<unsigned int>(), (int)np, 0, bits, st);
     ESF_CUDA(cudaMemsetAsync(sc->bstart.p, 0, (size_t)nkeys * 4, st));
     ESF_CUDA(cudaMemsetAsync(sc->bend.p, 0, (size_t)nkeys * 4, st));
-    k_bucket_bounds<<<kblocks(np), KT, 0, st>>>(np, sc->skeys.as<unsigned int>(), sc->bstart.as<int>(),
+    ESF_COUNTED k_bucket_bounds<<<kblocks(np), KT, 0, st>>>(np, sc->skeys.as<unsigned int>(), sc->bstart.as<int>(),
                                                 sc->bend.as<int>(), nkeys);
     ESF_CUDA(cudaMemcpyAsync(sc->hInts, sc->dInts, sizeof pinit, cudaMemcpyDeviceToHost, st));
     ESF_CUDA(cudaStreamSynchronize(st));
     Box nb = mkbox(std::max(sc->hInts[0], 0), std::max(sc->hInts[1], 0), std::max(sc->hInts[2], 0),
                    std::min(sc->hInts[3] + 4, G.X), std::min(sc->hInts[4] + 4, G.Y), std::min(sc->hInts[5] + 4, G.Z));
     if (boxn(nb) > 0)
-      k_p2g_gather<<<kblocks(boxn(nb)), KT, 0, st>>>(G, d->d, nb, d->part.as<double>(), sc->svals.as<unsigned int>(),
+      ESF_COUNTED k_p2g_gather<<<kblocks(boxn(nb)), KT, 0, st>>>(G, d->d, nb, d->part.as<double>(), sc->pweights.as<double>(), sc->svals.as<unsigned int>(),
                                                      sc->bstart.as<int>(), sc->bend.as<int>(), sc->p.flip_cutoff);
     ESF_LAUNCH_CHECK();
   }
-  for (int i = 0; i < sc->ns; i++) {  // extendVectorField
+  ESF_CUDA(cudaEventRecord(sc->ph[8], st));
+  for (int i = 0; i < sc->ns; i++) {  // extendVectorField = 4 x sweepVectorField
     Solid* d = sc->s[i];
     Box ex = mkbox(d->ex[0], d->ex[1], d->ex[2], d->ex[3], d->ex[4], d->ex[5]);
-    if (ex.hi[0] - ex.lo[0] >= 3 && ex.hi[1] - ex.lo[1] >= 3 && ex.hi[2] - ex.lo[2] >= 3)
-      k_extend_velocity<<<1, 1024, 0, st>>>(G, d->d, ex);
+    if (ex.hi[0] - ex.lo[0] < 3 || ex.hi[1] - ex.lo[1] < 3 || ex.hi[2] - ex.lo[2] < 3) continue;
+    unsigned long long* ranks = sc->dU64 + 8;
+    for (int rep = 0; rep < 4; rep++) {
+      for (int dir = 0; dir < 8; dir++) {
+        Sweep w;
+        w.dj = (dir & 1) ? -1 : 1;
+        w.di = (dir & 2) ? -1 : 1;
+        w.dk = (dir & 4) ? -1 : 1;
+        w.i0 = w.di > 0 ? ex.lo[0] + 1 : ex.hi[0] - 2;
+        w.j0 = w.dj > 0 ? ex.lo[1] + 1 : ex.hi[1] - 2;
+        w.k0 = w.dk > 0 ? ex.lo[2] + 1 : ex.hi[2] - 2;
+        w.ni = ex.hi[0] - ex.lo[0] - 2;
+        w.nj = ex.hi[1] - ex.lo[1] - 2;
+        w.nk = ex.hi[2] - ex.lo[2] - 2;
+        if (w.ni <= 0 || w.nj <= 0 || w.nk <= 0) continue;
+        ESF_CUDA(cudaMemsetAsync(ranks, 0xff, 3 * 8, st));
+        const long long total = (long long)w.ni * w.nj * w.nk;
+        ESF_COUNTED k_sweep_vec_ranks<<<kblocks(total), KT, 0, st>>>(G, d->d.phi, d->d.mass, w, ranks);
+        const int planes = w.ni + w.nj + w.nk - 2;
+        const int blocks = kblocks((long long)w.ni * w.nj);
+        for (int pl = 0; pl < planes; pl++)
+          ESF_COUNTED k_sweep_vec_plane<<<blocks, KT, 0, st>>>(G, d->d.vel, d->d.phi, d->d.mass, w, pl, ranks);
+      }
+      for (int axis = 2; axis >= 0; axis--) {
+        const long long nf = boxn(ex) / (ex.hi[axis] - ex.lo[axis]);
+        ESF_COUNTED k_extend_faces<<<kblocks(nf), KT, 0, st>>>(G, d->d.vel, d->d.mass, ex, axis);
+      }
+    }
     ESF_LAUNCH_CHECK();
   }
+  ESF_CUDA(cudaEventRecord(sc->ph[9], st));
   for (int i = 0; i < sc->ns; i++) {  // DEFOR_SOLID_3D::finalizeSolution() (:1198-1233)
     Solid* d = sc->s[i];
-    k_u_add<<<kblocks(3 * G.T), KT, 0, st>>>(G, d->d);
-    k_u_advect<<<kblocks(G.T), KT, 0, st>>>(G, d->d);
+    ESF_COUNTED k_u_add<<<kblocks(3 * G.T), KT, 0, st>>>(G, d->d);
+    ESF_COUNTED k_u_advect<<<kblocks(G.T), KT, 0, st>>>(G, d->d);
     std::swap(d->d.u, d->d.tmp3);
     Box ex = mkbox(d->ex[0], d->ex[1], d->ex[2], d->ex[3], d->ex[4], d->ex[5]);
     // the face extrapolation reads two layers inward: boxes thinner than 3
     // nodes (a vanished solid) are left as advected
     if (ex.hi[0] - ex.lo[0] >= 3 && ex.hi[1] - ex.lo[1] >= 3 && ex.hi[2] - ex.lo[2] >= 3)
       for (int axis = 2; axis >= 0; axis--)
-        k_u_extrapolate<<<kblocks(boxn(ex)), KT, 0, st>>>(G, d->d.u, ex, axis);
-    k_recover_X<<<kblocks(G.T), KT, 0, st>>>(G, d->d);
+        ESF_COUNTED k_u_extrapolate<<<kblocks(boxn(ex)), KT, 0, st>>>(G, d->d.u, ex, axis);
+    ESF_COUNTED k_recover_X<<<kblocks(G.T), KT, 0, st>>>(G, d->d);
     ESF_LAUNCH_CHECK();
   }
+  ESF_CUDA(cudaEventRecord(sc->ph[10], st));
   for (int i = 0; i < sc->ns; i++) TRY(compute_solid_mass(sc, sc->s[i], 1));
+  ESF_CUDA(cudaEventRecord(sc->ph[11], st));
   for (int i = 0; i < sc->ns; i++) TRY(advect_mesh(sc, sc->s[i]));
   for (int i = 0; i < sc->ns; i++) {
     TRY(compute_sdf(sc, sc->s[i]));
     TRY(init_particles(sc, sc->s[i]));
   }
   TRY(gather_solid_masses(sc));
-  k_advect_velocity<<<kblocks(G.T), KT, 0, st>>>(G, sc->solidMass, sc->vel, sc->vws, dt);
+  ESF_CUDA(cudaEventRecord(sc->ph[12], st));
+  ESF_COUNTED k_advect_velocity<<<kblocks(G.T), KT, 0, st>>>(G, sc->solidMass, sc->vel, sc->vws, dt);
   std::swap(sc->vel, sc->vws);
-  k_advect_scalar<<<kblocks(G.T), KT, 0, st>>>(G, sc->solidMass, sc->vel, sc->intensity, sc->ws, dt);
+  ESF_COUNTED k_advect_scalar<<<kblocks(G.T), KT, 0, st>>>(G, sc->solidMass, sc->vel, sc->intensity, sc->ws, dt);
   std::swap(sc->intensity, sc->ws);
   TRY(recover_velocity(sc));
-  k_dirichlet<<<kblocks(G.T), KT, 0, st>>>(G, sc->vel, sc->intensity);
+  ESF_COUNTED k_dirichlet<<<kblocks(G.T), KT, 0, st>>>(G, sc->vel, sc->intensity);
   ESF_LAUNCH_CHECK();
+  ESF_CUDA(cudaEventRecord(sc->ph[13], st));
   ESF_CUDA(cudaEventRecord(sc->e1, st));
   ESF_CUDA(cudaStreamSynchronize(st));
   if (rep) {
@@ -962,6 +1035,7 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
       rep->refinements[k] = rf[k];
     }
     rep->prone_to_contact = prone;
+    rep->fp64_iterations = it64;
     long long np = 0;
     for (int i = 0; i < sc->ns; i++) np += sc->s[i]->np;
     rep->num_particles = (int)np;
@@ -969,6 +1043,11 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     float ms = 0;
     cudaEventElapsedTime(&ms, sc->e0, sc->e1);
     rep->device_ms = ms;
+    for (int i = 0; i < 13; i++) {
+      float t = 0;
+      cudaEventElapsedTime(&t, sc->ph[i], sc->ph[i + 1]);
+      rep->phase_ms[i] = t;
+    }
   }
   return (esf_status)sc->status;
 }
@@ -1008,7 +1087,7 @@ static esf_status field_ref(esf_scene* s, int f, int si, FieldRef& r) {
     case ESF_F_SOLID_PRESSURE_CORRECTION: r = {s->solidPC.p, S3, 8, 0, false}; return ESF_OK;
     case ESF_F_DAMPED_SOLID_MASS: r = {s->damped.p, S3, 8, 0, false}; return ESF_OK;
     case ESF_F_SYSTEM_DIAG: r = {s->sysDiag.p, S3, 8, 0, false}; return ESF_OK;
-    case ESF_F_SYSTEM_BLOCKS: r = {s->blocks.p, 243ull * s->S, 8, 0, false}; return ESF_OK;
+    case ESF_F_SYSTEM_BLOCKS: r = {s->blocks.p, 243ull * s->S, 8, 5, false}; return ESF_OK;
     case ESF_F_SYSTEM_MASK: r = {s->mask.p, (size_t)s->S, 4, 0, false}; return ESF_OK;
     default: break;
   }
@@ -1064,6 +1143,15 @@ extern "C" esf_status esf_get_field(esf_scene* s, esf_field f, int si, void* hos
     int b[12] = {d->ex[0], d->ex[1], d->ex[2], d->ex[3], d->ex[4], d->ex[5],
                  d->tmin[0], d->tmin[1], d->tmin[2], d->tmax[0], d->tmax[1], d->tmax[2]};
     memcpy(host, b, 48);
+    return ESF_OK;
+  }
+  if (r.kind == 5) {  // system blocks: device entry-major -> [node][27][3][3]
+    const long long S = s->S;
+    std::vector<double> tmp(243 * S);
+    if (S) ESF_CUDA(cudaMemcpy(tmp.data(), r.dev, tmp.size() * 8, cudaMemcpyDeviceToHost));
+    double* o = (double*)host;
+    for (long long a = 0; a < S; a++)
+      for (int je = 0; je < 243; je++) o[243 * a + je] = tmp[je * S + a];
     return ESF_OK;
   }
   if (r.kind == 4) {  // _gridIdxToSolutionIdx (COUPLED_INTEGRATOR_3D.cpp:123-131)
@@ -1168,4 +1256,16 @@ extern "C" esf_status esf_read_frame(esf_scene* s, const char* path, int frame, 
   (void)s; (void)path; (void)frame; (void)debug;
   set_error("esf_read_frame: frame I/O is not implemented yet");
   return ESF_ERR_UNSUPPORTED;
+}
+
+extern "C" esf_status esf_time_pressure_kernels(esf_scene* s, int reps, double* update_ms,
+                                                double* axpy_ms) {
+  if (!s || reps < 1) return ESF_ERR_INVALID_ARG;
+  if (!s->inited) return ESF_ERR_STATE;
+  double u = 0, a = 0;
+  TRY(pressure_time_kernels(s->pw, s->g, s->minv, s->jdiag, s->b1, s->lambda, s->p.precision, reps,
+                            &u, &a, s->stream));
+  if (update_ms) *update_ms = u;
+  if (axpy_ms) *axpy_ms = a;
+  return ESF_OK;
 }

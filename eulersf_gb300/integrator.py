@@ -185,7 +185,7 @@ def params_from_desc(desc: SceneDesc, precision: int = abi.ESF_FP64) -> abi.Para
     p.flip_cutoff = 3
     p.flow_rate = 0.5
     p.precision = precision
-    p.inner_eps = 1e-4
+    p.inner_eps = desc.inner_eps
     p.max_refinements = 50
     return p
 

@@ -86,6 +86,7 @@ class SceneDesc:
     tight_border: int = 5
     noise_amplitude: float = 1e-3
     noise_seed: int = 0
+    inner_eps: float = 1e-4  # mixed precision: FP32 inner relative tolerance
 
     @property
     def res(self) -> int:

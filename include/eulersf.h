@@ -113,10 +113,18 @@ typedef struct esf_step_report {
   int converged[3];
   double rel_residual[3];     /* ||Ax-b|| / ||b|| at exit */
   int refinements[3];         /* mixed: outer FP64 refinement steps per solve */
+  int fp64_iterations;        /* mixed: FP64 PCR iterations that finished the pressure solve */
   int prone_to_contact;       /* CFL factor 0.6 instead of 1.8 */
   int num_particles;
   int status;                 /* esf_status of the step */
   double device_ms;           /* device time of the step (CUDA events) */
+  /* device time per phase, in the order of the reference's TIMING_BREAKDOWN
+   * labels (COUPLED_INTEGRATOR_3D.cpp:377-917): 0 broad phase + CFL,
+   * 1 solid forces/stiffness/assembly, 2 body forces, 3 solid solve 1,
+   * 4 pressure solve, 5 solid solve 2, 6 grid to particle, 7 particle to
+   * grid, 8 velocity extension, 9 solid displacement update, 10 solid mass,
+   * 11 surface mesh + SDF + particle seeding, 12 fluid advection + walls */
+  double phase_ms[13];
 } esf_step_report;
 
 /* Field identifiers for esf_get_field / esf_set_field / esf_field_info. */
@@ -227,6 +235,17 @@ esf_status esf_pressure_solve(const esf_grid* grid, const double* mass_inv_node,
                               const double* diag, const double* b, double* x,
                               double eps, int max_iterations, int precision,
                               int* iterations, double* rel_residual, void* stream);
+
+/* ---- instrumentation (no reference counterpart beyond TIMING_BREAKDOWN) -- */
+/* Number of kernels this library has launched in this process (graph
+ * replays count every kernel node). */
+uint64_t esf_kernel_launches(void);
+/* Average device time (ms) of the two pressure-PCR kernels on the scene's
+ * current pressure problem, timed with CUDA events on the scene's stream:
+ * the fused update+stencil+dot kernel and the axpy+norm kernel, at the
+ * scene's precision (FP32 for ESF_MIXED). Leaves the scene's state intact. */
+esf_status esf_time_pressure_kernels(esf_scene* scene, int reps, double* update_ms,
+                                     double* axpy_ms);
 
 /* ---- checkpoint (COUPLED_INTEGRATOR_3D::writeFrame/readFrame :977-1012) --- */
 esf_status esf_write_frame(esf_scene* scene, const char* data_path, int frame, int debug);

@@ -1096,6 +1096,7 @@ static void pressure_apply_d(int X, int Y, int Z, const int* dof, const double* 
                              const double* in, double* out, double* mid) {
   const long slab = (long)X * Y;
   const long cX = X - 1, cS = (long)(X - 1) * (Y - 1);
+#pragma omp parallel for schedule(static)
   for (int z = 1; z < Z - 1; z++)
     for (int y = 1; y < Y - 1; y++)
       for (int x = 1; x < X - 1; x++) {
@@ -1114,6 +1115,7 @@ static void pressure_apply_d(int X, int Y, int Z, const int* dof, const double* 
         mid[3 * k + 1] = m1;
         mid[3 * k + 2] = m2;
       }
+#pragma omp parallel for schedule(static)
   for (int z = 0; z < Z - 1; z++)
     for (int y = 0; y < Y - 1; y++)
       for (int x = 0; x < X - 1; x++) {
@@ -1142,7 +1144,9 @@ static int pcr_solve(matvec_fn A, void* ctx, const double* diag, const double* b
   double *q = w[0], *r = w[1], *d = w[2], *sv = w[3], *Ap = w[4], *tmp = w[5];
   if (zeroStart) memset(x, 0, n * 8);
   A(ctx, x, q);
+  _Pragma("omp parallel for schedule(static)")
   for (long i = 0; i < n; i++) r[i] = b[i] - q[i];
+  _Pragma("omp parallel for schedule(static)")
   for (long i = 0; i < n; i++) d[i] = r[i] / diag[i];
   memcpy(r, d, n * 8);
   A(ctx, r, sv);
@@ -1152,21 +1156,29 @@ static int pcr_solve(matvec_fn A, void* ctx, const double* diag, const double* b
   int converged = 0, i = 0;
   double tmpNorm = NAN;
   for (; i < maxIt && !converged; i++) {
+    _Pragma("omp parallel for schedule(static)")
     for (long k = 0; k < n; k++) q[k] = Ap[k] / diag[k];
     double alpha = edot(Ap, q, n);
     if (fabs(alpha) > 0.0) alpha = deltaNew / alpha;
+    _Pragma("omp parallel for schedule(static)")
     for (long k = 0; k < n; k++) x[k] += alpha * d[k];
+    _Pragma("omp parallel for schedule(static)")
     for (long k = 0; k < n; k++) r[k] -= alpha * q[k];
     A(ctx, r, sv);
     double deltaOld = deltaNew;
     deltaNew = edot(r, sv, n);
     double beta = deltaNew / deltaOld;
+    _Pragma("omp parallel for schedule(static)")
     for (long k = 0; k < n; k++) d[k] *= beta;
+    _Pragma("omp parallel for schedule(static)")
     for (long k = 0; k < n; k++) d[k] += r[k];
+    _Pragma("omp parallel for schedule(static)")
     for (long k = 0; k < n; k++) Ap[k] *= beta;
+    _Pragma("omp parallel for schedule(static)")
     for (long k = 0; k < n; k++) Ap[k] += sv[k];
     if (i > 0 && i % 5 == 0) {
       A(ctx, x, tmp);
+      _Pragma("omp parallel for schedule(static)")
       for (long k = 0; k < n; k++) tmp[k] -= b[k];
       tmpNorm = enorm(tmp, n);
       if (tmpNorm < eps * bNorm) {
@@ -1179,6 +1191,7 @@ static int pcr_solve(matvec_fn A, void* ctx, const double* diag, const double* b
   if (relres) {
     if (!(tmpNorm == tmpNorm)) {
       A(ctx, x, tmp);
+      _Pragma("omp parallel for schedule(static)")
       for (long k = 0; k < n; k++) tmp[k] -= b[k];
       tmpNorm = enorm(tmp, n);
     }

@@ -26,8 +26,8 @@ def build(force: bool = False) -> str:
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
             os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "esf_oracle.h"))):
         tmp = LIB + f".tmp{os.getpid()}"
-        subprocess.check_call(["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fPIC", "-shared",
-                               "-o", tmp, SRC, "-lm"])
+        subprocess.check_call(["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fopenmp", "-fPIC",
+                               "-shared", "-o", tmp, SRC, "-lm"])
         os.replace(tmp, LIB)
     return LIB
 
