@@ -23,7 +23,7 @@ EXPORTS = [
     "esf_abi_version", "esf_last_error", "esf_params_default", "esf_parse_config", "esf_create",
     "esf_destroy", "esf_add_solid", "esf_set_fluid", "esf_init", "esf_set_max_dt", "esf_step",
     "esf_dt", "esf_field_info", "esf_get_field", "esf_set_field", "esf_pressure_apply",
-    "esf_pressure_solve", "esf_write_frame", "esf_read_frame", "esf_kernel_launches",
+    "esf_pressure_solve", "esf_pressure_solve_static", "esf_write_frame", "esf_read_frame", "esf_kernel_launches",
     "esf_time_pressure_kernels",
 ]
 
@@ -48,6 +48,9 @@ def load(build_if_missing: bool = False) -> C.CDLL:
     lib.esf_pressure_apply.argtypes = [C.POINTER(abi.Grid), vp, vp, vp, vp]
     lib.esf_pressure_solve.argtypes = [C.POINTER(abi.Grid), vp, vp, vp, vp, C.c_double, C.c_int,
                                        C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), vp]
+    lib.esf_pressure_solve_static.argtypes = [C.POINTER(abi.Grid), vp, vp, vp, vp, C.c_double,
+                                              C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                              vp]
     lib.esf_parse_config.argtypes = [C.c_char_p, C.POINTER(abi.Grid), C.POINTER(abi.Params),
                                      C.POINTER(C.c_int), C.c_char_p, C.c_size_t,
                                      C.POINTER(abi.SolidDesc), C.c_int]

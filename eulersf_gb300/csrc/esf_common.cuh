@@ -163,6 +163,12 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
                           int precision, double innerEps, int maxRefine, int* iters,
                           double* relres, int* refinements, int* converged, cudaStream_t st,
                           int* fp64Iters = nullptr);
+// allocation-free FP64 solve on the module's static scratch (esf_solver.cu)
+esf_status static_scratch_address(void** out);
+esf_status pressure_solve_static(void* scratch, const GridDev& g, const double* minv,
+                                 const double* diag, const double* b, double* x, double eps,
+                                 int maxIt, int* iters, double* relres, int* converged,
+                                 cudaStream_t st);
 
 // Average device time of the fused update kernel and of the axpy+norm kernel
 // on scratch copies of the pressure problem (state untouched).

@@ -1237,4 +1237,78 @@ esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const in
   return status;
 }
 
+// ------------------------------------ allocation-free FP64 pressure solve
+// Scratch of esf_pressure_solve_static: one file-scope device array, carved
+// into [PcrState | block partials | invd r d Ap s], sized for grids of at
+// most ESF_STATIC_SOLVE_MAX_CELLS cells (10.1 MiB). It is part of the
+// module image, so no call allocates device or pinned memory, creates a
+// stream, event or graph, or frees anything.
+constexpr long long kStaticPartials = 16384;
+constexpr size_t kStaticStateBytes = 256;
+constexpr size_t kStaticScratchBytes =
+    kStaticStateBytes + kStaticPartials * 8 + 5ull * ESF_STATIC_SOLVE_MAX_CELLS * 8;
+static_assert(sizeof(PcrState) <= kStaticStateBytes, "PcrState outgrew its slot");
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+esf_status static_scratch_address(void** out) {
+  return cudaGetSymbolAddress(out, g_static_scratch) == cudaSuccess ? ESF_OK : ESF_ERR_CUDA;
+}
+
+// The reference's FP64 solvePCR with the kernels of the graph path, launched
+// one by one: set-up, iterations 0..5 and their residual check, then chunks
+// of 5 iterations + check, the state polled after every 4 chunks (kernels
+// queued after convergence exit at once, as in the graph path). Same kernels
+// in the same order as esf_pressure_solve at ESF_FP64, so the same bits.
+esf_status pressure_solve_static(void* scratch, const GridDev& g, const double* minv,
+                                 const double* diag, const double* b, double* x, double eps,
+                                 int maxIt, int* iters, double* relres, int* converged,
+                                 cudaStream_t st) {
+  if (g.R > ESF_STATIC_SOLVE_MAX_CELLS) {
+    set_error("esf_pressure_solve_static: grid has %lld cells, the static scratch holds at most %d",
+              g.R, ESF_STATIC_SOLVE_MAX_CELLS);
+    return ESF_ERR_UNSUPPORTED;
+  }
+  {
+    dim3 gr = stencil_grid<double>(g);
+    long long nb = (long long)gr.x * gr.y * gr.z;
+    if (nb > kStaticPartials) {
+      set_error("esf_pressure_solve_static: grid needs %lld stencil blocks, the static scratch holds "
+                "%lld partial sums", nb, kStaticPartials);
+      return ESF_ERR_UNSUPPORTED;
+    }
+  }
+  unsigned char* base = static_cast<unsigned char*>(scratch);
+  PcrState* state = reinterpret_cast<PcrState*>(base);
+  double* partial = reinterpret_cast<double*>(base + kStaticStateBytes);
+  double* vec = partial + kStaticPartials;
+  const long long R = g.R;
+  double *invd = vec, *r = vec + R, *d = vec + 2 * R, *Ap = vec + 3 * R, *s = vec + 4 * R;
+  ESF_COUNTED inv_vec<<<vec_blocks(R), VT, 0, st>>>(R, diag, invd, nullptr);
+  ESF_LAUNCH_CHECK();
+  // zeroes the whole state (tickets included) before any kernel reads it;
+  // set-up zeroes d and Ap
+  {
+    esf_status e = init_state(state, eps, maxIt, st);
+    if (e) return e;
+  }
+  PressureKernels<double> k{g, minv, invd, b, x, r, d, Ap, s, partial, state};
+  k.setup_warm(st);
+  k.chunk(st, 6, true);
+  ESF_LAUNCH_CHECK();
+  const int maxChunks = maxIt / 5 + 3;
+  int launched = 1;
+  PcrState h;
+  for (;;) {
+    ESF_CUDA(cudaMemcpyAsync(&h, state, sizeof h, cudaMemcpyDeviceToHost, st));
+    ESF_CUDA(cudaStreamSynchronize(st));
+    if (h.done || launched >= maxChunks) break;
+    for (int c = 0; c < 4 && launched < maxChunks; c++, launched++) k.chunk(st, 5, true);
+    ESF_LAUNCH_CHECK();
+  }
+  if (iters) *iters = h.iter;
+  if (converged) *converged = h.converged;
+  if (relres) *relres = h.bnorm2 > 0 ? sqrt(h.resid2 / h.bnorm2) : sqrt(h.resid2);
+  return h.status ? (esf_status)h.status : ESF_OK;
+}
+
 }  // namespace esf

@@ -11,6 +11,7 @@
 
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1242,6 +1243,56 @@ extern "C" esf_status esf_pressure_solve(const esf_grid* g, const double* minv, 
                                 &cv, (cudaStream_t)stream);
   cudaStreamSynchronize((cudaStream_t)stream);
   pressure_work_free(w);
+  if (iters) *iters = it;
+  if (relres) *relres = rr;
+  return e;
+}
+
+// Per-device address of the static scratch, looked up on the first call on
+// each device.
+static std::mutex g_static_mu;
+static void* g_static_addr[ESF_STATIC_SOLVE_MAX_DEVICES];
+
+extern "C" esf_status esf_pressure_solve_static(const esf_grid* g, const double* minv,
+                                                const double* diag, const double* b, double* x,
+                                                double eps, int maxIt, int* iters, double* relres,
+                                                void* stream) {
+  if (!g || !minv || !diag || !b || !x || g->xRes < 3 || g->yRes < 3 || g->zRes < 3 || maxIt < 0) {
+    set_error("esf_pressure_solve_static: invalid argument");
+    return ESF_ERR_INVALID_ARG;
+  }
+  const long long cells = (long long)(g->xRes - 1) * (g->yRes - 1) * (g->zRes - 1);
+  if (cells > ESF_STATIC_SOLVE_MAX_CELLS) {
+    set_error("esf_pressure_solve_static: grid has %lld cells, the static scratch holds at most %d",
+              cells, ESF_STATIC_SOLVE_MAX_CELLS);
+    return ESF_ERR_UNSUPPORTED;
+  }
+  int dev = 0;
+  ESF_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= ESF_STATIC_SOLVE_MAX_DEVICES) {
+    set_error("esf_pressure_solve_static: device %d beyond the %d supported", dev,
+              ESF_STATIC_SOLVE_MAX_DEVICES);
+    return ESF_ERR_UNSUPPORTED;
+  }
+  void* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_addr[dev]) {
+      void* p = nullptr;
+      if (static_scratch_address(&p) != ESF_OK || !p) {
+        set_error("esf_pressure_solve_static: cudaGetSymbolAddress failed on device %d: %s", dev,
+                  cudaGetErrorString(cudaGetLastError()));
+        return ESF_ERR_CUDA;
+      }
+      g_static_addr[dev] = p;
+    }
+    scratch = g_static_addr[dev];
+  }
+  GridDev G = grid_dev(g);
+  int it = 0, cv = 0;
+  double rr = 0;
+  esf_status e = pressure_solve_static(scratch, G, minv, diag, b, x, eps, maxIt, &it, &rr, &cv,
+                                       (cudaStream_t)stream);
   if (iters) *iters = it;
   if (relres) *relres = rr;
   return e;

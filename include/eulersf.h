@@ -236,6 +236,30 @@ esf_status esf_pressure_solve(const esf_grid* grid, const double* mass_inv_node,
                               double eps, int max_iterations, int precision,
                               int* iterations, double* rel_residual, void* stream);
 
+/* Allocation-free variant of esf_pressure_solve at ESF_FP64; no reference
+ * counterpart (solvePCR allocates its vectors per call,
+ * CONJUGATE_RESIDUAL.inl:109-125). For callers that must not allocate or
+ * free device memory during a solve: a host whose HBM is reserved up front
+ * by its own pool (a framework's caching allocator, a serving runtime), where
+ * a cudaMalloc can fail or fragment, and callers overlapping other streams,
+ * which cudaFree's implicit device-wide synchronisation would stall.
+ * Same kernels, order and results as esf_pressure_solve(..., ESF_FP64, ...).
+ * Its scratch is a file-scope static device array (10.1 MiB per device,
+ * part of the loaded module) for grids of at most ESF_STATIC_SOLVE_MAX_CELLS
+ * cells; larger grids return ESF_ERR_UNSUPPORTED with a message. Nothing is
+ * allocated, freed or created (no stream, event or graph). The scratch
+ * address is looked up with cudaGetSymbolAddress on the first call on each
+ * device (this can load the module): make that first call outside any stream
+ * capture. One scratch per device: calls that overlap on the same device,
+ * from two host threads or two streams, race on it and must be serialised by
+ * the caller. Returns when the solve has finished on `stream`. */
+#define ESF_STATIC_SOLVE_MAX_CELLS (64 * 64 * 64)
+#define ESF_STATIC_SOLVE_MAX_DEVICES 64
+esf_status esf_pressure_solve_static(const esf_grid* grid, const double* mass_inv_node,
+                                     const double* diag, const double* b, double* x,
+                                     double eps, int max_iterations, int* iterations,
+                                     double* rel_residual, void* stream);
+
 /* ---- instrumentation (no reference counterpart beyond TIMING_BREAKDOWN) -- */
 /* Number of kernels this library has launched in this process (graph
  * replays count every kernel node). */

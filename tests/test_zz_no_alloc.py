@@ -1,0 +1,88 @@
+"""esf_pressure_solve_static, the allocation-free FP64 pressure solve, against
+esf_pressure_solve at ESF_FP64 on two different systems solved one after the
+other (and the first again): same iterations, same bits, the same device
+memory free before and after. Collected last so that it runs both alone and
+after every other test in the process."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(a):
+    import torch
+    return torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def _jacobi_diag(X, minv):
+    """diag(J M^-1 J^T): 3 m^-1 summed over the DOF corners of each cell."""
+    m = minv.reshape(X, X, X).copy()
+    m[0, :, :] = m[-1, :, :] = 0
+    m[:, 0, :] = m[:, -1, :] = 0
+    m[:, :, 0] = m[:, :, -1] = 0
+    d = np.zeros((X - 1,) * 3)
+    for i in range(8):
+        dx, dy, dz = i & 1, (i >> 1) & 1, (i >> 2) & 1
+        d += 3 * m[dz:dz + X - 1, dy:dy + X - 1, dx:dx + X - 1]
+    return d.reshape(-1)
+
+
+def _system(X, seed):
+    rng = np.random.default_rng(seed)
+    g = oracle.grid(X, 1.0 / (X - 1))
+    minv = rng.uniform(50.0, 300.0, X ** 3)
+    b = oracle.pressure_apply(g, minv, rng.standard_normal((X - 1) ** 3))
+    x0 = 0.1 * rng.standard_normal(len(b))
+    return g, minv, _jacobi_diag(X, minv), b, x0
+
+
+def _solve(lib, fn, system):
+    import torch
+    g, minv, diag, b, x0 = system
+    dm, dd, db, dx = _dev(minv), _dev(diag), _dev(b), _dev(x0)
+    it, rr = C.c_int(), C.c_double()
+    if fn == "static":
+        s = lib.esf_pressure_solve_static(C.byref(g), _ptr(dm), _ptr(dd), _ptr(db), _ptr(dx), 1e-8,
+                                          20000, C.byref(it), C.byref(rr), None)
+    else:
+        s = lib.esf_pressure_solve(C.byref(g), _ptr(dm), _ptr(dd), _ptr(db), _ptr(dx), 1e-8, 20000,
+                                   0, C.byref(it), C.byref(rr), None)
+    torch.cuda.synchronize()
+    return s, it.value, rr.value, dx.cpu().numpy()
+
+
+def test_static_solve_equals_allocating_solve(gpu_lib):
+    import torch
+    systems = [_system(25, 11), _system(33, 12)]
+    # first call on this device: looks up the scratch address
+    first = _solve(gpu_lib, "static", systems[0])
+    free0 = torch.cuda.mem_get_info()[0]
+    got = [_solve(gpu_lib, "static", systems[1]), _solve(gpu_lib, "static", systems[0])]
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 == free0, (free0, free1)
+    ref = [_solve(gpu_lib, "alloc", s) for s in systems]
+    for (s, it, rr, x), (s0, it0, rr0, x0) in zip([first, got[0]], ref):
+        assert s == 0 and s0 == 0
+        assert rr < 1e-8 and it == it0 and rr == rr0
+        assert np.array_equal(x, x0)
+    # the repeat of system 0 starts from clean scratch: identical to the first call
+    assert got[1][1] == first[1] and np.array_equal(got[1][3], first[3])
+
+
+def test_static_solve_rejects_oversize_grid(gpu_lib):
+    g = oracle.grid(66, 1.0 / 65)  # 65^3 cells > 64^3
+    nodes, cells = np.ones(66 ** 3), np.ones(65 ** 3)
+    dm, dd, db, dx = _dev(nodes), _dev(cells), _dev(cells), _dev(cells)
+    it, rr = C.c_int(), C.c_double()
+    s = gpu_lib.esf_pressure_solve_static(C.byref(g), _ptr(dm), _ptr(dd), _ptr(db), _ptr(dx), 1e-8,
+                                          10, C.byref(it), C.byref(rr), None)
+    assert s == 8  # ESF_ERR_UNSUPPORTED
+    assert b"static scratch holds at most" in gpu_lib.esf_last_error()
