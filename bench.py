@@ -138,30 +138,6 @@ def sum_over_ranks(pg, v):
 
 
 # --------------------------------------------------------- CPU baseline
-def synthetic_pressure_problem(desc, seed=0):
-    """A pressure problem of the workload's size: m^-1 of fluid nodes
-    (rho_f dh^3) with the ball's nodes also carrying solid mass, its Jacobi
-    diagonal and a smooth right-hand side. The cost of a PCR iteration
-    depends only on the grid, not on these values."""
-    import numpy as np
-    res, N, dh = desc.res, desc.N, desc.dh
-    s = desc.solids[0]
-    z, y, x = np.meshgrid(*(np.arange(res) * dh,) * 3, indexing="ij")
-    fluid = desc.fluid_density * dh ** 3
-    inside = (x - s.center[0]) ** 2 + (y - s.center[1]) ** 2 + (z - s.center[2]) ** 2 <= s.radius ** 2
-    mass = fluid + np.where(inside, s.density * dh ** 3, 0.0)
-    minv = (1.0 / mass).reshape(-1)
-    m = minv.reshape(res, res, res).copy()
-    m[0], m[-1], m[:, 0], m[:, -1], m[:, :, 0], m[:, :, -1] = 0, 0, 0, 0, 0, 0
-    diag = np.zeros((N, N, N))
-    for i in range(8):
-        dx, dy, dz = i & 1, (i >> 1) & 1, (i >> 2) & 1
-        diag += 3 * m[dz:dz + N, dy:dy + N, dx:dx + N]
-    rng = np.random.default_rng(seed)
-    b = rng.standard_normal(N ** 3)
-    return minv, diag.reshape(-1), b
-
-
 def cpu_pressure_sample(desc, iters, threads=None):
     """Time `iters` FP64 pressure-PCR iterations at the workload's size with
     the CPU oracle (the reference's algorithm restated in C, OpenMP on the
@@ -171,7 +147,8 @@ def cpu_pressure_sample(desc, iters, threads=None):
     if threads:
         os.environ["OMP_NUM_THREADS"] = str(threads)
     import oracle
-    minv, diag, b = synthetic_pressure_problem(desc)
+    from eulersf_gb300.scene import pressure_problem
+    minv, diag, b = pressure_problem(desc)
     g = oracle.grid(desc.res, desc.dh)
     oracle.pressure_apply(g, minv, b)  # load + first touch
     t0 = time.perf_counter()
@@ -242,9 +219,11 @@ def ours(args):
     torch.cuda.synchronize()
     l0 = lib.esf_kernel_launches()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("timed")
     e0.record(stream)
     reports = [I.stepImplicit() for _ in range(args.steps)]
     e1.record(stream)
+    torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     barrier(pg)
     launches = lib.esf_kernel_launches() - l0
@@ -329,7 +308,7 @@ def ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=256)

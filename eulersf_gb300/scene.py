@@ -289,3 +289,29 @@ def write_scene(desc: SceneDesc, directory: str, name: str = "sphere") -> str:
     noise = noise_field(desc.res, desc.noise_seed, desc.noise_amplitude)
     noise.astype("<f8").tofile(os.path.join(directory, "noise.f64"))
     return cfg_path
+
+
+def pressure_problem(desc: SceneDesc, seed: int = 0):
+    """A pressure system of the scene's size, for the solver seam alone:
+    node m^-1 of the fluid (rho_f dh^3) with the sphere's nodes also carrying
+    solid mass (boundary nodes carry no unknown), the Jacobi diagonal of
+    J diag(m^-1) J^T (3 m^-1 summed over each cell's DOF corners) and a
+    seeded standard-normal right-hand side. Returns (minv, diag, b) as
+    float64 arrays of X^3, N^3 and N^3 entries. The cost of a PCR iteration
+    depends only on the grid, not on these values."""
+    res, N, dh = desc.res, desc.N, desc.dh
+    s = desc.solids[0]
+    z, y, x = np.meshgrid(*(np.arange(res) * dh,) * 3, indexing="ij")
+    fluid = desc.fluid_density * dh ** 3
+    inside = (x - s.center[0]) ** 2 + (y - s.center[1]) ** 2 + (z - s.center[2]) ** 2 <= s.radius ** 2
+    mass = fluid + np.where(inside, s.density * dh ** 3, 0.0)
+    minv = (1.0 / mass).reshape(-1)
+    m = minv.reshape(res, res, res).copy()
+    m[0], m[-1], m[:, 0], m[:, -1], m[:, :, 0], m[:, :, -1] = 0, 0, 0, 0, 0, 0
+    diag = np.zeros((N, N, N))
+    for i in range(8):
+        dx, dy, dz = i & 1, (i >> 1) & 1, (i >> 2) & 1
+        diag += 3 * m[dz:dz + N, dy:dy + N, dx:dx + N]
+    rng = np.random.default_rng(seed)
+    b = rng.standard_normal(N ** 3)
+    return minv, diag.reshape(-1), b
