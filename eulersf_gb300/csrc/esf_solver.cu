@@ -13,8 +13,12 @@
 #include <stdlib.h>
 #include <string.h>
 #include <chrono>
+#include <type_traits>
 
 #include <vector>
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 #include "esf_common.cuh"
 
@@ -336,6 +340,8 @@ __global__ void __launch_bounds__(NT) pressure_stencil(GridDev g, StencilArgs<T>
   }
 }
 
+#include "esf_tma.cuh"
+
 // ------------------------------------------------------- vector kernels
 constexpr int VT = 256;
 
@@ -456,6 +462,20 @@ __global__ void convert_vec(long long n, const A* in, B* out) {
   for (long long i = blockIdx.x * (long long)VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT)
     out[i] = (B)in[i];
 }
+// Node m^-1 in FP32 with rows padded to `pitch` floats (a multiple of 4, as
+// TMA wants 16-byte row strides); boundary nodes (no unknown) and padding 0.
+__global__ void convert_minv_padded(GridDev g, const double* in, float* out, int pitch) {
+  const long long n = (long long)pitch * g.Y * g.Z;
+  for (long long i = blockIdx.x * (long long)VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT) {
+    const int x = (int)(i % pitch);
+    const long long yz = i / pitch;
+    const int y = (int)(yz % g.Y), z = (int)(yz / g.Y);
+    float v = 0.0f;
+    if (x > 0 && x < g.X - 1 && y > 0 && y < g.Y - 1 && z > 0 && z < g.Z - 1)
+      v = (float)in[x + (long long)y * g.X + (long long)z * g.slab];
+    out[i] = v;
+  }
+}
 __global__ void inv_vec(long long n, const double* in, double* out64, float* out32) {
   for (long long i = blockIdx.x * (long long)VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT) {
     double v = 1.0 / in[i];
@@ -494,6 +514,11 @@ struct PressureWork {
   cudaEvent_t ev[4];
   unsigned long long kFirst, kChunk, kFirst32, kChunk32;  // kernels per graph
   PcrState* stT;  // state used by the kernel timer
+  // TMA path of the FP32 update kernel (cells per row a multiple of 4)
+  float* minv32p;  // padded node m^-1
+  int mpitch;
+  TmaMaps tmaps;
+  bool tmaOk;
 };
 
 // z-chunk depth: deep enough to amortise the two halo layers, shallow
@@ -550,6 +575,8 @@ esf_status pressure_work_alloc(PressureWork** out, const GridDev& g, int mixed) 
     ESF_CUDA(cudaMalloc(&w->invd32, R * 4));
     ESF_CUDA(cudaMalloc(&w->b32, R * 4));
     ESF_CUDA(cudaMalloc(&w->minv32, g.T * 4));
+    w->mpitch = (g.X + 3) / 4 * 4;
+    ESF_CUDA(cudaMalloc(&w->minv32p, (size_t)w->mpitch * g.Y * g.Z * 4));
   }
   ESF_CUDA(cudaMalloc(&w->partial, ESF_MAX_PARTIALS * 8));
   ESF_CUDA(cudaMalloc(&w->st, sizeof(PcrState)));
@@ -568,7 +595,7 @@ void pressure_work_free(PressureWork* w) {
   if (!w) return;
   cudaFree(w->r); cudaFree(w->d); cudaFree(w->Ap); cudaFree(w->s); cudaFree(w->invd);
   cudaFree(w->x32); cudaFree(w->r32); cudaFree(w->d32); cudaFree(w->Ap32); cudaFree(w->s32);
-  cudaFree(w->invd32); cudaFree(w->b32); cudaFree(w->minv32);
+  cudaFree(w->invd32); cudaFree(w->b32); cudaFree(w->minv32); cudaFree(w->minv32p);
   cudaFree(w->partial); cudaFree(w->st); cudaFree(w->st32); cudaFree(w->stT);
   if (w->hst) cudaFreeHost(w->hst);
   if (w->gFirst) cudaGraphExecDestroy(w->gFirst);
@@ -581,6 +608,71 @@ void pressure_work_free(PressureWork* w) {
   delete w;
 }
 
+// ---- tensor maps of the TMA update kernel
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+// 3-D FP32 array [d][h][w] (w a multiple of 4), box bw x bh x 1, zero fill
+static esf_status encode3d(CUtensorMap* m, const void* base, long long w, long long h, long long d,
+                           unsigned bw, unsigned bh) {
+  PFN_cuTensorMapEncodeTiled_v12000 fn = tensor_map_encoder();
+  if (!fn) {
+    set_error("cuTensorMapEncodeTiled is not available from the driver");
+    return ESF_ERR_CUDA;
+  }
+  cuuint64_t dims[3] = {(cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)d};
+  cuuint64_t strides[2] = {(cuuint64_t)w * 4, (cuuint64_t)w * h * 4};
+  cuuint32_t box[3] = {bw, bh, 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(base), dims, strides, box, es,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return ESF_ERR_CUDA;
+  }
+  return ESF_OK;
+}
+
+// Chooses the FP32 update kernel for the mixed path: the TMA-staged one when
+// the cell rows are a multiple of 4 floats (16-byte row strides) unless
+// ESF_PRESSURE_KERNEL=register asks for the register-prefetch kernel (same
+// bits; kept for comparison). Converts m^-1 into the padded layout and
+// builds the maps once per work.
+static esf_status prepare_tma(PressureWork* w, const GridDev& g, const double* minv64,
+                              cudaStream_t st, const TmaMaps** out) {
+  *out = nullptr;
+  const char* pick = getenv("ESF_PRESSURE_KERNEL");
+  if (g.cX % 4 != 0 || (pick && strcmp(pick, "register") == 0)) return ESF_OK;
+  ESF_COUNTED convert_minv_padded<<<vec_blocks((long long)w->mpitch * g.Y * g.Z), VT, 0, st>>>(
+      g, minv64, w->minv32p, w->mpitch);
+  ESF_LAUNCH_CHECK();
+  if (!w->tmaOk) {
+    TmaMaps m;
+    esf_status e;
+    if ((e = encode3d(&m.r, w->r32, g.cX, g.cY, g.cZ, TMA_HW, TMA_HH))) return e;
+    if ((e = encode3d(&m.ap, w->Ap32, g.cX, g.cY, g.cZ, TMA_HW, TMA_HH))) return e;
+    if ((e = encode3d(&m.iv, w->invd32, g.cX, g.cY, g.cZ, TMA_HW, TMA_HH))) return e;
+    if ((e = encode3d(&m.x, w->x32, g.cX, g.cY, g.cZ, TX, TY))) return e;
+    if ((e = encode3d(&m.d, w->d32, g.cX, g.cY, g.cZ, TX, TY))) return e;
+    if ((e = encode3d(&m.m, w->minv32p, w->mpitch, g.Y, g.Z, TMA_NW, TMA_NH))) return e;
+    w->tmaps = m;
+    w->tmaOk = true;
+  }
+  *out = &w->tmaps;
+  return ESF_OK;
+}
+
 // Enqueue iterations of the PCR loop for precision T on stream s.
 template <typename T>
 struct PressureKernels {
@@ -589,6 +681,7 @@ struct PressureKernels {
   T *x, *r, *d, *Ap, *s;
   double* partial;
   PcrState* st;
+  const TmaMaps* tma = nullptr;  // FP32 only: TMA-staged update kernel
   void setup_warm(cudaStream_t cs) const {  // r = (b - Ax)/diag, ||b||; then s = Ar, delta
     StencilArgs<T> a;
     memset(&a, 0, sizeof a);
@@ -605,6 +698,13 @@ struct PressureKernels {
     ESF_COUNTED pcr_phase_a<T, true><<<vec_blocks(g.R), VT, 0, cs>>>(g.R, d, r, Ap, s, invd, partial, st);
   }
   void update(cudaStream_t cs) const {
+    if constexpr (std::is_same<T, float>::value) {
+      if (tma) {
+        ESF_COUNTED pressure_update_tma<<<stencil_grid<T>(g), NT, 0, cs>>>(g, *tma, x, s, partial, st,
+                                                                        stencil_cz(g));
+        return;
+      }
+    }
     StencilArgs<T> a;
     memset(&a, 0, sizeof a);
     a.x = x; a.d = d; a.r = r; a.Ap = Ap; a.invd = invd; a.minv = minv; a.out = s;
@@ -761,9 +861,15 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
   // feeds the operator's near-null checkerboard modes (J J^T on the
   // node-collocated grid).
   ESF_COUNTED convert_vec<double, float><<<vec_blocks(g.T), VT, 0, st>>>(g.T, minv64, w->minv32);
+  const TmaMaps* tma = nullptr;
+  {
+    esf_status e = prepare_tma(w, g, minv64, st, &tma);
+    if (e) return e;
+  }
   PressureKernels<float> k32{g, w->minv32, w->invd32, w->b32, w->x32, w->r32, w->d32, w->Ap32,
                              w->s32, w->partial, w->st32};
-  const void* key[8] = {w->minv32, w->invd32, w->b32, w->x32, nullptr, nullptr, nullptr, nullptr};
+  k32.tma = tma;
+  const void* key[8] = {w->minv32, w->invd32, w->b32, w->x32, tma, nullptr, nullptr, nullptr};
   if (!w->graphsFor32 || memcmp(key, w->keyB, sizeof key) != 0) {
     esf_status e = capture(w->capStream, k32, false, false, &w->gChunk32, &w->kChunk32);
     if (e) return e;
@@ -901,7 +1007,8 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
 template <typename T>
 static esf_status time_kernels_t(PressureWork* w, const GridDev& g, const T* minv, const T* invd,
                                  const T* bsrc, T* x, T* r, T* d, T* Ap, T* s, int reps,
-                                 double* upd, double* ax, cudaStream_t st) {
+                                 double* upd, double* ax, cudaStream_t st,
+                                 const TmaMaps* tma = nullptr) {
   const long long R = g.R;
   ESF_CUDA(cudaMemcpyAsync(r, bsrc, R * sizeof(T), cudaMemcpyDeviceToDevice, st));
   ESF_CUDA(cudaMemcpyAsync(d, bsrc, R * sizeof(T), cudaMemcpyDeviceToDevice, st));
@@ -920,6 +1027,7 @@ static esf_status time_kernels_t(PressureWork* w, const GridDev& g, const T* min
   ESF_CUDA(cudaMemcpyAsync(w->stT, &h, sizeof h, cudaMemcpyHostToDevice, st));
   ESF_CUDA(cudaStreamSynchronize(st));
   PressureKernels<T> k{g, minv, invd, bsrc, x, r, d, Ap, s, w->partial, w->stT};
+  k.tma = tma;
   cudaEvent_t e0, e1, e2;
   ESF_CUDA(cudaEventCreate(&e0));
   ESF_CUDA(cudaEventCreate(&e1));
@@ -954,8 +1062,11 @@ esf_status pressure_time_kernels(PressureWork* w, const GridDev& g, const double
     ESF_COUNTED convert_vec<double, float><<<vec_blocks(g.T), VT, 0, st>>>(g.T, minv64, w->minv32);
     ESF_COUNTED convert_vec<double, float><<<vec_blocks(g.R), VT, 0, st>>>(g.R, b, w->b32);
     ESF_LAUNCH_CHECK();
+    const TmaMaps* tma = nullptr;
+    esf_status e = prepare_tma(w, g, minv64, st, &tma);
+    if (e) return e;
     return time_kernels_t<float>(w, g, w->minv32, w->invd32, w->b32, w->x32, w->r32, w->d32,
-                                 w->Ap32, w->s32, reps, update_ms, axpy_ms, st);
+                                 w->Ap32, w->s32, reps, update_ms, axpy_ms, st, tma);
   }
   // FP64: x scratch is w->s's neighbour; use the FP64 work arrays only
   double* xs = nullptr;
