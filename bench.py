@@ -6,8 +6,8 @@ density 1100, E = 2e5, nu = 0.45, fluid density 1000, gravity 9.8,
 dt = 1/240, all solves to 1e-8 relative residual, seeded fluid noise
 (seed 7), mixed precision (FP32 inner PCR in FP64 refinement). Synthetic
 input: the scene generator of eulersf_gb300/scene.py. Every working array
-(>= 135 MB each, ~2 GB in all) is larger than the 129 MB L2, so no flush is
-needed between steps.
+the pressure iterations stream (>= 67 MB each, ~4 GB in all) is larger than
+the 129 MB L2, so no flush is needed between steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -29,12 +29,23 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "coupled steps/s at 256^3 (mixed precision; CG iters/s reported beside it)"
+METRIC = "coupled steps/s and CG iters/s at 256^3 (mixed vs FP64 GPU)"
 UNIT = "steps/s"
-# Pressure PCR iterations of the reference's FP64 algorithm per step of this
-# workload, measured with the FP64 GPU path (its counts match the reference's
-# to within one 5-iteration check interval): profiles/pressure_fp64_256.md.
-FP64_ITERS_PER_STEP_256 = 18025
+# Pressure PCR iterations per step of the reference's FP64 algorithm on this
+# workload (steps 0-7), from the FP64 GPU path, whose counts match the
+# reference's to within one 5-iteration check interval:
+# profiles/mixed_vs_fp64_256.md. Later steps use the mean of steps 5-7.
+FP64_PRESSURE_ITERS_256 = [19060, 14655, 9545, 8925, 6770, 5385, 5740, 5360]
+
+
+def fp64_iters(step):
+    t = FP64_PRESSURE_ITERS_256
+    return t[step] if step < len(t) else sum(t[-3:]) / 3.0
+
+
+def fp64_iters_window(warmup, steps):
+    """FP64 pressure iterations per step over the timed steps warmup .. warmup+steps-1."""
+    return sum(fp64_iters(k) for k in range(warmup, warmup + steps)) / steps
 
 
 def workload(N=256, seed=7):
@@ -176,14 +187,15 @@ def reference_arm(args):
     sample_iters = max(2, args.cpu_iters)
     for _ in range(args.warmup):
         cpu_pressure_sample(desc, 1, threads)
-    for _ in range(args.steps):
+    for k in range(args.warmup, args.warmup + args.steps):
         it, t = cpu_pressure_sample(desc, sample_iters, threads)
-        per_step.append(t / max(it, 1) * FP64_ITERS_PER_STEP_256)
+        per_step.append(t / max(it, 1) * fp64_iters(k))
     t_step = statistics.mean(per_step)
     value = 1.0 / t_step
     sample = (f"{sample_iters} FP64 pressure-PCR iterations at {desc.N}^3 per timed step "
-              f"(oracle port, {threads} threads); steps/s = iterations/s / "
-              f"{FP64_ITERS_PER_STEP_256} iterations per step (the reference algorithm's count); "
+              f"(oracle port, {threads} threads); each step's time = time per iteration x the "
+              f"reference algorithm's pressure iterations of that step (steps {args.warmup}.."
+              f"{args.warmup + args.steps - 1}: {fp64_iters_window(args.warmup, args.steps):.0f} per step); "
               f"the non-solver part of the step (<2% at this tolerance) is not counted")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_step,
@@ -198,7 +210,6 @@ def reference_arm(args):
 
 # ------------------------------------------------------------- our arm
 def ours(args):
-    import numpy as np
     import torch
     rank, world, pg = dist_setup(args.gpus)
     local = int(os.environ.get("LOCAL_RANK", 0))
@@ -212,79 +223,88 @@ def ours(args):
     I = E.make_scene(desc, precision=prec, stream=stream.cuda_stream)
     for _ in range(args.warmup):
         I.stepImplicit()
-    # ---- timed region: device time, inputs resident in HBM
+    # ---- timed region. Every step goes through the public C ABI: the step's
+    # input field (intensity, the smoke source) is copied in from pinned host
+    # memory, esf_step runs, and its result (the velocity field) is copied
+    # out. `value` is the device time of the steps alone (CUDA events around
+    # esf_step on the scene stream, inputs resident); `e2e` is the wall time
+    # of the whole loop including both copies.
+    res = desc.res
+    h_in = torch.from_numpy(I.get("intensity")).pin_memory()
+    h_out = torch.empty(res ** 3 * 3, dtype=torch.float64).pin_memory()
+    fid_in, fid_out = abi.FIELDS["intensity"][0], abi.FIELDS["velocity"][0]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    reports = []
+    rep = abi.StepReport()
     clocks = ClockSampler(local)
     clocks.start()
     barrier(pg)
     torch.cuda.synchronize()
     l0 = lib.esf_kernel_launches()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.nvtx.range_push("timed")
-    e0.record(stream)
-    reports = [I.stepImplicit() for _ in range(args.steps)]
-    e1.record(stream)
-    torch.cuda.nvtx.range_pop()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        st_in = lib.esf_set_field(I._h, fid_in, 0, C.c_void_p(h_in.data_ptr()), h_in.numel() * 8)
+        ev[k][0].record(stream)
+        st = lib.esf_step(I._h, C.byref(rep))
+        ev[k][1].record(stream)
+        st_out = lib.esf_get_field(I._h, fid_out, 0, C.c_void_p(h_out.data_ptr()), h_out.numel() * 8)
+        if st_in or st_out or st not in (0, 6):  # 6: ESF_ERR_NUMERIC, carried in the report
+            raise RuntimeError(f"step {k}: status {st_in}/{st}/{st_out}: {E.last_error()}")
+        reports.append(rep.as_dict())
     torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t0
+    torch.cuda.nvtx.range_pop()
     barrier(pg)
     launches = lib.esf_kernel_launches() - l0
     clk = clocks.stop()
-    t = e0.elapsed_time(e1) / 1e3
+    t = sum(a.elapsed_time(b) for a, b in ev) / 1e3
     t_max = max_over_ranks(pg, t)
+    te = max_over_ranks(pg, t_wall)
     steps_all = sum_over_ranks(pg, args.steps)
     value = steps_all / t_max
     piters = sum(r["iterations"][1] for r in reports)
     cg_rate = sum_over_ranks(pg, piters) / t_max
+    e2e = {"value": steps_all / te, "unit": UNIT,
+           "h2d_bytes_per_step": int(h_in.numel() * 8), "d2h_bytes_per_step": int(h_out.numel() * 8),
+           "what": "the timed steps themselves, each with the intensity field copied in and the "
+                   "velocity field copied out through pinned host buffers (esf_set_field, esf_step, "
+                   "esf_get_field)"}
     # ---- dominant kernel: fused update + stencil + dot of the pressure PCR
     upd, axpy = C.c_double(), C.c_double()
-    st = lib.esf_time_pressure_kernels(I._h, 20, C.byref(upd), C.byref(axpy))
+    stt = lib.esf_time_pressure_kernels(I._h, 20, C.byref(upd), C.byref(axpy))
     R = desc.N ** 3
     w = 4 if prec == abi.ESF_MIXED else 8
     peak, peak_kind = read_peaks()
-    algo = 10 * w * R  # P2 + P3 of the per-iteration byte model: 10 words per row
-    achieved = algo / (upd.value * 1e-3) / 1e9 if st == 0 and upd.value > 0 else None
+    algo = 10 * w * R  # P2 + P3 of the 17.6-word per-iteration model
+    achieved = algo / (upd.value * 1e-3) / 1e9 if stt == 0 and upd.value > 0 else None
     traffic = None
     tp = os.path.join(ROOT, "profiles", "pressure_update_traffic.json")
     if os.path.exists(tp):
         with open(tp) as f:
             tj = json.load(f)
-        key = f"{'fp32' if w == 4 else 'fp64'}_{desc.N}"
-        if key in tj:
-            traffic = tj[key]
+        traffic = tj.get(f"{'fp32' if w == 4 else 'fp64'}_{desc.N}")
+    kname = ("pressure_update_tma" if (w == 4 and desc.N % 4 == 0) else
+             f"pressure_stencil<{'float' if w == 4 else 'double'}, update>")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                "peak_kind": peak_kind, "kernel": f"pressure_stencil<{'float' if w == 4 else 'double'}, update>",
+                "peak_kind": peak_kind, "kernel": kname,
                 "kernel_ms": upd.value, "axpy_kernel_ms": axpy.value,
                 "algorithmic_bytes_per_launch": algo}
-    # ---- e2e: public API with host buffers (pinned), copies in the timed region
-    e2e = None
-    if args.e2e_steps > 0:
-        res = desc.res
-        inten = I.get("intensity")
-        h_in = torch.from_numpy(inten).pin_memory()
-        h_out = torch.empty(res ** 3 * 3, dtype=torch.float64).pin_memory()
-        fid_in, fid_out = abi.FIELDS["intensity"][0], abi.FIELDS["velocity"][0]
-        barrier(pg)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
-            lib.esf_set_field(I._h, fid_in, 0, C.c_void_p(h_in.data_ptr()), h_in.numel() * 8)
-            lib.esf_step(I._h, None)
-            lib.esf_get_field(I._h, fid_out, 0, C.c_void_p(h_out.data_ptr()), h_out.numel() * 8)
-        torch.cuda.synchronize()
-        te = max_over_ranks(pg, time.perf_counter() - t0)
-        e2e = {"value": sum_over_ranks(pg, args.e2e_steps) / te, "unit": UNIT,
-               "h2d_bytes_per_step": int(h_in.numel() * 8), "d2h_bytes_per_step": int(h_out.numel() * 8),
-               "what": "per step: intensity field H2D, esf_step, velocity field D2H (pinned host buffers)"}
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = cpu_threads()
         it, tc = cpu_pressure_sample(desc, args.cpu_iters, threads)
-        t_step = tc / max(it, 1) * FP64_ITERS_PER_STEP_256
+        per_iter = tc / max(it, 1)
+        t_step = per_iter * fp64_iters_window(args.warmup, args.steps)
         cpu = {"value": 1.0 / t_step, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{it} FP64 pressure-PCR iterations of this {desc.N}^3 step on the oracle port "
-                         f"({tc:.1f} s); steps/s = iterations/s / {FP64_ITERS_PER_STEP_256} iterations per "
-                         f"step of the reference algorithm; non-solver work not counted"}
+               "sample": f"{it} FP64 pressure-PCR iterations at {desc.N}^3 on the oracle port "
+                         f"({tc:.1f} s, {threads} threads); steps/s = 1 / (time per iteration x "
+                         f"{fp64_iters_window(args.warmup, args.steps):.0f}, the reference algorithm's "
+                         f"pressure iterations per step over the same steps "
+                         f"{args.warmup}..{args.warmup + args.steps - 1}); non-solver work not counted"}
     if rank == 0:
         last = reports[-1]
         line = {
@@ -293,8 +313,11 @@ def ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer" if w == 4 else "f64",
             "data": "synthetic (seeded scene generator)", "config": config_dict(desc, args.precision, world),
             "cg_iters_per_s": cg_rate, "pressure_iters_per_step": piters / args.steps,
+            "pressure_iters_each_step": [r["iterations"][1] for r in reports],
+            "fp64_pressure_iters_same_steps": fp64_iters_window(args.warmup, args.steps),
             "solid_iters_per_step": [r["iterations"][0] + r["iterations"][2] for r in reports],
-            "refinements_last_step": last["refinements"], "rel_residual_last_step": last["rel_residual"],
+            "refinements_last_step": last["refinements"],
+            "rel_residual_max": max(max(r["rel_residual"]) for r in reports),
             "phase_ms_last_step": last["phase_ms"], "roofline": roofline, "cpu_baseline": cpu,
             "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
         }
@@ -313,7 +336,6 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-iters", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
