@@ -5,6 +5,7 @@ Three translation units, compiled in parallel:
   esf_step.cu    every other kernel and the C ABI, -fmad=false so flags, maps
                  and particle seeding keep the reference's non-FMA arithmetic
   esf_config.cpp the cfg reader
+  esf_io.cpp     frame files (gz fields, OBJ); zlib is loaded at run time
 Host code is compiled with -ffp-contract=off for the same reason (the box's
 aarch64 compiler would otherwise contract a*b+c).
 """
@@ -35,6 +36,7 @@ def _sources():
         "esf_solver.cu": ["-O3", "-lineinfo"],
         "esf_step.cu": ["-O3", "-lineinfo", "-fmad=false"],
         "esf_config.cpp": ["-O2"],
+        "esf_io.cpp": ["-O2"],
     }
 
 
@@ -70,10 +72,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
             sys.stderr.write(r.stderr)
         return obj
 
-    with cf.ThreadPoolExecutor(max_workers=3) as ex:
+    with cf.ThreadPoolExecutor(max_workers=4) as ex:
         objs = list(ex.map(one, _sources().items()))
     tmp = LIB + f".tmp{os.getpid()}"
-    cmd = [nvcc, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart"]
+    cmd = [nvcc, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     for o in objs:
         try:

@@ -921,6 +921,19 @@ __global__ void k_recover_X(GridDev g, SolidDev s) {
   }
 }
 
+// DEFOR_SOLID_3D::readFrame (DEFOR_SOLID_3D.cpp:1305-1316): workspace =
+// velocity, X = (node position + origin) - u
+__global__ void k_frame_X(GridDev g, SolidDev s) {
+  FOR_N(g.T, n) {
+    int x = (int)(n % g.X), y = (int)((n / g.X) % g.Y), z = (int)(n / g.slab);
+    double pos[3] = {x * g.dh, y * g.dh, z * g.dh};
+    for (int q = 0; q < 3; q++) {
+      s.vws[3 * n + q] = s.vel[3 * n + q];
+      s.X[3 * n + q] = (pos[q] + g.o[q]) - s.u[3 * n + q];
+    }
+  }
+}
+
 // --------------------------------------------------- surface mesh (a24)
 // DEFOR_SOLID_3D::advectSurfaceMesh (DEFOR_SOLID_3D.cpp:1125-1180)
 __global__ void k_advect_mesh(GridDev g, SolidDev s, int nv, double* verts, const double* rest) {

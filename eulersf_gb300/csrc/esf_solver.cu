@@ -1095,15 +1095,19 @@ __global__ void __launch_bounds__(VT) solid_spmv(long long S, const T* __restric
     // blocks are stored entry-major, B[(j * 9 + e) * S + a]: consecutive
     // threads read consecutive words
     const int* nb = nbr + a;
-#pragma unroll 1
+    // unrolled by rows of the 3x3x3 neighbourhood so that the loads of nine
+    // blocks are in flight together; absent neighbours (m < 0) are skipped,
+    // keeping the summation order of the assembled matrix
+#pragma unroll 9
     for (int j = 0; j < 27; j++) {
-      int m = nb[(long long)j * S];
-      if (m < 0) continue;
-      T v0 = in[3 * (long long)m], v1 = in[3 * (long long)m + 1], v2 = in[3 * (long long)m + 2];
-      const T* Bj = blocks + (long long)j * 9 * S + a;
-      y0 += Bj[0] * v0 + Bj[S] * v1 + Bj[2 * S] * v2;
-      y1 += Bj[3 * S] * v0 + Bj[4 * S] * v1 + Bj[5 * S] * v2;
-      y2 += Bj[6 * S] * v0 + Bj[7 * S] * v1 + Bj[8 * S] * v2;
+      const int m = __ldg(nb + (long long)j * S);
+      if (m >= 0) {
+        const T v0 = in[3 * (long long)m], v1 = in[3 * (long long)m + 1], v2 = in[3 * (long long)m + 2];
+        const T* Bj = blocks + (long long)j * 9 * S + a;
+        y0 += Bj[0] * v0 + Bj[S] * v1 + Bj[2 * S] * v2;
+        y1 += Bj[3 * S] * v0 + Bj[4 * S] * v1 + Bj[5 * S] * v2;
+        y2 += Bj[6 * S] * v0 + Bj[7 * S] * v1 + Bj[8 * S] * v2;
+      }
     }
     T y[3] = {y0, y1, y2};
 #pragma unroll

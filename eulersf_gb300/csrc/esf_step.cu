@@ -15,6 +15,7 @@
 #include <string>
 #include <vector>
 
+#include "esf_io.h"
 #include "esf_kernels.cuh"
 
 namespace esf {
@@ -1298,15 +1299,118 @@ extern "C" esf_status esf_pressure_solve_static(const esf_grid* g, const double*
   return e;
 }
 
+// COUPLED_INTEGRATOR_3D::writeFrame (COUPLED_INTEGRATOR_3D.cpp:997-1012) with
+// DEFOR_SOLID_3D::writeFrame (DEFOR_SOLID_3D.cpp:1362-1370): per solid i
+// "frame.NNNN.solid.i" + .displacement/.velocity/.phi (every 10th frame or
+// debug) and .obj (always); the fluid .velocity (every 10th frame or debug)
+// and .intensity (always). The .pbrt render export is not written.
 extern "C" esf_status esf_write_frame(esf_scene* s, const char* path, int frame, int debug) {
-  (void)s; (void)path; (void)frame; (void)debug;
-  set_error("esf_write_frame: frame I/O is not implemented yet");
-  return ESF_ERR_UNSUPPORTED;
+  if (!s || !path) {
+    set_error("esf_write_frame: invalid argument");
+    return ESF_ERR_INVALID_ARG;
+  }
+  if (!s->inited) {
+    set_error("esf_write_frame: scene not initialised");
+    return ESF_ERR_STATE;
+  }
+  const GridDev& G = s->g;
+  const int res[3] = {G.X, G.Y, G.Z};
+  const bool full = debug || (frame % 10 == 0);
+  const std::string base = frame_prefix(path, frame);
+  std::vector<double> buf((size_t)G.T * 3);
+  for (int i = 0; i < s->ns; i++) {
+    Solid* d = s->s[i];
+    const std::string fn = base + ".solid." + std::to_string(i);
+    if (full) {
+      TRY(esf_get_field(s, ESF_F_S_U, i, buf.data(), G.T * 24));
+      TRY(write_field_gz(fn + ".displacement", res, G.dh, G.o, buf.data(), G.T * 3));
+      TRY(esf_get_field(s, ESF_F_S_VELOCITY, i, buf.data(), G.T * 24));
+      TRY(write_field_gz(fn + ".velocity", res, G.dh, G.o, buf.data(), G.T * 3));
+      TRY(esf_get_field(s, ESF_F_S_PHI, i, buf.data(), G.T * 8));
+      TRY(write_field_gz(fn + ".phi", res, G.dh, G.o, buf.data(), G.T));
+    }
+    std::vector<double> v((size_t)d->nv * 3);
+    TRY(esf_get_field(s, ESF_F_S_MESH_VERTICES, i, v.data(), v.size() * 8));
+    TRY(write_obj(fn + ".obj", v.data(), d->nv, d->tris.data(), d->ntri));
+  }
+  if (full) {
+    TRY(esf_get_field(s, ESF_F_VELOCITY, 0, buf.data(), G.T * 24));
+    TRY(write_field_gz(base + ".velocity", res, G.dh, G.o, buf.data(), G.T * 3));
+  }
+  TRY(esf_get_field(s, ESF_F_INTENSITY, 0, buf.data(), G.T * 8));
+  TRY(write_field_gz(base + ".intensity", res, G.dh, G.o, buf.data(), G.T));
+  return ESF_OK;
 }
+
+// COUPLED_INTEGRATOR_3D::readFrame (COUPLED_INTEGRATOR_3D.cpp:977-996) with
+// DEFOR_SOLID_3D::readFrame (DEFOR_SOLID_3D.cpp:1299-1361): the fields above,
+// then per solid X from u, the mesh from its OBJ, the boxes from the mesh's
+// vertex bounds, computeSolidMass(true) and initMaterialParticles; then
+// gatherSolidMasses and recoverVelocityField. Like the reference, the
+// pressure warm start and dt are not part of a frame.
 extern "C" esf_status esf_read_frame(esf_scene* s, const char* path, int frame, int debug) {
-  (void)s; (void)path; (void)frame; (void)debug;
-  set_error("esf_read_frame: frame I/O is not implemented yet");
-  return ESF_ERR_UNSUPPORTED;
+  if (!s || !path) {
+    set_error("esf_read_frame: invalid argument");
+    return ESF_ERR_INVALID_ARG;
+  }
+  if (!s->inited) {
+    set_error("esf_read_frame: scene not initialised");
+    return ESF_ERR_STATE;
+  }
+  cudaSetDevice(s->device);
+  const GridDev& G = s->g;
+  cudaStream_t st = s->stream;
+  const int res[3] = {G.X, G.Y, G.Z};
+  const bool full = debug || (frame % 10 == 0);
+  const std::string base = frame_prefix(path, frame);
+  std::vector<double> buf((size_t)G.T * 3);
+  for (int i = 0; i < s->ns; i++) {
+    Solid* d = s->s[i];
+    const std::string fn = base + ".solid." + std::to_string(i);
+    if (full) {
+      TRY(read_field_gz(fn + ".displacement", res, G.T * 3, buf.data()));
+      TRY(esf_set_field(s, ESF_F_S_U, i, buf.data(), G.T * 24));
+      TRY(read_field_gz(fn + ".velocity", res, G.T * 3, buf.data()));
+      TRY(esf_set_field(s, ESF_F_S_VELOCITY, i, buf.data(), G.T * 24));
+      TRY(read_field_gz(fn + ".phi", res, G.T, buf.data()));
+      TRY(esf_set_field(s, ESF_F_S_PHI, i, buf.data(), G.T * 8));
+    }
+    ESF_COUNTED k_frame_X<<<kblocks(G.T), KT, 0, st>>>(G, d->d);
+    ESF_LAUNCH_CHECK();
+    std::vector<double> v((size_t)d->nv * 3);
+    TRY(read_obj_vertices(fn + ".obj", d->nv, v.data()));
+    ESF_CUDA(cudaMemcpyAsync(d->dVerts, v.data(), v.size() * 8, cudaMemcpyHostToDevice, st));
+    double mn[3] = {1e9, 1e9, 1e9}, mx[3] = {-1e9, -1e9, -1e9};
+    for (int k = 0; k < d->nv; k++)
+      for (int q = 0; q < 3; q++) {
+        mn[q] = std::min(mn[q], v[3 * k + q]);
+        mx[q] = std::max(mx[q], v[3 * k + q]);
+      }
+    int lo[3], hi[3];
+    for (int q = 0; q < 3; q++) {
+      lo[q] = (int)((mn[q] - G.o[q]) / G.dh);
+      hi[q] = (int)((mx[q] - G.o[q]) / G.dh);
+    }
+    const int tb = s->p.tight_border, exn = s->p.extrapolation_cells;
+    for (int q = 0; q < 3; q++) {
+      d->tmin[q] = std::max(lo[q] - tb, 0);
+      d->tmax[q] = std::min(hi[q] + tb, res[q]);
+      d->ex[q] = std::max(lo[q] - exn, 0);
+      d->ex[3 + q] = std::min(hi[q] + exn, res[q]);
+    }
+    TRY(compute_solid_mass(s, d, 1));
+    TRY(init_particles(s, d));
+  }
+  if (full) {
+    TRY(read_field_gz(base + ".velocity", res, G.T * 3, buf.data()));
+    TRY(esf_set_field(s, ESF_F_VELOCITY, 0, buf.data(), G.T * 24));
+  }
+  TRY(read_field_gz(base + ".intensity", res, G.T, buf.data()));
+  TRY(esf_set_field(s, ESF_F_INTENSITY, 0, buf.data(), G.T * 8));
+  TRY(gather_solid_masses(s));
+  TRY(recover_velocity(s));
+  ESF_CUDA(cudaStreamSynchronize(st));
+  return ESF_OK;
 }
 
 extern "C" esf_status esf_time_pressure_kernels(esf_scene* s, int reps, double* update_ms,

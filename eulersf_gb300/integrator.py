@@ -109,6 +109,14 @@ class CoupledIntegrator3D:
     def dt(self) -> float:
         return getattr(self._lib, self._p + "dt")(self._h)
 
+    def writeFrame(self, frame: int, debug: bool = False, data_path: str = ""):
+        """COUPLED_INTEGRATOR_3D::writeFrame: files "<data_path>frame.NNNN.*"."""
+        self._call("write_frame", self._h, data_path.encode(), int(frame), int(bool(debug)))
+
+    def readFrame(self, frame: int, debug: bool = False, data_path: str = ""):
+        """COUPLED_INTEGRATOR_3D::readFrame of files written by writeFrame (or the reference)."""
+        self._call("read_frame", self._h, data_path.encode(), int(frame), int(bool(debug)))
+
     # ------------------------------------------------------------ fields
     def field_info(self, name, solid=0):
         fid, dtype, comp = abi.FIELDS[name]

@@ -271,7 +271,17 @@ uint64_t esf_kernel_launches(void);
 esf_status esf_time_pressure_kernels(esf_scene* scene, int reps, double* update_ms,
                                      double* axpy_ms);
 
-/* ---- checkpoint (COUPLED_INTEGRATOR_3D::writeFrame/readFrame :977-1012) --- */
+/* ---- frames (COUPLED_INTEGRATOR_3D::writeFrame/readFrame,
+ * COUPLED_INTEGRATOR_3D.cpp:977-1012; DEFOR_SOLID_3D.cpp:1299-1370) -------
+ * Files "<data_path>frame.NNNN.velocity|.intensity" and, per solid i,
+ * "...solid.i.displacement|.velocity|.phi|.obj", in the reference's gz and
+ * OBJ formats, so frames move between the reference and this library. The
+ * gz fields (and the fluid velocity) are written and read only when
+ * frame % 10 == 0 or debug != 0, as in the reference; the .pbrt render
+ * export is not written. Reading recomputes X, the boxes, the solid mass and
+ * the particles the way readFrame does; the scene's grid must match the
+ * files'. Needs zlib (libz.so.1) at run time: ESF_ERR_UNSUPPORTED without it,
+ * ESF_ERR_IO on a missing or mismatched file. */
 esf_status esf_write_frame(esf_scene* scene, const char* data_path, int frame, int debug);
 esf_status esf_read_frame(esf_scene* scene, const char* data_path, int frame, int debug);
 

@@ -82,6 +82,14 @@ class CoupledIntegrator3D {
     return r.energy;
   }
   double dt() const { return esf_dt(scene_); }
+  // COUPLED_INTEGRATOR_3D::writeFrame/readFrame; dataPath is the cfg's
+  // "data path" (prefix of "frame.NNNN.*")
+  void writeFrame(int frame, bool debug = false, const std::string& dataPath = "") {
+    check(esf_write_frame(scene_, dataPath.c_str(), frame, debug ? 1 : 0), "esf_write_frame");
+  }
+  void readFrame(int frame, bool debug = false, const std::string& dataPath = "") {
+    check(esf_read_frame(scene_, dataPath.c_str(), frame, debug ? 1 : 0), "esf_read_frame");
+  }
 
   // FIELD_3Df& intensity() of the reference, as a host copy
   std::vector<double> intensity() { return get<double>(ESF_F_INTENSITY); }
