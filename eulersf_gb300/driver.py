@@ -4,7 +4,9 @@ keys, loads each solid's ``<path><name>.mass`` (FIELD_3D gz layout) and
 ``<path><name>.obj``, sets up the integrator in the order of
 APPLICATION::init/addSolids, seeds the smoke carpet, and runs frames with
 APPLICATION::step's substep loop on the GPU. Instead of GLUT windows it
-prints one JSON line per substep.
+prints one JSON line per substep. With "save data = true" it writes each
+frame's files under "data path" (main.cpp:198-199); a "start frame" above 0
+resumes from the previous frame's files (main.cpp:95).
 
     python -m eulersf_gb300.driver scene.cfg [frames] [--mixed]
 """
@@ -97,12 +99,24 @@ def run(cfg_path, frames=None, precision=abi.ESF_FP64, out=sys.stdout):
     end = int(float(cfg.get("end frame", 100)))
     nframes = frames if frames is not None else end - start
     frame_dt = float(cfg.get("dt", 0.005))
+    data_path = cfg.get("data path", "")
+    save = cfg.get("save data", "false") in ("1", "true")
+    debug = cfg.get("debug", "false") in ("1", "true")
+    # main.cpp:95: resume from the previous frame's files
+    if start > 0:
+        I.readFrame(start - 1, debug, data_path)
 
-    def report(k, r):
-        out.write(json.dumps({"substep": k, **r}) + "\n")
-        out.flush()
+    reports = []
+    for f in range(start, start + nframes):
+        def report(k, r, f=f):
+            r["frame"] = f
+            reports.append(r)
+            out.write(json.dumps({"substep": len(reports), **r}) + "\n")
+            out.flush()
 
-    reports = run_frames(I, nframes, frame_dt, on_step=report)
+        run_frames(I, 1, frame_dt, on_step=report)
+        if save:  # main.cpp:198-199
+            I.writeFrame(f, debug, data_path)
     I.close()
     return reports
 

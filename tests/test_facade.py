@@ -120,3 +120,26 @@ def test_cfg_driver_first_substep(tmp_path, gpu_lib):
     assert abs(first["energy"] - r0["energy"]) <= 1e-9 * abs(r0["energy"])
     assert first["dt"] == r0["dt"]
     G.close()
+
+
+@pytest.mark.gpu
+def test_cfg_driver_saves_and_resumes_frames(tmp_path, gpu_lib):
+    """"save data" writes each frame's files under "data path"
+    (main.cpp:198-199); "start frame = 1" resumes from frame 0's files
+    (main.cpp:95) and keeps stepping."""
+    import io
+    from eulersf_gb300 import driver
+    cfg = write_scene(DESC, str(tmp_path / "scene"))
+    data = str(tmp_path / "out") + "/"
+    os.makedirs(data)
+    with open(cfg, "a") as f:
+        f.write(f"save data = true\ndata path = {data}\n")
+    driver.run(cfg, frames=1, out=io.StringIO())
+    names = set(os.listdir(data))
+    assert {"frame.0000.velocity", "frame.0000.intensity", "frame.0000.solid.0.obj",
+            "frame.0000.solid.0.displacement"} <= names
+    with open(cfg, "a") as f:
+        f.write("start frame = 1\n")
+    reports = driver.run(cfg, frames=1, out=io.StringIO())
+    assert reports and reports[0]["frame"] == 1 and all(r["status"] == 0 for r in reports)
+    assert "frame.0001.intensity" in set(os.listdir(data))
