@@ -658,13 +658,20 @@ static esf_status prepare_tma(PressureWork* w, const GridDev& g, const double* m
       g, minv64, w->minv32p, w->mpitch);
   ESF_LAUNCH_CHECK();
   if (!w->tmaOk) {
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        pressure_update_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, TW_SMEM);
+    if (attr != cudaSuccess) {
+      set_error("pressure_update_tma: %d bytes of shared memory refused: %s", TW_SMEM,
+                cudaGetErrorString(attr));
+      return ESF_ERR_CUDA;
+    }
     TmaMaps m;
     esf_status e;
     if ((e = encode3d(&m.r, w->r32, g.cX, g.cY, g.cZ, TMA_HW, TMA_HH))) return e;
     if ((e = encode3d(&m.ap, w->Ap32, g.cX, g.cY, g.cZ, TMA_HW, TMA_HH))) return e;
     if ((e = encode3d(&m.iv, w->invd32, g.cX, g.cY, g.cZ, TMA_HW, TMA_HH))) return e;
-    if ((e = encode3d(&m.x, w->x32, g.cX, g.cY, g.cZ, TX, TY))) return e;
-    if ((e = encode3d(&m.d, w->d32, g.cX, g.cY, g.cZ, TX, TY))) return e;
+    if ((e = encode3d(&m.x, w->x32, g.cX, g.cY, g.cZ, TXW, TY))) return e;
+    if ((e = encode3d(&m.d, w->d32, g.cX, g.cY, g.cZ, TXW, TY))) return e;
     if ((e = encode3d(&m.m, w->minv32p, w->mpitch, g.Y, g.Z, TMA_NW, TMA_NH))) return e;
     w->tmaps = m;
     w->tmaOk = true;
@@ -700,8 +707,9 @@ struct PressureKernels {
   void update(cudaStream_t cs) const {
     if constexpr (std::is_same<T, float>::value) {
       if (tma) {
-        ESF_COUNTED pressure_update_tma<<<stencil_grid<T>(g), NT, 0, cs>>>(g, *tma, x, s, partial, st,
-                                                                        stencil_cz(g));
+        const int cz = stencil_cz(g);
+        ESF_COUNTED pressure_update_tma<<<tma_grid(g, cz), NT, TW_SMEM, cs>>>(g, *tma, x, s, partial, st,
+                                                                           cz);
         return;
       }
     }
