@@ -24,7 +24,9 @@ EXPORTS = [
     "esf_destroy", "esf_add_solid", "esf_set_fluid", "esf_init", "esf_set_max_dt", "esf_step",
     "esf_dt", "esf_field_info", "esf_get_field", "esf_set_field", "esf_pressure_apply",
     "esf_pressure_solve", "esf_pressure_solve_static", "esf_write_frame", "esf_read_frame", "esf_kernel_launches",
-    "esf_time_pressure_kernels",
+    "esf_time_pressure_kernels", "esf_scene_footprint", "esf_server_create", "esf_server_submit",
+    "esf_server_poll", "esf_server_wait", "esf_server_get_field", "esf_server_release",
+    "esf_server_destroy",
 ]
 
 
@@ -58,6 +60,8 @@ def load(build_if_missing: bool = False) -> C.CDLL:
     lib.esf_time_pressure_kernels.argtypes = [vp, C.c_int, C.POINTER(C.c_double),
                                               C.POINTER(C.c_double)]
     lib.esf_write_frame.argtypes = [vp, C.c_char_p, C.c_int, C.c_int]
+    from . import serve as _serve
+    _serve.declare(lib)
     lib.esf_read_frame.argtypes = [vp, C.c_char_p, C.c_int, C.c_int]
     _lib = lib
     return lib

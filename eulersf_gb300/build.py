@@ -6,6 +6,7 @@ Three translation units, compiled in parallel:
                  and particle seeding keep the reference's non-FMA arithmetic
   esf_config.cpp the cfg reader
   esf_io.cpp     frame files (gz fields, OBJ); zlib is loaded at run time
+  esf_serve.cpp  the multi-scene server (host threads, one stream per scene)
 Host code is compiled with -ffp-contract=off for the same reason (the box's
 aarch64 compiler would otherwise contract a*b+c).
 """
@@ -37,6 +38,7 @@ def _sources():
         "esf_step.cu": ["-O3", "-lineinfo", "-fmad=false"],
         "esf_config.cpp": ["-O2"],
         "esf_io.cpp": ["-O2"],
+        "esf_serve.cpp": ["-O2"],
     }
 
 
@@ -72,10 +74,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
             sys.stderr.write(r.stderr)
         return obj
 
-    with cf.ThreadPoolExecutor(max_workers=4) as ex:
+    with cf.ThreadPoolExecutor(max_workers=5) as ex:
         objs = list(ex.map(one, _sources().items()))
     tmp = LIB + f".tmp{os.getpid()}"
-    cmd = [nvcc, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart", "-ldl"]
+    cmd = [nvcc, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart", "-ldl", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     for o in objs:
         try:

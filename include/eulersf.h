@@ -260,6 +260,63 @@ esf_status esf_pressure_solve_static(const esf_grid* grid, const double* mass_in
                                      double eps, int max_iterations, int* iterations,
                                      double* rel_residual, void* stream);
 
+/* ---- serving: many scenes on one GPU -------------------------------------
+ * No reference counterpart: the reference runs one scene per process (its
+ * function-local statics pin one grid size per process). Requests arrive at
+ * any time; a request is admitted when its estimated footprint
+ * (esf_scene_footprint) fits what is left of the memory budget and one of
+ * max_active slots is free, taking the first request in arrival order that
+ * fits. Each admitted scene runs on its own CUDA stream and host thread, so
+ * requests that arrive while others run overlap with them on the device.
+ * Results stay readable (esf_server_get_field) until esf_server_release,
+ * which returns the request's memory to the budget. */
+typedef struct esf_server esf_server;
+typedef struct esf_server_config {
+  size_t hbm_budget_bytes; /* admission budget; 0: 85% of the device's free memory */
+  int max_active;          /* scenes stepping at once; 0: 8 */
+} esf_server_config;
+typedef struct esf_request {
+  esf_grid grid;
+  esf_params params;
+  int num_solids;
+  const esf_solid_desc* solids;  /* copied at submit, with their arrays */
+  double fluid_density, fluid_viscosity;
+  double smoke_carpet;           /* "smoke carpet thickness" (intensity 0.8 below it); 0: none */
+  unsigned long long noise_seed; /* fluid noise U(-a, a) per component at interior nodes */
+  double noise_amplitude;        /* without solid mass, added after init; 0: none */
+  int steps;                     /* stepImplicit calls */
+} esf_request;
+typedef enum esf_request_state {
+  ESF_REQ_QUEUED = 0,
+  ESF_REQ_RUNNING = 1,
+  ESF_REQ_DONE = 2,
+  ESF_REQ_FAILED = 3
+} esf_request_state;
+typedef struct esf_request_status {
+  int state;               /* esf_request_state */
+  int steps_done;
+  esf_status status;       /* ESF_ERR_NUMERIC from a step, or the failure */
+  double queued_ms;        /* submit -> admitted */
+  double latency_ms;       /* submit -> last step done */
+  double device_ms;        /* sum of the steps' device time */
+  size_t footprint_bytes;  /* admission estimate */
+  esf_step_report last;    /* report of the last step */
+} esf_request_status;
+/* admission estimate of a scene's device memory (fields, solvers, particles) */
+size_t esf_scene_footprint(const esf_grid* grid, const esf_params* params, int num_solids,
+                           const esf_solid_desc* solids);
+esf_status esf_server_create(const esf_server_config* config, esf_server** server);
+/* ESF_ERR_OOM if the request alone exceeds the budget */
+esf_status esf_server_submit(esf_server* server, const esf_request* request, uint64_t* ticket);
+esf_status esf_server_poll(esf_server* server, uint64_t ticket, esf_request_status* status);
+/* blocks until the request is done or failed */
+esf_status esf_server_wait(esf_server* server, uint64_t ticket, esf_request_status* status);
+esf_status esf_server_get_field(esf_server* server, uint64_t ticket, esf_field field, int solid,
+                                void* host, size_t bytes);
+esf_status esf_server_release(esf_server* server, uint64_t ticket);
+/* lets running requests finish their steps, drops queued ones */
+esf_status esf_server_destroy(esf_server* server);
+
 /* ---- instrumentation (no reference counterpart beyond TIMING_BREAKDOWN) -- */
 /* Number of kernels this library has launched in this process (graph
  * replays count every kernel node). */

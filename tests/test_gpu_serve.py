@@ -1,0 +1,61 @@
+"""The multi-scene server (esf_server_*): each request's result is the same,
+bit for bit, whether it runs alone or concurrently with others; admission
+holds a request back until the memory budget has room; a request larger
+than the budget is refused."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from eulersf_gb300 import abi
+from eulersf_gb300.scene import SceneDesc
+
+pytestmark = pytest.mark.gpu
+
+
+def _descs():
+    return [SceneDesc(N=16, mass_sample_dh=(1.0 / 16) / 4, noise_seed=1),
+            SceneDesc(N=20, mass_sample_dh=(1.0 / 20) / 4, noise_seed=2),
+            SceneDesc(N=16, mass_sample_dh=(1.0 / 16) / 4, noise_seed=3, fluid_height=0.25)]
+
+
+def test_concurrent_requests_equal_solo_runs(gpu_lib):
+    import eulersf_gb300 as E
+    from eulersf_gb300.serve import ESF_REQ_DONE, Server
+    descs, steps = _descs(), 2
+    with Server(max_active=3) as srv:
+        tickets = [srv.submit(d, steps, abi.ESF_MIXED) for d in descs]
+        got = []
+        for d, t in zip(descs, tickets):
+            st = srv.wait(t)
+            assert st["state"] == ESF_REQ_DONE and st["steps_done"] == steps, st
+            got.append((srv.get(t, "velocity", d.res ** 3 * 3), srv.get(t, "lambda1", d.N ** 3),
+                         st["last"]["iterations"]))
+            srv.release(t)
+    for d, (vel, lam, its) in zip(descs, got):
+        G = E.make_scene(d, precision=abi.ESF_MIXED)
+        for _ in range(steps):
+            r = G.stepImplicit()
+        assert its == r["iterations"]
+        assert np.array_equal(vel, G.get("velocity")), d
+        assert np.array_equal(lam, G.get("lambda1")), d
+        G.close()
+
+
+def test_admission_waits_for_budget_and_refuses_oversize(gpu_lib):
+    from eulersf_gb300.serve import Server, request_for
+    d = _descs()[0]
+    q, keep = request_for(d, 1)
+    one = gpu_lib.esf_scene_footprint(C.byref(q.grid), C.byref(q.params), q.num_solids, q.solids)
+    assert one > 0
+    with Server(hbm_budget_bytes=int(one * 1.5), max_active=4) as srv:
+        a, b = srv.submit(d, 1), srv.submit(d, 1)
+        sa = srv.wait(a)
+        assert srv.poll(b)["state"] == 0  # still queued: a holds the budget until released
+        srv.release(a)
+        sb = srv.wait(b)
+        assert sb["state"] == 2 and sb["queued_ms"] >= sa["latency_ms"]
+        srv.release(b)
+        with pytest.raises(abi.EsfError) as e:
+            srv.submit(SceneDesc(N=64), 1)
+        assert e.value.status == 4  # ESF_ERR_OOM

@@ -109,3 +109,25 @@ def test_rest_mass_and_mesh(tmp_path):
 def test_lame():
     lam, mu = scene.lame(2e5, 0.45)
     assert lam == pytest.approx(620689.6551724138) and mu == pytest.approx(68965.51724137931)
+
+
+def test_server_without_gpu_and_footprint_model(lib):
+    """The server needs a device (a clean status without one); the admission
+    estimate is host arithmetic and grows with the grid."""
+    import ctypes as C
+    from eulersf_gb300.scene import SceneDesc
+    from eulersf_gb300.serve import ServerConfig, request_for
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except ImportError:
+        has_gpu = False
+    if not has_gpu:
+        h = C.c_void_p()
+        assert lib.esf_server_create(C.byref(ServerConfig(0, 2)), C.byref(h)) == 7
+        assert b"device" in lib.esf_last_error()
+    sizes = []
+    for n in (32, 64):
+        q, keep = request_for(SceneDesc(N=n), 1)
+        sizes.append(lib.esf_scene_footprint(C.byref(q.grid), C.byref(q.params), q.num_solids, q.solids))
+    assert 0 < sizes[0] < sizes[1] and sizes[1] > 2 * sizes[0]
