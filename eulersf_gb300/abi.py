@@ -50,6 +50,7 @@ class SolidDesc(C.Structure):
         ("scaling", C.c_double * 3), ("initial_velocity", C.c_double * 3),
         ("num_vertices", C.c_int), ("vertices", C.POINTER(C.c_double)),
         ("num_triangles", C.c_int), ("triangles", C.POINTER(C.c_int)),
+        ("plastic_yield", C.c_double),
     ]
 
 
@@ -98,6 +99,7 @@ FIELDS = {
     "solid.quarterVolumeFractions": (58, np.float64, 1),
     "solid.particles": (59, np.float64, 10), "solid.meshVertices": (60, np.float64, 3),
     "solid.boxes": (61, np.int32, 1),
+    "solid.FpInv": (62, np.float64, 9), "solid.FpInvGrid": (63, np.float64, 1),
 }
 
 

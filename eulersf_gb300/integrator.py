@@ -145,7 +145,7 @@ class CoupledIntegrator3D:
         return self.get("intensity")
 
 
-def make_solid_desc(radius, center, density, E, nu, velocity=(0, 0, 0)):
+def make_solid_desc(radius, center, density, E, nu, velocity=(0, 0, 0), plastic_yield=-1.0):
     """Solid descriptor for the synthetic sphere (rest assets from scene.py)."""
     (res, mdh, morig, mdata), verts, faces = solid_assets(radius)
     lam, mu = lame(E, nu)
@@ -166,6 +166,7 @@ def make_solid_desc(radius, center, density, E, nu, velocity=(0, 0, 0)):
     d.vertices = v.ctypes.data_as(C.POINTER(C.c_double))
     d.num_triangles = len(faces)
     d.triangles = t.ctypes.data_as(C.POINTER(C.c_int))
+    d.plastic_yield = float(plastic_yield)
     return d, (rest, v, t)
 
 
@@ -191,7 +192,7 @@ def params_from_desc(desc: SceneDesc, precision: int = abi.ESF_FP64) -> abi.Para
     p.contact_spring_stiffness = 10000.0
     p.friction = 0.5
     p.flip_cutoff = 3
-    p.flow_rate = 0.5
+    p.flow_rate = desc.flow_rate
     p.precision = precision
     p.inner_eps = desc.inner_eps
     p.max_refinements = 50
@@ -207,7 +208,8 @@ def build_from_scene(lib, prefix, desc: SceneDesc, precision=abi.ESF_FP64, noise
     I = CoupledIntegrator3D(lib, prefix, res, res, res, desc.dh, (0.0, 0.0, 0.0),
                             params_from_desc(desc, precision), stream=stream)
     for s in desc.solids:
-        d, keep = make_solid_desc(s.radius, s.center, s.density, s.E, s.nu, s.velocity)
+        d, keep = make_solid_desc(s.radius, s.center, s.density, s.E, s.nu, s.velocity,
+                                  s.plastic_yield)
         I.addSolid(d, keep)
     I.setFluidDensity(desc.fluid_density)
     I.setFluidViscocity(0.0)

@@ -64,6 +64,7 @@ class SolidDesc:
     E: float = 2e5
     nu: float = 0.45
     velocity: tuple = (0.0, 0.0, 0.0)
+    plastic_yield: float = -1.0  # "solid plastic yield i"; <= 0: elastic
 
 
 @dataclass
@@ -87,6 +88,7 @@ class SceneDesc:
     noise_amplitude: float = 1e-3
     noise_seed: int = 0
     inner_eps: float = 1e-4  # mixed precision: FP32 inner relative tolerance
+    flow_rate: float = 0.5   # "flow rate" of the plastic update
 
     @property
     def res(self) -> int:
@@ -117,7 +119,7 @@ class SceneDesc:
             "implicit solver eps": self.eps, "div free solver eps": self.eps,
             "number of particles per material cell": self.particles_per_cell,
             "mass sample dh": self.mass_sample_dh, "flip cutoff": 3,
-            "flow rate": 0.5,
+            "flow rate": self.flow_rate,
         }
         for i, s in enumerate(self.solids):
             lam, mu = lame(s.E, s.nu)
@@ -126,7 +128,7 @@ class SceneDesc:
                 f"solid path {i}": solid_dir, f"solid name {i}": f"{solid_name}{i}",
                 f"solid mass density {i}": s.density,
                 f"material lambda {i}": lam, f"material mu {i}": mu,
-                f"solid plastic yield {i}": -1.0,
+                f"solid plastic yield {i}": s.plastic_yield,
                 f"solid initial velocity {i}": tuple(s.velocity),
                 f"solid translation {i}": tuple(s.center),
                 f"solid scaling {i}": (sc, sc, sc),

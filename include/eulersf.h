@@ -103,6 +103,7 @@ typedef struct esf_solid_desc {
   const double* vertices;     /* num_vertices x 3, rest pose */
   int num_triangles;
   const int* triangles;       /* num_triangles x 3, 0-based */
+  double plastic_yield;       /* "solid plastic yield i" (setPlasticYield); <= 0: elastic */
 } esf_solid_desc;
 
 /* What one stepImplicit() call did (COUPLED_INTEGRATOR_3D.cpp:377-636). */
@@ -166,7 +167,9 @@ typedef enum esf_field {
   ESF_F_S_QUARTER_FRACTIONS = 58, /* f64 8 per node */
   ESF_F_S_PARTICLES = 59,      /* f64 10 per particle: pos, velocity, restPos, mass */
   ESF_F_S_MESH_VERTICES = 60,  /* f64 x3 per vertex (current pose) */
-  ESF_F_S_BOXES = 61           /* i32 12: xmin..zmax, tightMin, tightMax */
+  ESF_F_S_BOXES = 61,          /* i32 12: xmin..zmax, tightMin, tightMax */
+  ESF_F_S_FPINV = 62,          /* f64 9 per material cell (row-major 3x3): _FpInv, plastic solids */
+  ESF_F_S_FPINV_GRID = 63      /* f64 7: material grid xRes, yRes, zRes, dh, origin (plastic) */
 } esf_field;
 
 typedef struct esf_scene esf_scene;

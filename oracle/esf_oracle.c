@@ -376,6 +376,15 @@ typedef struct {
   double* part; /* 10 per particle: pos, vel, rest, mass */
   double safeMin[3], safeMax[3];
   double G[8][3];
+  /* plasticity (setPlasticYield, DEFOR_SOLID_3D.h:55-58; material grid of
+   * loadSurfaceMesh, DEFOR_SOLID_3D.cpp:175-186) */
+  int plastic;
+  double yield;
+  int pres[3];
+  double pdh, porig[3];
+  double *FpInv, *FpNew; /* 9 per material cell, row-major */
+  double pgrid[7];       /* xRes, yRes, zRes, dh, origin */
+  signed char* fpSet;
 } solid_t;
 
 struct esfo_scene {
@@ -507,6 +516,7 @@ static void free_solid(solid_t* d) {
   free(d->rest); free(d->restPose); free(d->verts); free(d->tris);
   free(d->X); free(d->u); free(d->vel); free(d->vws); free(d->mass); free(d->phi);
   free(d->detFInv); free(d->quarter); free(d->tmp3); free(d->valid); free(d->part);
+  free(d->FpInv); free(d->FpNew); free(d->fpSet);
   free(d);
 }
 
@@ -693,6 +703,34 @@ int esfo_add_solid(esfo_scene* s, const esf_solid_desc* dd) {
     for (int i = 0; i < 3; i++)
       q[i] = (d->rot[i * 3 + 0] * p[0] + d->rot[i * 3 + 1] * p[1]) + d->rot[i * 3 + 2] * p[2];
     for (int k = 0; k < 3; k++) d->verts[3 * v + k] = q[k] + d->trans[k];
+  }
+  /* the inverse plastic deformation gradient lives on a grid of half the
+   * cell size over the rest mesh's box grown by one cell
+   * (DEFOR_SOLID_3D.cpp:158-186), identity at the start */
+  if (dd->plastic_yield > 0) {
+    d->plastic = 1;
+    d->yield = dd->plastic_yield;
+    double bmin[3] = {1e9, 1e9, 1e9}, bmax[3] = {-1e9, -1e9, -1e9};
+    for (int v = 0; v < d->nv; v++)
+      for (int k = 0; k < 3; k++) {
+        bmin[k] = fmin(bmin[k], d->restPose[3 * v + k]);
+        bmax[k] = fmax(bmax[k], d->restPose[3 * v + k]);
+      }
+    d->pdh = s->dh * .5;
+    for (int k = 0; k < 3; k++) {
+      bmin[k] -= s->dh;
+      bmax[k] += s->dh;
+      d->pres[k] = (int)((bmax[k] - bmin[k]) / d->pdh + 1);
+      d->porig[k] = bmin[k];
+    }
+    long pn = (long)d->pres[0] * d->pres[1] * d->pres[2];
+    d->FpInv = xcalloc(pn * 9, 8);
+    d->FpNew = xcalloc(pn * 9, 8);
+    d->fpSet = xcalloc(pn, 1);
+    for (long c = 0; c < pn; c++)
+      for (int i = 0; i < 3; i++) d->FpInv[c * 9 + i * 4] = 1.0;
+    double hdr[7] = {d->pres[0], d->pres[1], d->pres[2], d->pdh, d->porig[0], d->porig[1], d->porig[2]};
+    memcpy(d->pgrid, hdr, sizeof hdr);
   }
   /* _G (DEFOR_SOLID_3D.cpp:304-310) */
   for (int i = 0; i < 8; i++) {
@@ -1311,11 +1349,44 @@ static void tpush(tripvec* v, int r, int c, double x) {
   v->n++;
 }
 
+/* ||A|| of a 3x3 matrix (Eigen's norm()): the squares in column-major order
+ * summed as two-lane packets ((a0,a1)+(a2,a3)) + ((a4,a5)+(a6,a7)), the lanes
+ * added, then the ninth square. */
+static double m3_norm(const m3* a) {
+  double q[9];
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++) q[j * 3 + i] = a->m[i][j] * a->m[i][j];
+  double l0 = (q[0] + q[2]) + (q[4] + q[6]);
+  double l1 = (q[1] + q[3]) + (q[5] + q[7]);
+  return sqrt((l0 + l1) + q[8]);
+}
+/* MATRIX3_FIELD_3D::interpolate_value (MATRIX3_FIELD_3D.h:127-135): the
+ * material cell holding a rest position, clamped to the grid. */
+static long fp_index(const solid_t* d, const double p[3]) {
+  int c[3];
+  for (int k = 0; k < 3; k++) {
+    double x = (p[k] - d->porig[k]) / d->pdh;
+    int i = (int)floor(x);
+    if (i <= 0) i = 0;
+    else if (i >= d->pres[k] - 1) i = d->pres[k] - 1;
+    c[k] = i;
+  }
+  return ((long)c[2] * d->pres[1] + c[1]) * d->pres[0] + c[0];
+}
+static m3 fp_get(const double* f, long c) {
+  m3 r;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) r.m[i][j] = f[c * 9 + i * 3 + j];
+  return r;
+}
+
 /* computeStiffnessMatrixAndMaterialForce (DEFOR_SOLID_3D.cpp:697-871) for
  * an elastic solid, and computePFPxhat (:684-695) folded in. */
 static double stiffness(esfo_scene* s, solid_t* d, double* force, tripvec* tl, const int* map) {
   const long off[8] = {0, 1, s->X, s->X + 1, s->slab, s->slab + 1, s->slab + s->X,
                        s->slab + s->X + 1};
+  const long pn = d->plastic ? (long)d->pres[0] * d->pres[1] * d->pres[2] : 0;
+  if (pn) memset(d->fpSet, 0, pn);
   const double dh = s->dh;
   double energy = 0;
   corot mat;
@@ -1337,6 +1408,42 @@ static double stiffness(esfo_scene* s, solid_t* d, double* force, tripvec* tl, c
         for (int i = 0; i < 3; i++)
           for (int j = 0; j < 3; j++) JP.m[i][j] = Jinv * P.m[i][j];
         m3 cs = m3_mul_bt(&JP, &F);
+        /* plasticity (DEFOR_SOLID_3D.cpp:765-791): above the yield stress the
+         * elastic part F FpInv is used, and FpInv is updated by a flow step
+         * on the singular values; the updates are written after the sweep,
+         * the last cell in sweep order winning for a material cell */
+        if (d->plastic && m3_norm(&cs) > d->yield) {
+          double rp[3] = {0, 0, 0};
+          for (int i = 0; i < 8; i++)
+            for (int k = 0; k < 3; k++) rp[k] += d->X[3 * (index + off[i]) + k];
+          for (int k = 0; k < 3; k++) rp[k] /= 8;
+          const long mc = fp_index(d, rp);
+          m3 Fp = fp_get(d->FpInv, mc);
+          F = m3_mul(&F, &Fp);
+          corot_init(&mat, &F);
+          P = corot_pk1(&mat);
+          for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) JP.m[i][j] = Jinv * P.m[i][j];
+          cs = m3_mul_bt(&JP, &F);
+          const double cNorm = m3_norm(&cs);
+          if (cNorm > d->yield) {
+            const double gamma = s->p.flow_rate * (cNorm - d->yield) / cNorm;
+            const double cr = cbrt(1.0 / fmax(fabs(Jinv), 1e-3));
+            m3 Fh = mat.Fhat;
+            for (int i = 0; i < 3; i++) Fh.m[i][i] = pow(Fh.m[i][i] / cr, -gamma);
+            m3 VF = m3_mul(&mat.V, &Fh);
+            m3 dFp = m3_mul_bt(&VF, &mat.V);
+            m3 nFp = m3_mul(&dFp, &Fp);
+            int bad = 0;
+            for (int i = 0; i < 3; i++)
+              for (int j = 0; j < 3; j++) bad |= nFp.m[i][j] != nFp.m[i][j];
+            if (!bad) {
+              for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) d->FpNew[mc * 9 + i * 3 + j] = nFp.m[i][j];
+              d->fpSet[mc] = 1;
+            }
+          }
+        }
         double GF[8][3]; /* _G * F */
         for (int i = 0; i < 8; i++)
           for (int j = 0; j < 3; j++)
@@ -1381,6 +1488,8 @@ static double stiffness(esfo_scene* s, solid_t* d, double* force, tripvec* tl, c
           }
         }
       }
+  for (long c = 0; c < pn; c++)
+    if (d->fpSet[c]) memcpy(d->FpInv + c * 9, d->FpNew + c * 9, 72);
   return energy;
 }
 
@@ -2141,6 +2250,16 @@ static int field_ptr(esfo_scene* s, int f, int si, void** p, size_t* count, size
     case ESF_F_S_QUARTER_FRACTIONS: *p = d->quarter; *count = T * 8; return 0;
     case ESF_F_S_PARTICLES: *p = d->part; *count = d->np * 10; return 0;
     case ESF_F_S_MESH_VERTICES: *p = d->verts; *count = d->nv * 3L; return 0;
+    case ESF_F_S_FPINV:
+      if (!d || !d->plastic) return ESF_ERR_INVALID_ARG;
+      *p = d->FpInv;
+      *count = 9L * d->pres[0] * d->pres[1] * d->pres[2];
+      return 0;
+    case ESF_F_S_FPINV_GRID:
+      if (!d || !d->plastic) return ESF_ERR_INVALID_ARG;
+      *p = d->pgrid;
+      *count = 7;
+      return 0;
     default: break;
   }
   return ESF_ERR_INVALID_ARG;

@@ -193,6 +193,18 @@ static void dump_state(Dumper& d, COUPLED_INTEGRATOR_3D* I, bool full) {
     for (size_t i = 0; i < verts.size(); i++)
       for (int k = 0; k < 3; k++) vv[i * 3 + k] = verts[i][k];
     ds.f64("meshVertices", vv.data(), vv.size(), {(long)verts.size(), 3});
+    if (S->_isPlastic) {
+      // inverse plastic deformation gradient on the material grid, row-major
+      const MATRIX3_FIELD_3D& F = S->_FpInv;
+      std::vector<double> fp((size_t)F._totalCells * 9);
+      for (int c = 0; c < F._totalCells; c++)
+        for (int i = 0; i < 3; i++)
+          for (int j = 0; j < 3; j++) fp[(size_t)c * 9 + i * 3 + j] = F._data[c](i, j);
+      ds.f64("FpInv", fp.data(), fp.size(), {(long)F._totalCells, 3, 3});
+      double hdr[7] = {(double)F._xRes, (double)F._yRes, (double)F._zRes, F._dh,
+                       F._origin[0], F._origin[1], F._origin[2]};
+      ds.f64("FpInvGrid", hdr, 7);
+    }
   }
 }
 
@@ -248,6 +260,9 @@ int main(int argc, char** argv) {
     solid->setMaterial(lambda, mu);
     solid->setMassDensity(
         SIMPLE_PARSER::getFloat("solid mass density " + index, 1));
+    Real plasticYield =
+        SIMPLE_PARSER::getFloat("solid plastic yield " + index, -1);
+    if (plasticYield > 0) solid->setPlasticYield(plasticYield);
     VEC3F translation =
         SIMPLE_PARSER::getVEC3F("solid translation " + index, VEC3F(0, 0, 0));
     VEC3F scaling =

@@ -15,7 +15,7 @@ for p in (ROOT, os.path.join(ROOT, "oracle")):
 
 from eulersf_gb300.scene import SceneDesc, SolidDesc  # noqa: E402
 
-GOLDEN_SCENES = ["ball16", "ball20_vort", "wall20"]
+GOLDEN_SCENES = ["ball16", "ball20_vort", "wall20", "plastic20"]
 
 # bit-exact integer/flag fields (the reference's DOF maps, cell flags, boxes)
 EXACT = ["gridIdxToSolutionIdx", "gridIdxToSolidIdx", "solid0.valid", "solid0.boxes"]
@@ -24,7 +24,7 @@ FLOAT = ["velocity", "intensity", "solidMass", "nodeSolidVolumeFraction", "lambd
          "solid0.mass", "solid0.phi", "solid0.u", "solid0.X", "solid0.velocity",
          "solid0.particles", "solid0.meshVertices", "solid0.detFInv", "nzMassVecInv",
          "JMInvJTDiag", "b1", "velocityAtDt0", "solidUnitForce", "dampedSolidMassVec",
-         "solidVelocityAtDt0"]
+         "solidVelocityAtDt0", "solid0.FpInv", "solid0.FpInvGrid"]
 
 # golden name -> integrator field name (abi.FIELDS)
 NAME = {n: n.replace("solid0.", "solid.") for n in EXACT + FLOAT}
@@ -35,10 +35,12 @@ def load_golden(name):
     meta = json.loads(str(z["scene"]))
     log = json.loads(str(z["log"]))
     solids = [SolidDesc(center=tuple(s["center"]), radius=s["radius"], density=s["density"],
-                        E=s["E"], nu=s["nu"], velocity=tuple(s["velocity"])) for s in meta["solids"]]
+                        E=s["E"], nu=s["nu"], velocity=tuple(s["velocity"]),
+                        plastic_yield=s.get("plastic_yield", -1.0)) for s in meta["solids"]]
     desc = SceneDesc(N=meta["N"], mass_sample_dh=meta["mass_sample_dh"],
                      vorticity_eps=meta["vorticity_eps"], buoyancy=meta["buoyancy"],
-                     noise_seed=meta["noise_seed"], solids=solids)
+                     noise_seed=meta["noise_seed"], flow_rate=meta.get("flow_rate", 0.5),
+                     solids=solids)
     return desc, z, log
 
 

@@ -2,7 +2,7 @@
 CPU implementation (oracle/_ref/ref_harness, built by oracle/Makefile from
 the unmodified EULERSF sources) on small synthetic scenes.
 
-    make -C oracle REF=/path/to/EULERSF && python tests/golden/make_golden.py
+    make -C oracle REF=/path/to/EULERSF && python tests/golden/make_golden.py [scene ...]
 
 Each scene is written as <name>.npz holding the initial state (s0.*) and the
 state after every step (s<k>.*) for the fields listed below, plus the step
@@ -39,6 +39,10 @@ def scenes():
     out["wall20"] = (SceneDesc(N=20, mass_sample_dh=(1 / 20) / 4, noise_seed=5,
                                solids=[SolidDesc(center=(0.5, 0.2, 0.45), radius=0.14,
                                                  velocity=(0.0, -0.6, 0.0))]), 2)
+    # plastic ball hitting the floor: stress above the yield, FpInv updated
+    out["plastic20"] = (SceneDesc(N=20, mass_sample_dh=(1 / 20) / 4, noise_seed=7, flow_rate=0.5,
+                                  solids=[SolidDesc(center=(0.5, 0.2, 0.45), radius=0.14,
+                                                    velocity=(0.0, -0.6, 0.0), plastic_yield=40.0)]), 2)
     return out
 
 
@@ -53,6 +57,7 @@ STEP_FIELDS = ["gridIdxToSolidIdx", "velocity", "intensity", "lambda1",
                "solidVelocityAtDt0", "systemMatrix.indptr", "systemMatrix.indices",
                "systemMatrix.data"]
 LAST_STEP_FIELDS = ["solid0.particles"]
+PLASTIC_FIELDS = ["solid0.FpInv", "solid0.FpInvGrid"]
 
 
 def run(name, desc, frames, out_dir):
@@ -64,11 +69,13 @@ def run(name, desc, frames, out_dir):
                         os.path.join(tmp, "scene", "noise.f64")], check=True,
                        stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
         arrays = {}
-        for f in INIT_FIELDS:
-            arrays["s0." + f] = np.load(os.path.join(dump, f"s0.{f}.npy"))
+        for f in INIT_FIELDS + PLASTIC_FIELDS:
+            p = os.path.join(dump, f"s0.{f}.npy")
+            if os.path.exists(p):
+                arrays["s0." + f] = np.load(p)
         log = [json.loads(l) for l in open(os.path.join(dump, "log.jsonl"))][1:]
         for k in range(1, len(log) + 1):
-            for f in STEP_FIELDS + (LAST_STEP_FIELDS if k == len(log) else []):
+            for f in STEP_FIELDS + PLASTIC_FIELDS + (LAST_STEP_FIELDS if k == len(log) else []):
                 p = os.path.join(dump, f"s{k}.{f}.npy")
                 if os.path.exists(p):
                     arrays[f"s{k}.{f}"] = np.load(p)
@@ -78,7 +85,7 @@ def run(name, desc, frames, out_dir):
         arrays["scene"] = np.array(json.dumps({
             "N": desc.N, "mass_sample_dh": desc.mass_sample_dh, "vorticity_eps": desc.vorticity_eps,
             "buoyancy": desc.buoyancy, "noise_seed": desc.noise_seed, "frames": frames,
-            "solids": [s.__dict__ for s in desc.solids]}))
+            "flow_rate": desc.flow_rate, "solids": [s.__dict__ for s in desc.solids]}))
         np.savez_compressed(os.path.join(out_dir, name + ".npz"), **arrays)
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
@@ -87,7 +94,10 @@ def run(name, desc, frames, out_dir):
 def main():
     if not os.path.exists(HARNESS):
         sys.exit(f"{HARNESS} missing: build it with make -C oracle")
+    only = sys.argv[1:]  # optional scene names
     for name, (desc, frames) in scenes().items():
+        if only and name not in only:
+            continue
         run(name, desc, frames, HERE)
         print(name, os.path.getsize(os.path.join(HERE, name + ".npz")), "bytes")
 
