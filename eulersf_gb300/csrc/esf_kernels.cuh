@@ -54,6 +54,14 @@ struct SolidDev {
   double lambda, mu, qcm;
   double G;  // 0.25 / dh
   double dt;
+  // plasticity (setPlasticYield; material grid of loadSurfaceMesh)
+  int plastic;
+  double yield, flowRate;
+  int pres[3];
+  double pdh, porig[3];
+  double* FpInv;    // 9 per material cell, row-major
+  int* updIdx;      // per valid cell: material cell it updates, or -1
+  double* updVal;   // per valid cell: the updated FpInv
 };
 
 // --------------------------------------------------------- 3x3 helpers
@@ -1097,6 +1105,7 @@ __device__ void sym_eig3(const M3& A, double w[3], M3& V) {
 struct Corot {
   double lambda, mu;
   M3 R, S, L;
+  M3 V, Fh;  // of the decomposition (COROTATION::V(), Fhat())
 };
 
 // COROTATION::orthogonalizeU (COROTATION.cpp:127-230)
@@ -1187,6 +1196,8 @@ __device__ void corot_init(Corot& c, const M3& F) {
   }
   c.R = m3_mul_bt(U, V);
   c.S = m3_mul_bt(m3_mul(V, Fh), V);
+  c.V = V;
+  c.Fh = Fh;
   double trF = sum3(Fh.m[0][0], Fh.m[1][1], Fh.m[2][2]);
   double trFm1 = sum3(Fh.m[0][0] - 1.0, Fh.m[1][1] - 1.0, Fh.m[2][2] - 1.0);
   M3 T;
@@ -1235,6 +1246,35 @@ __device__ M3 corot_dpk_row(const Corot& c, int j, const double* gf) {
 // DEFOR_SOLID_3D::computeStiffnessMatrixAndMaterialForce
 // (DEFOR_SOLID_3D.cpp:697-871), one thread per valid cell: stores the
 // cell's 24x24 stiffness (row k, column i) and its 3x8 nodal forces.
+// ||A|| (Eigen's norm()): squares in column-major order, summed as two-lane
+// packets ((a0,a1)+(a2,a3)) + ((a4,a5)+(a6,a7)), lanes added, then the ninth
+__device__ double m3_norm(const M3& a) {
+  double q[9];
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++) q[j * 3 + i] = a.m[i][j] * a.m[i][j];
+  const double l0 = (q[0] + q[2]) + (q[4] + q[6]);
+  const double l1 = (q[1] + q[3]) + (q[5] + q[7]);
+  return sqrt((l0 + l1) + q[8]);
+}
+
+// FpInv write-back after the stiffness sweep: per material cell the update
+// of the last valid cell in sweep order (z, y, x) wins, as the reference's
+// serial map assignment does (DEFOR_SOLID_3D.cpp:862-868)
+__global__ void k_fp_winner(const int* upd, long long nc, int* winner) {
+  FOR_N(nc, t) {
+    const int m = upd[t];
+    if (m >= 0) atomicMax(&winner[m], (int)t);
+  }
+}
+__global__ void k_fp_apply(const int* upd, const double* val, long long nc, const int* winner,
+                           double* FpInv) {
+  FOR_N(nc, t) {
+    const int m = upd[t];
+    if (m >= 0 && winner[m] == (int)t)
+      for (int q = 0; q < 9; q++) FpInv[9 * m + q] = val[9 * t + q];
+  }
+}
+
 __global__ void k_element_stiffness(GridDev g, SolidDev s, const long long* cells, long long nc,
                                     double* Ke, double* nf, double* energyPart) {
   double dh = g.dh;
@@ -1247,20 +1287,66 @@ __global__ void k_element_stiffness(GridDev g, SolidDev s, const long long* cell
     Corot c;
     c.lambda = s.lambda;
     c.mu = s.mu;
-    corot_init(c, F);
-    // P = R (2 mu E + lambda tr(E) I), E = S - I  (COROTATION.cpp:53-62)
-    M3 E = c.S;
-    for (int i = 0; i < 3; i++) E.m[i][i] -= 1.0;
-    M3 tmp;
-    for (int i = 0; i < 3; i++)
-      for (int j = 0; j < 3; j++) tmp.m[i][j] = 2.0 * c.mu * E.m[i][j];
-    double trE = sum3(E.m[0][0], E.m[1][1], E.m[2][2]);
-    for (int i = 0; i < 3; i++) tmp.m[i][i] += c.lambda * trE;
-    M3 P = m3_mul(c.R, tmp);
-    M3 JP;
-    for (int i = 0; i < 3; i++)
-      for (int j = 0; j < 3; j++) JP.m[i][j] = Jinv * P.m[i][j];
-    M3 cs = m3_mul_bt(JP, F);
+    M3 E, cs;
+    double trE;
+    // P = R (2 mu E + lambda tr(E) I), E = S - I  (COROTATION.cpp:53-62);
+    // cauchy = Jinv P F^T
+    auto stress = [&]() {
+      corot_init(c, F);
+      E = c.S;
+      for (int i = 0; i < 3; i++) E.m[i][i] -= 1.0;
+      M3 tmp;
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) tmp.m[i][j] = 2.0 * c.mu * E.m[i][j];
+      trE = sum3(E.m[0][0], E.m[1][1], E.m[2][2]);
+      for (int i = 0; i < 3; i++) tmp.m[i][i] += c.lambda * trE;
+      M3 P = m3_mul(c.R, tmp);
+      M3 JP;
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) JP.m[i][j] = Jinv * P.m[i][j];
+      cs = m3_mul_bt(JP, F);
+    };
+    stress();
+    // plasticity (DEFOR_SOLID_3D.cpp:765-791): above the yield stress the
+    // elastic part F FpInv is used and a flow step on the singular values
+    // gives the cell's FpInv update, written after the sweep (k_fp_apply)
+    if (s.plastic) {
+      int upd = -1;
+      if (m3_norm(cs) > s.yield) {
+        double rp[3] = {0, 0, 0};
+        for (int i = 0; i < 8; i++)
+          for (int k = 0; k < 3; k++) rp[k] += s.X[3 * (n + off[i]) + k];
+        for (int k = 0; k < 3; k++) rp[k] /= 8;
+        int ci[3];
+        for (int k = 0; k < 3; k++) {
+          int i = (int)floor((rp[k] - s.porig[k]) / s.pdh);
+          ci[k] = i <= 0 ? 0 : (i >= s.pres[k] - 1 ? s.pres[k] - 1 : i);
+        }
+        const int mc = (ci[2] * s.pres[1] + ci[1]) * s.pres[0] + ci[0];
+        M3 Fp;
+        for (int i = 0; i < 3; i++)
+          for (int j = 0; j < 3; j++) Fp.m[i][j] = s.FpInv[9 * mc + 3 * i + j];
+        F = m3_mul(F, Fp);
+        stress();
+        const double cN = m3_norm(cs);
+        if (cN > s.yield) {
+          const double gamma = s.flowRate * (cN - s.yield) / cN;
+          const double cr = cbrt(1.0 / fmax(fabs(Jinv), 1e-3));
+          M3 Fh = c.Fh;
+          for (int i = 0; i < 3; i++) Fh.m[i][i] = pow(Fh.m[i][i] / cr, -gamma);
+          const M3 nFp = m3_mul(m3_mul_bt(m3_mul(c.V, Fh), c.V), Fp);
+          bool bad = false;
+          for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) bad |= nFp.m[i][j] != nFp.m[i][j];
+          if (!bad) {
+            upd = mc;
+            for (int i = 0; i < 3; i++)
+              for (int j = 0; j < 3; j++) s.updVal[9 * t + 3 * i + j] = nFp.m[i][j];
+          }
+        }
+      }
+      s.updIdx[t] = upd;
+    }
     double GF[8][3];
     for (int i = 0; i < 8; i++) {
       double gi[3] = {sgnx(i) * s.G, sgny(i) * s.G, sgnz(i) * s.G};

@@ -87,6 +87,9 @@ struct Solid {
   double safeMin[3], safeMax[3];
   // particles and valid-cell list
   DBuf part, cellList, cellFlag, cellScan;
+  // plasticity: FpInv per material cell, per-valid-cell updates, winners
+  DBuf fp, fpUpd, fpVal, fpWin;
+  long long pn = 0;
   long long np = 0, nValid = 0;
   double pmass = 0;
 };
@@ -302,6 +305,7 @@ static void free_solid(Solid* d) {
   cudaFree(x.mass); cudaFree(x.phi); cudaFree(x.detFInv); cudaFree(x.quarter); cudaFree(x.valid);
   cudaFree(d->dRot); cudaFree(d->dVerts); cudaFree(d->dRest); cudaFree(d->dRestMass); cudaFree(d->dTris);
   d->part.release(); d->cellList.release(); d->cellFlag.release(); d->cellScan.release();
+  d->fp.release(); d->fpUpd.release(); d->fpVal.release(); d->fpWin.release();
   delete d;
 }
 
@@ -426,6 +430,39 @@ extern "C" esf_status esf_add_solid(esf_scene* sc, const esf_solid_desc* dd) {
   ESF_CUDA(cudaMemsetAsync(x.detFInv, 0, T * 8, st));
   ESF_CUDA(cudaMemsetAsync(x.quarter, 0, T * 64, st));
   ESF_CUDA(cudaMemsetAsync(x.valid, 0, G.R, st));
+  // setPlasticYield before loadSurfaceMesh (main.cpp:119-123, 144): FpInv
+  // on a grid of half the cell size over the rest mesh's box grown by one
+  // cell, identity (DEFOR_SOLID_3D.cpp:158-186)
+  if (dd->plastic_yield > 0) {
+    x.plastic = 1;
+    x.yield = dd->plastic_yield;
+    x.flowRate = sc->p.flow_rate;
+    double bmin[3] = {1e9, 1e9, 1e9}, bmax[3] = {-1e9, -1e9, -1e9};
+    for (int v = 0; v < d->nv; v++)
+      for (int k = 0; k < 3; k++) {
+        bmin[k] = std::min(bmin[k], d->restPose[3 * v + k]);
+        bmax[k] = std::max(bmax[k], d->restPose[3 * v + k]);
+      }
+    x.pdh = G.dh * .5;
+    for (int k = 0; k < 3; k++) {
+      bmin[k] -= G.dh;
+      bmax[k] += G.dh;
+      x.pres[k] = (int)((bmax[k] - bmin[k]) / x.pdh + 1);
+      x.porig[k] = bmin[k];
+    }
+    d->pn = (long long)x.pres[0] * x.pres[1] * x.pres[2];
+    std::vector<double> id((size_t)d->pn * 9, 0.0);
+    for (long long c = 0; c < d->pn; c++)
+      for (int i = 0; i < 3; i++) id[c * 9 + 4 * i] = 1.0;
+    esf_status ea = d->fp.ensure(d->pn * 72);
+    if (!ea) ea = d->fpWin.ensure(d->pn * 4);
+    if (ea) {
+      free_solid(d);
+      return ea;
+    }
+    x.FpInv = d->fp.as<double>();
+    ESF_CUDA(cudaMemcpy(x.FpInv, id.data(), d->pn * 72, cudaMemcpyHostToDevice));
+  }
   ESF_COUNTED k_initial_state<<<kblocks(G.T), KT, 0, st>>>(G, x, d->dRot, d->trans[0], d->trans[1], d->trans[2],
                                                d->scale[0], d->scale[1], d->scale[2], d->v0[0],
                                                d->v0[1], d->v0[2]);
@@ -728,10 +765,22 @@ static esf_status solid_system(esf_scene* sc, double* energyOut) {
     long long nc = d->nValid;
     TRY(sc->Ke.ensure((576 * nc + 1) * 8));
     TRY(sc->nf.ensure((24 * nc + 1) * 8));
+    if (nc > 0 && d->d.plastic) {
+      TRY(d->fpUpd.ensure(nc * 4));
+      TRY(d->fpVal.ensure(nc * 72));
+      d->d.updIdx = d->fpUpd.as<int>();
+      d->d.updVal = d->fpVal.as<double>();
+    }
     if (nc > 0) {
       ESF_COUNTED k_element_stiffness<<<kblocks(nc, 128), 128, 0, st>>>(G, d->d, d->cellList.as<long long>(), nc,
                                                              sc->Ke.as<double>(), sc->nf.as<double>(),
                                                              ePart);
+      if (d->d.plastic) {
+        ESF_CUDA(cudaMemsetAsync(d->fpWin.p, 0xff, d->pn * 4, st));
+        ESF_COUNTED k_fp_winner<<<kblocks(nc), KT, 0, st>>>(d->d.updIdx, nc, d->fpWin.as<int>());
+        ESF_COUNTED k_fp_apply<<<kblocks(nc), KT, 0, st>>>(d->d.updIdx, d->d.updVal, nc, d->fpWin.as<int>(),
+                                                           d->d.FpInv);
+      }
       // cell -> ordinal in the valid list
       ESF_COUNTED k_cell_ord_fill<<<kblocks(nc), KT, 0, st>>>(G, d->cellList.as<long long>(), nc, sc->cellOrd);
     }
@@ -1060,7 +1109,8 @@ struct FieldRef {
   void* dev = nullptr;     // device source (node/cell/solid layouts)
   size_t count = 0;        // elements exposed
   size_t eb = 8;
-  int kind = 0;            // 0 direct, 1 node3->dof3, 2 node1->dof3, 3 host ints, 4 dof map
+  int kind = 0;            // 0 direct, 1 node3->dof3, 2 node1->dof3, 3 host ints, 4 dof map,
+                           // 5 system blocks, 6 plastic material grid header
   bool writable = false;
 };
 }  // namespace
@@ -1110,6 +1160,14 @@ static esf_status field_ref(esf_scene* s, int f, int si, FieldRef& r) {
     case ESF_F_S_PARTICLES: r = {d->part.p, (size_t)d->np * 10, 8, 0, false}; return ESF_OK;
     case ESF_F_S_MESH_VERTICES: r = {d->dVerts, (size_t)d->nv * 3, 8, 0, false}; return ESF_OK;
     case ESF_F_S_BOXES: r = {nullptr, 12, 4, 3, false}; return ESF_OK;
+    case ESF_F_S_FPINV:
+      if (!d->d.plastic) break;
+      r = {d->d.FpInv, (size_t)d->pn * 9, 8, 0, true};
+      return ESF_OK;
+    case ESF_F_S_FPINV_GRID:
+      if (!d->d.plastic) break;
+      r = {nullptr, 7, 8, 6, false};
+      return ESF_OK;
     default: break;
   }
   set_error("unknown field id %d", f);
@@ -1145,6 +1203,13 @@ extern "C" esf_status esf_get_field(esf_scene* s, esf_field f, int si, void* hos
     int b[12] = {d->ex[0], d->ex[1], d->ex[2], d->ex[3], d->ex[4], d->ex[5],
                  d->tmin[0], d->tmin[1], d->tmin[2], d->tmax[0], d->tmax[1], d->tmax[2]};
     memcpy(host, b, 48);
+    return ESF_OK;
+  }
+  if (r.kind == 6) {  // material grid of FpInv: xRes, yRes, zRes, dh, origin
+    const SolidDev& x = s->s[si]->d;
+    const double h[7] = {(double)x.pres[0], (double)x.pres[1], (double)x.pres[2], x.pdh,
+                         x.porig[0], x.porig[1], x.porig[2]};
+    memcpy(host, h, sizeof h);
     return ESF_OK;
   }
   if (r.kind == 5) {  // system blocks: device entry-major -> [node][27][3][3]
@@ -1328,6 +1393,15 @@ extern "C" esf_status esf_write_frame(esf_scene* s, const char* path, int frame,
       TRY(write_field_gz(fn + ".velocity", res, G.dh, G.o, buf.data(), G.T * 3));
       TRY(esf_get_field(s, ESF_F_S_PHI, i, buf.data(), G.T * 8));
       TRY(write_field_gz(fn + ".phi", res, G.dh, G.o, buf.data(), G.T));
+      if (d->d.plastic) {
+        // MATRIX3_FIELD_3D::writeGz: 9 doubles per cell, column-major
+        std::vector<double> fp((size_t)d->pn * 9), cm((size_t)d->pn * 9);
+        TRY(esf_get_field(s, ESF_F_S_FPINV, i, fp.data(), fp.size() * 8));
+        for (long long c = 0; c < d->pn; c++)
+          for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) cm[9 * c + 3 * b + a] = fp[9 * c + 3 * a + b];
+        TRY(write_field_gz(fn + ".plasticdefor", d->d.pres, d->d.pdh, d->d.porig, cm.data(), cm.size()));
+      }
     }
     std::vector<double> v((size_t)d->nv * 3);
     TRY(esf_get_field(s, ESF_F_S_MESH_VERTICES, i, v.data(), v.size() * 8));
@@ -1374,6 +1448,14 @@ extern "C" esf_status esf_read_frame(esf_scene* s, const char* path, int frame, 
       TRY(esf_set_field(s, ESF_F_S_VELOCITY, i, buf.data(), G.T * 24));
       TRY(read_field_gz(fn + ".phi", res, G.T, buf.data()));
       TRY(esf_set_field(s, ESF_F_S_PHI, i, buf.data(), G.T * 8));
+      if (d->d.plastic) {
+        std::vector<double> fp((size_t)d->pn * 9), cm((size_t)d->pn * 9);
+        TRY(read_field_gz(fn + ".plasticdefor", d->d.pres, cm.size(), cm.data()));
+        for (long long c = 0; c < d->pn; c++)
+          for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) fp[9 * c + 3 * a + b] = cm[9 * c + 3 * b + a];
+        TRY(esf_set_field(s, ESF_F_S_FPINV, i, fp.data(), fp.size() * 8));
+      }
     }
     ESF_COUNTED k_frame_X<<<kblocks(G.T), KT, 0, st>>>(G, d->d);
     ESF_LAUNCH_CHECK();

@@ -86,6 +86,7 @@ def run(cfg_path, frames=None, precision=abi.ESF_FP64, out=sys.stdout):
         d.initial_velocity[:] = list(vec(f"solid initial velocity {i}", (0, 0, 0)))
         d.num_vertices, d.vertices = len(verts), v.ctypes.data_as(C.POINTER(C.c_double))
         d.num_triangles, d.triangles = len(tris), t.ctypes.data_as(C.POINTER(C.c_int))
+        d.plastic_yield = float(cfg.get(f"solid plastic yield {i}", -1))
         I.addSolid(d, keep=(rest, v, t))
     I.setFluidDensity(float(cfg.get("fluid density", 1)))
     I.setFluidViscocity(float(cfg.get("fluid viscocity", 0)))

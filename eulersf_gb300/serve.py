@@ -63,7 +63,8 @@ def request_for(desc, steps: int, precision: int = abi.ESF_MIXED):
     from .integrator import make_solid_desc, params_from_desc
     descs, keep = [], []
     for s in desc.solids:
-        d, k = make_solid_desc(s.radius, s.center, s.density, s.E, s.nu, s.velocity)
+        d, k = make_solid_desc(s.radius, s.center, s.density, s.E, s.nu, s.velocity,
+                               s.plastic_yield)
         descs.append(d)
         keep.extend(k)
     arr = (abi.SolidDesc * len(descs))(*descs)
