@@ -14,14 +14,13 @@ from __future__ import annotations
 
 import ctypes as C
 import json
-import math
 import sys
 
 import numpy as np
 
 from . import abi, load
 from .integrator import CoupledIntegrator3D, run_frames
-from .scene import parse_cfg, read_field_gz
+from .scene import parse_cfg, read_field_gz, rotation_matrix
 
 
 def read_obj(path):
@@ -41,15 +40,6 @@ def read_obj(path):
                 for k in range(1, len(idx) - 1):
                     tris.append([idx[0], idx[k], idx[k + 1]])
     return np.array(verts, dtype=np.float64), np.array(tris, dtype=np.int32)
-
-
-def rotation(angles):
-    """Rx(a pi) Ry(b pi) Rz(c pi) as main.cpp:131-136 builds it."""
-    a, b, c = (x * math.pi for x in angles)
-    rx = np.array([[1, 0, 0], [0, math.cos(a), -math.sin(a)], [0, math.sin(a), math.cos(a)]])
-    ry = np.array([[math.cos(b), 0, math.sin(b)], [0, 1, 0], [-math.sin(b), 0, math.cos(b)]])
-    rz = np.array([[math.cos(c), -math.sin(c), 0], [math.sin(c), math.cos(c), 0], [0, 0, 1]])
-    return rx @ ry @ rz
 
 
 def run(cfg_path, frames=None, precision=abi.ESF_FP64, out=sys.stdout):
@@ -80,7 +70,7 @@ def run(cfg_path, frames=None, precision=abi.ESF_FP64, out=sys.stdout):
         d.lambda_ = float(cfg.get(f"material lambda {i}", 100))
         d.mu = float(cfg.get(f"material mu {i}", 100))
         d.density = float(cfg.get(f"solid mass density {i}", 1))
-        d.rotation[:] = list(rotation(vec(f"solid rotation {i}", (0, 0, 0))).reshape(-1))
+        d.rotation[:] = list(rotation_matrix(vec(f"solid rotation {i}", (0, 0, 0))).reshape(-1))
         d.translation[:] = list(vec(f"solid translation {i}", (0, 0, 0)))
         d.scaling[:] = list(vec(f"solid scaling {i}", (1, 1, 1)))
         d.initial_velocity[:] = list(vec(f"solid initial velocity {i}", (0, 0, 0)))

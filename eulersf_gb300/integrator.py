@@ -145,8 +145,11 @@ class CoupledIntegrator3D:
         return self.get("intensity")
 
 
-def make_solid_desc(radius, center, density, E, nu, velocity=(0, 0, 0), plastic_yield=-1.0):
-    """Solid descriptor for the synthetic sphere (rest assets from scene.py)."""
+def make_solid_desc(radius, center, density, E, nu, velocity=(0, 0, 0), plastic_yield=-1.0,
+                    rotation=(0.0, 0.0, 0.0), scaling=(1.0, 1.0, 1.0), rotation_matrix=None):
+    """Solid descriptor for the synthetic sphere (rest assets from scene.py);
+    `rotation` in the cfg's units (angles / pi), or an exact `rotation_matrix`."""
+    from .scene import rotation_matrix as _rot
     (res, mdh, morig, mdata), verts, faces = solid_assets(radius)
     lam, mu = lame(E, nu)
     rest = np.ascontiguousarray(mdata.reshape(-1), dtype=np.float64)
@@ -158,9 +161,10 @@ def make_solid_desc(radius, center, density, E, nu, velocity=(0, 0, 0), plastic_
     d.mass_origin[:] = [float(x) for x in morig]
     d.rest_mass = rest.ctypes.data_as(C.POINTER(C.c_double))
     d.lambda_, d.mu, d.density = lam, mu, density
-    d.rotation[:] = [1, 0, 0, 0, 1, 0, 0, 0, 1]
+    rm = rotation_matrix if rotation_matrix is not None else _rot(rotation).reshape(-1)
+    d.rotation[:] = [float(x) for x in np.asarray(rm).reshape(-1)]
     d.translation[:] = [float(x) for x in center]
-    d.scaling[:] = [1.0, 1.0, 1.0]
+    d.scaling[:] = [float(x) for x in scaling]
     d.initial_velocity[:] = [float(x) for x in velocity]
     d.num_vertices = len(verts)
     d.vertices = v.ctypes.data_as(C.POINTER(C.c_double))
@@ -209,7 +213,7 @@ def build_from_scene(lib, prefix, desc: SceneDesc, precision=abi.ESF_FP64, noise
                             params_from_desc(desc, precision), stream=stream)
     for s in desc.solids:
         d, keep = make_solid_desc(s.radius, s.center, s.density, s.E, s.nu, s.velocity,
-                                  s.plastic_yield)
+                                  s.plastic_yield, s.rotation, s.scaling, s.rotation_matrix)
         I.addSolid(d, keep)
     I.setFluidDensity(desc.fluid_density)
     I.setFluidViscocity(0.0)

@@ -18,9 +18,9 @@ Inputs that stand in for the reference's shipped assets (meshes/sphere/*):
   on a grid of mass_dh = r/100 (the shipped 0.1-radius sphere uses 0.001);
 * surface mesh: a subdivided icosahedron of radius r (only its vertex
   AABB drives the step, via the CFL factor, COUPLED_INTEGRATOR_3D.cpp:386-410);
-* ``solid scaling`` stays 1: the reference treats it as a deformation of the
-  rest shape (X = R^T (x - T) / s, DEFOR_SOLID_3D.cpp:126-152), so a scaled
-  ball would start stretched (F = s I);
+* ``solid scaling`` defaults to 1: the reference treats it as a deformation
+  of the rest shape (X = R^T (x - T) / s, DEFOR_SOLID_3D.cpp:126-152), so a
+  scaled ball starts stretched (F = s I);
 * fluid noise: U(-a, a) per component at interior nodes from a counter-based
   splitmix64 stream keyed by (seed, node, component), so that C, CUDA and
   numpy produce the same values.
@@ -65,6 +65,11 @@ class SolidDesc:
     nu: float = 0.45
     velocity: tuple = (0.0, 0.0, 0.0)
     plastic_yield: float = -1.0  # "solid plastic yield i"; <= 0: elastic
+    rotation: tuple = (0.0, 0.0, 0.0)  # "solid rotation i": angles about x, y, z in units of pi
+    scaling: tuple = (1.0, 1.0, 1.0)   # "solid scaling i" (deforms the rest shape)
+    # the 3x3 rotation (row-major) the reference built from `rotation`, when
+    # known exactly (golden fixtures); otherwise computed by rotation_matrix()
+    rotation_matrix: tuple | None = None
 
 
 @dataclass
@@ -123,7 +128,6 @@ class SceneDesc:
         }
         for i, s in enumerate(self.solids):
             lam, mu = lame(s.E, s.nu)
-            sc = 1.0
             c.update({
                 f"solid path {i}": solid_dir, f"solid name {i}": f"{solid_name}{i}",
                 f"solid mass density {i}": s.density,
@@ -131,8 +135,8 @@ class SceneDesc:
                 f"solid plastic yield {i}": s.plastic_yield,
                 f"solid initial velocity {i}": tuple(s.velocity),
                 f"solid translation {i}": tuple(s.center),
-                f"solid scaling {i}": (sc, sc, sc),
-                f"solid rotation {i}": (0.0, 0.0, 0.0),
+                f"solid scaling {i}": tuple(s.scaling),
+                f"solid rotation {i}": tuple(s.rotation),
             })
         return c
 
@@ -317,3 +321,14 @@ def pressure_problem(desc: SceneDesc, seed: int = 0):
     rng = np.random.default_rng(seed)
     b = rng.standard_normal(N ** 3)
     return minv, diag.reshape(-1), b
+
+
+def rotation_matrix(angles) -> np.ndarray:
+    """Rx(a pi) Ry(b pi) Rz(c pi) (main.cpp:131-136), row-major 3x3. The
+    reference forms it through Eigen quaternions, so the last bits can
+    differ; golden fixtures carry the reference's own matrix instead."""
+    a, b, c = (float(x) * np.pi for x in angles)
+    rx = np.array([[1, 0, 0], [0, np.cos(a), -np.sin(a)], [0, np.sin(a), np.cos(a)]])
+    ry = np.array([[np.cos(b), 0, np.sin(b)], [0, 1, 0], [-np.sin(b), 0, np.cos(b)]])
+    rz = np.array([[np.cos(c), -np.sin(c), 0], [np.sin(c), np.cos(c), 0], [0, 0, 1]])
+    return rx @ ry @ rz

@@ -64,7 +64,7 @@ def request_for(desc, steps: int, precision: int = abi.ESF_MIXED):
     descs, keep = [], []
     for s in desc.solids:
         d, k = make_solid_desc(s.radius, s.center, s.density, s.E, s.nu, s.velocity,
-                               s.plastic_yield)
+                               s.plastic_yield, s.rotation, s.scaling, s.rotation_matrix)
         descs.append(d)
         keep.extend(k)
     arr = (abi.SolidDesc * len(descs))(*descs)

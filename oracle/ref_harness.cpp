@@ -126,6 +126,10 @@ struct Dumper {
   }
 };
 
+// the rotation each solid was set up with (main.cpp:131-136 builds it through
+// Eigen quaternions), dumped so that other implementations can take it as is
+static std::vector<MATRIX3> harnessRotations;
+
 static void dump_state(Dumper& d, COUPLED_INTEGRATOR_3D* I, bool full) {
   d.vfield("velocity", I->_velocity);
   d.field("intensity", I->_intensity);
@@ -176,6 +180,12 @@ static void dump_state(Dumper& d, COUPLED_INTEGRATOR_3D* I, bool full) {
                    S->_tightMin[0], S->_tightMin[1], S->_tightMin[2],
                    S->_tightMax[0], S->_tightMax[1], S->_tightMax[2]};
     ds.i32("boxes", box, 12);
+    if (s < harnessRotations.size()) {
+      double rm[9];
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) rm[i * 3 + j] = harnessRotations[s](i, j);
+      ds.f64("rotation", rm, 9);
+    }
     long np = S->_materialParticles.size();
     std::vector<double> pp(np * 10);
     for (long i = 0; i < np; i++) {
@@ -274,6 +284,7 @@ int main(int argc, char** argv) {
           Eigen::AngleAxisd(rotation[1] * M_PI, VEC3F::UnitY()) *
           Eigen::AngleAxisd(rotation[2] * M_PI, VEC3F::UnitZ());
     solid->setInitialState(rot, translation, scaling);
+    harnessRotations.push_back(rot);
     solid->setInitialVelocity(SIMPLE_PARSER::getVEC3F(
         "solid initial velocity " + index, VEC3F(0, 0, 0)));
     solid->loadSurfaceMesh(meshPath + ".obj");

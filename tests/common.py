@@ -15,7 +15,7 @@ for p in (ROOT, os.path.join(ROOT, "oracle")):
 
 from eulersf_gb300.scene import SceneDesc, SolidDesc  # noqa: E402
 
-GOLDEN_SCENES = ["ball16", "ball20_vort", "wall20", "plastic20"]
+GOLDEN_SCENES = ["ball16", "ball20_vort", "wall20", "plastic20", "rot20"]
 
 # bit-exact integer/flag fields (the reference's DOF maps, cell flags, boxes)
 EXACT = ["gridIdxToSolutionIdx", "gridIdxToSolidIdx", "solid0.valid", "solid0.boxes"]
@@ -36,7 +36,10 @@ def load_golden(name):
     log = json.loads(str(z["log"]))
     solids = [SolidDesc(center=tuple(s["center"]), radius=s["radius"], density=s["density"],
                         E=s["E"], nu=s["nu"], velocity=tuple(s["velocity"]),
-                        plastic_yield=s.get("plastic_yield", -1.0)) for s in meta["solids"]]
+                        plastic_yield=s.get("plastic_yield", -1.0),
+                        rotation=tuple(s.get("rotation", (0.0, 0.0, 0.0))),
+                        scaling=tuple(s.get("scaling", (1.0, 1.0, 1.0))),
+                        rotation_matrix=s.get("rotation_matrix")) for s in meta["solids"]]
     desc = SceneDesc(N=meta["N"], mass_sample_dh=meta["mass_sample_dh"],
                      vorticity_eps=meta["vorticity_eps"], buoyancy=meta["buoyancy"],
                      noise_seed=meta["noise_seed"], flow_rate=meta.get("flow_rate", 0.5),

@@ -43,6 +43,12 @@ def scenes():
     out["plastic20"] = (SceneDesc(N=20, mass_sample_dh=(1 / 20) / 4, noise_seed=7, flow_rate=0.5,
                                   solids=[SolidDesc(center=(0.5, 0.2, 0.45), radius=0.14,
                                                     velocity=(0.0, -0.6, 0.0), plastic_yield=40.0)]), 2)
+    # rotated, non-uniformly scaled (pre-stretched) ball: setInitialState's
+    # transform of X and of the mesh
+    out["rot20"] = (SceneDesc(N=20, mass_sample_dh=(1 / 20) / 4, noise_seed=4,
+                              solids=[SolidDesc(center=(0.5, 0.55, 0.5), radius=0.12,
+                                                rotation=(0.1, 0.25, 0.4),
+                                                scaling=(1.05, 0.95, 1.0))]), 2)
     return out
 
 
@@ -82,10 +88,15 @@ def run(name, desc, frames, out_dir):
         for l in log:
             l.pop("seconds", None)
         arrays["log"] = np.array(json.dumps(log))
+        solids = [dict(sd.__dict__) for sd in desc.solids]
+        for i, sd in enumerate(solids):
+            p = os.path.join(dump, f"s0.solid{i}.rotation.npy")
+            if os.path.exists(p):  # the reference's own rotation matrix
+                sd["rotation_matrix"] = [float(x) for x in np.load(p).reshape(-1)]
         arrays["scene"] = np.array(json.dumps({
             "N": desc.N, "mass_sample_dh": desc.mass_sample_dh, "vorticity_eps": desc.vorticity_eps,
             "buoyancy": desc.buoyancy, "noise_seed": desc.noise_seed, "frames": frames,
-            "flow_rate": desc.flow_rate, "solids": [s.__dict__ for s in desc.solids]}))
+            "flow_rate": desc.flow_rate, "solids": solids}))
         np.savez_compressed(os.path.join(out_dir, name + ".npz"), **arrays)
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
