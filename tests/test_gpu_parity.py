@@ -46,7 +46,7 @@ def test_gpu_step_matches_reference(name, gpu_lib):
     G.close()
 
 
-@pytest.mark.parametrize("N,steps", [(24, 3), (32, 2)])
+@pytest.mark.parametrize("N,steps", [(24, 3), (32, 2), (64, 1)])
 def test_gpu_step_matches_oracle(N, steps, gpu_lib):
     """Longer/larger runs than the fixtures hold, against the oracle run here."""
     import eulersf_gb300 as E
