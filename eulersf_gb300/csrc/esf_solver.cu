@@ -766,10 +766,10 @@ static esf_status capture(cudaStream_t cs, const K& k, bool first, bool warm, cu
 
 // Runs one PCR solve from graphs; keeps up to 3 chunks in flight and polls
 // pinned copies of the device state.
-static esf_status run_graph_solve(PressureWork* w, PcrState* dst, cudaGraphExec_t gFirst,
-                                  cudaGraphExec_t gChunk, unsigned long long kFirst,
-                                  unsigned long long kChunk, int maxIt, cudaStream_t st,
-                                  PcrState* out) {
+static esf_status run_graph_solve(PcrState* hst, cudaEvent_t* ev, PcrState* dst,
+                                  cudaGraphExec_t gFirst, cudaGraphExec_t gChunk,
+                                  unsigned long long kFirst, unsigned long long kChunk, int maxIt,
+                                  cudaStream_t st, PcrState* out) {
   const int inflight = 3;
   int launched = 0, waited = 0;
   const int maxChunks = maxIt / 5 + 3;
@@ -779,13 +779,13 @@ static esf_status run_graph_solve(PressureWork* w, PcrState* dst, cudaGraphExec_
       const bool first = launched == 0 && gFirst;
       ESF_CUDA(cudaGraphLaunch(first ? gFirst : gChunk, st));
       note_graph_replay(first ? kFirst : kChunk);
-      ESF_CUDA(cudaMemcpyAsync(&w->hst[launched % 4], dst, sizeof(PcrState), cudaMemcpyDeviceToHost, st));
-      ESF_CUDA(cudaEventRecord(w->ev[launched % 4], st));
+      ESF_CUDA(cudaMemcpyAsync(&hst[launched % 4], dst, sizeof(PcrState), cudaMemcpyDeviceToHost, st));
+      ESF_CUDA(cudaEventRecord(ev[launched % 4], st));
       launched++;
     }
     if (launched - waited >= inflight || launched >= maxChunks) {
-      ESF_CUDA(cudaEventSynchronize(w->ev[waited % 4]));
-      PcrState h = w->hst[waited % 4];
+      ESF_CUDA(cudaEventSynchronize(ev[waited % 4]));
+      PcrState h = hst[waited % 4];
       waited++;
       if (h.done) {
         done = true;
@@ -843,7 +843,7 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
     }
     esf_status e = init_state(w->st, eps, itCap, st);
     if (e) return e;
-    return run_graph_solve(w, w->st, w->gFirst, w->gChunk, w->kFirst, w->kChunk, itCap, st, out);
+    return run_graph_solve(w->hst, w->ev, w->st, w->gFirst, w->gChunk, w->kFirst, w->kChunk, itCap, st, out);
   };
   if (precision == ESF_FP64) {
     PcrState h;
@@ -950,7 +950,7 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
         fprintf(stderr, "[esf] refine %d at %.2f ms: iters %d rel %.3e\n", ref, ms, total, rel);
       }
       PcrState hi;
-      esf_status e = run_graph_solve(w, w->st32, nullptr, w->gChunk32, 0, w->kChunk32,
+      esf_status e = run_graph_solve(w->hst, w->ev, w->st32, nullptr, w->gChunk32, 0, w->kChunk32,
                                      maxIt, st, &hi);
       if (e) return e;
       total = hi.iter;
@@ -1179,6 +1179,12 @@ struct SolidWork {
   long long S;
   PcrState* hst;      // pinned state copies [4]
   cudaEvent_t ev[4];
+  // iteration chunks as CUDA graphs, per precision (0 FP64, 1 FP32 inner),
+  // recaptured when the system's size or buffers change
+  cudaStream_t capStream;
+  cudaGraphExec_t gFirst[2], gChunk[2];
+  unsigned long long kFirst[2], kChunk[2];
+  const void* key[2][10];
   double *r, *d, *Ap, *s, *invd, *partial;
   float *blocks32, *x32, *r32, *d32, *Ap32, *s32, *invd32, *b32;
   PcrState *st, *st32;
@@ -1201,6 +1207,7 @@ esf_status solid_work_alloc(SolidWork** out, long long S, int mixed) {
   ESF_CUDA(cudaMalloc(&w->st32, sizeof(PcrState)));
   ESF_CUDA(cudaMallocHost(&w->hst, 4 * sizeof(PcrState)));
   for (int i = 0; i < 4; i++) ESF_CUDA(cudaEventCreateWithFlags(&w->ev[i], cudaEventDisableTiming));
+  ESF_CUDA(cudaStreamCreateWithFlags(&w->capStream, cudaStreamNonBlocking));
   if (mixed) {
     ESF_CUDA(cudaMalloc(&w->blocks32, w->cap * 243 * 4));
     ESF_CUDA(cudaMalloc(&w->x32, n * 4));
@@ -1224,59 +1231,91 @@ void solid_work_free(SolidWork* w) {
   if (w->hst) cudaFreeHost(w->hst);
   for (int i = 0; i < 4; i++)
     if (w->ev[i]) cudaEventDestroy(w->ev[i]);
+  for (int p = 0; p < 2; p++) {
+    if (w->gFirst[p]) cudaGraphExecDestroy(w->gFirst[p]);
+    if (w->gChunk[p]) cudaGraphExecDestroy(w->gChunk[p]);
+  }
+  if (w->capStream) cudaStreamDestroy(w->capStream);
   delete w;
 }
 
+// The assembled-matrix PCR (CONJUGATE_RESIDUAL.inl:194-276) of the solid
+// system: zero start, three kernels per iteration, a residual check every
+// 5th iteration for reference solves (inner solves stop on delta).
 template <typename T>
-static esf_status solid_pcr(long long S, const T* blocks, const int* nbr, const T* invd,
-                            const T* b, T* x, T* r, T* d, T* Ap, T* s, double* partial,
-                            PcrState* dst, double eps, int maxIt, cudaStream_t st, PcrState* out,
-                            int inner, PcrState* hbuf, cudaEvent_t* evs) {
-  const long long n = 3 * S;
-  const int vb = vec_blocks(n), sb = vec_blocks(S);
+struct SolidKernels {
+  long long S;
+  const T *blocks, *invd, *b;
+  const int* nbr;
+  T *x, *r, *d, *Ap, *s;
+  double* partial;
+  PcrState* st;
+  void setup_zero(cudaStream_t cs) const {
+    const long long n = 3 * S;
+    ESF_COUNTED pcr_zero_start<T><<<vec_blocks(n), VT, 0, cs>>>(n, b, invd, x, r, d, Ap, partial, st);
+    ESF_COUNTED solid_spmv<T, S_UPDATE><<<vec_blocks(S), VT, 0, cs>>>(S, blocks, nbr, r, nullptr, nullptr, s,
+                                                                      nullptr, partial, st);
+  }
+  void chunk(cudaStream_t cs, int n_it, bool check) const {
+    const long long n = 3 * S;
+    const int vb = vec_blocks(n), sb = vec_blocks(S);
+    for (int k = 0; k < n_it; k++) {
+      ESF_COUNTED pcr_phase_a<T, false><<<vb, VT, 0, cs>>>(n, d, r, Ap, s, invd, partial, st);
+      ESF_COUNTED pcr_update_xr<T><<<vb, VT, 0, cs>>>(n, x, d, r, Ap, invd, st);
+      ESF_COUNTED solid_spmv<T, S_UPDATE><<<sb, VT, 0, cs>>>(S, blocks, nbr, r, nullptr, nullptr, s, nullptr,
+                                                             partial, st);
+    }
+    if (check)
+      ESF_COUNTED solid_spmv<T, S_CHECK><<<sb, VT, 0, cs>>>(S, blocks, nbr, x, b, nullptr, nullptr, nullptr,
+                                                            partial, st);
+  }
+};
+
+template <typename T>
+static esf_status capture_solid(cudaStream_t cs, const SolidKernels<T>& k, bool first, bool check,
+                                cudaGraphExec_t* exec, unsigned long long* kernels) {
+  cudaGraph_t graph;
+  *kernels = 0;
+  set_capturing(true, kernels);
+  cudaError_t ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (ce != cudaSuccess) {
+    set_capturing(false, nullptr);
+    ESF_CUDA(ce);
+  }
+  if (first) {
+    k.setup_zero(cs);
+    k.chunk(cs, 6, check);  // iterations 0..5, first check at i = 5
+  } else {
+    k.chunk(cs, 5, check);  // iterations 5j+1 .. 5j+5
+  }
+  set_capturing(false, nullptr);
+  ESF_CUDA(cudaStreamEndCapture(cs, &graph));
+  if (*exec) cudaGraphExecDestroy(*exec);
+  ESF_CUDA(cudaGraphInstantiate(exec, graph, 0));
+  cudaGraphDestroy(graph);
+  return ESF_OK;
+}
+
+// One solid PCR solve from graphs, set-up and iterations as the reference's.
+template <typename T>
+static esf_status solid_pcr_graph(SolidWork* w, int slot, long long S, const T* blocks, const int* nbr,
+                                  const T* invd, const T* b, T* x, T* r, T* d, T* Ap, T* s,
+                                  PcrState* dst, double eps, int maxIt, cudaStream_t st, PcrState* out,
+                                  int inner) {
+  SolidKernels<T> k{S, blocks, invd, b, nbr, x, r, d, Ap, s, w->partial, dst};
+  const void* key[10] = {(const void*)(intptr_t)S, blocks, nbr, invd, b, x, r, d, dst,
+                         (const void*)(intptr_t)inner};
+  if (!w->gFirst[slot] || memcmp(key, w->key[slot], sizeof key) != 0) {
+    esf_status e = capture_solid(w->capStream, k, true, !inner, &w->gFirst[slot], &w->kFirst[slot]);
+    if (e) return e;
+    e = capture_solid(w->capStream, k, false, !inner, &w->gChunk[slot], &w->kChunk[slot]);
+    if (e) return e;
+    memcpy(w->key[slot], key, sizeof key);
+  }
   esf_status e = init_state(dst, eps, maxIt, st, inner);
   if (e) return e;
-  // assembled variant: x = 0, r = b/diag (CONJUGATE_RESIDUAL.inl:196-205)
-  ESF_COUNTED pcr_zero_start<T><<<vb, VT, 0, st>>>(n, b, invd, x, r, d, Ap, partial, dst);
-  ESF_COUNTED solid_spmv<T, S_UPDATE><<<sb, VT, 0, st>>>(S, blocks, nbr, r, nullptr, nullptr, s, nullptr,
-                                             partial, dst);
-  ESF_LAUNCH_CHECK();
-  // chunks of 5 iterations (the first 6) each followed by an async copy of
-  // the state into pinned memory; up to 3 chunks in flight, then poll
-  PcrState h;
-  memset(&h, 0, sizeof h);
-  const int maxChunks = maxIt / 5 + 3;
-  const int inflight = 3;
-  int launched = 0, waited = 0;
-  bool done = false;
-  while (!done) {
-    if (launched < maxChunks) {
-      const int nIt = (launched == 0) ? 6 : 5;  // iterations 0..5, then 5j+1..5j+5
-      for (int k = 0; k < nIt; k++) {
-        ESF_COUNTED pcr_phase_a<T, false><<<vb, VT, 0, st>>>(n, d, r, Ap, s, invd, partial, dst);
-        ESF_COUNTED pcr_update_xr<T><<<vb, VT, 0, st>>>(n, x, d, r, Ap, invd, dst);
-        ESF_COUNTED solid_spmv<T, S_UPDATE><<<sb, VT, 0, st>>>(S, blocks, nbr, r, nullptr, nullptr, s,
-                                                               nullptr, partial, dst);
-      }
-      if (!inner)
-        ESF_COUNTED solid_spmv<T, S_CHECK><<<sb, VT, 0, st>>>(S, blocks, nbr, x, b, nullptr, nullptr,
-                                                              nullptr, partial, dst);
-      ESF_LAUNCH_CHECK();
-      ESF_CUDA(cudaMemcpyAsync(&hbuf[launched % 4], dst, sizeof(PcrState), cudaMemcpyDeviceToHost, st));
-      ESF_CUDA(cudaEventRecord(evs[launched % 4], st));
-      launched++;
-    }
-    if (launched - waited >= inflight || launched >= maxChunks) {
-      ESF_CUDA(cudaEventSynchronize(evs[waited % 4]));
-      h = hbuf[waited % 4];
-      waited++;
-      if (h.done || waited >= maxChunks) done = true;
-    }
-  }
-  ESF_CUDA(cudaStreamSynchronize(st));
-  ESF_CUDA(cudaMemcpy(&h, dst, sizeof h, cudaMemcpyDeviceToHost));
-  *out = h;
-  return ESF_OK;
+  return run_graph_solve(w->hst, w->ev, dst, w->gFirst[slot], w->gChunk[slot], w->kFirst[slot],
+                         w->kChunk[slot], maxIt, st, out);
 }
 
 esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const int* nbr,
@@ -1296,8 +1335,8 @@ esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const in
   ESF_LAUNCH_CHECK();
   if (precision == ESF_FP64) {
     PcrState h;
-    esf_status e = solid_pcr<double>(S, blocks, nbr, w->invd, b, x, w->r, w->d, w->Ap, w->s,
-                                     w->partial, w->st, eps, maxIt, st, &h, 0, w->hst, w->ev);
+    esf_status e = solid_pcr_graph<double>(w, 0, S, blocks, nbr, w->invd, b, x, w->r, w->d, w->Ap, w->s,
+                                           w->st, eps, maxIt, st, &h, 0);
     if (e) return e;
     if (iters) *iters = h.iter;
     if (converged) *converged = h.converged;
@@ -1342,9 +1381,9 @@ esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const in
     }
     if (ref == maxRefine || total >= maxIt) break;
     PcrState hi;
-    esf_status e = solid_pcr<float>(S, w->blocks32, nbr, w->invd32, w->b32, w->x32, w->r32, w->d32,
-                                    w->Ap32, w->s32, w->partial, w->st32, innerEps, maxIt - total,
-                                    st, &hi, 1, w->hst, w->ev);
+    esf_status e = solid_pcr_graph<float>(w, 1, S, w->blocks32, nbr, w->invd32, w->b32, w->x32, w->r32,
+                                          w->d32, w->Ap32, w->s32, w->st32, innerEps, maxIt - total,
+                                          st, &hi, 1);
     if (e) return e;
     total += hi.iter;
     if (hi.status) {
