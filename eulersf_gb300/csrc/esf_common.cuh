@@ -113,6 +113,14 @@ struct PcrState {
   unsigned int ticket[4];
 };
 
+// Solid system layout ("sliced"): the 27 neighbour 3x3 blocks of solid node a,
+// entry je = 9 j + e, live at ((a / 32) * 243 + je) * 32 + a % 32, and the
+// neighbour index of block j at ((a / 32) * 27 + j) * 32 + a % 32, so a warp's
+// 32 rows read one contiguous region. Arrays hold S rounded up to 32 rows.
+ESF_HD long long blk_at(long long a, int je) { return (((a >> 5) * 243 + je) << 5) + (a & 31); }
+ESF_HD long long nbr_at(long long a, int j) { return (((a >> 5) * 27 + j) << 5) + (a & 31); }
+ESF_HD long long rows32(long long S) { return (S + 31) & ~31LL; }
+
 // Block partial sums live in a scratch array sized for the largest grid; the
 // last block of each kernel folds them in block order (deterministic).
 #define ESF_MAX_PARTIALS 65536

@@ -1427,8 +1427,7 @@ __global__ void k_assemble(GridDev g, SolidDev s, const int* sdof, const long lo
         }
       }
     }
-    // entry-major layout: blocks[(j * 9 + e) * S + a]
-    for (int e = 0; e < 9; e++) blocks[((long long)j * 9 + e) * S + a] = present ? blk[e] * scale : 0.0;
+    for (int e = 0; e < 9; e++) blocks[blk_at(a, 9 * j + e)] = present ? blk[e] * scale : 0.0;
     if (j == 13) {
       present = true;  // coeffRef(i, i) creates the diagonal entries
       // force: cells containing n in increasing index, corner ia
@@ -1442,7 +1441,7 @@ __global__ void k_assemble(GridDev g, SolidDev s, const int* sdof, const long lo
       }
       for (int r = 0; r < 3; r++) force[3 * a + r] = f[r];
     }
-    nbr[(long long)j * S + a] = present ? mdof : -1;
+    nbr[nbr_at(a, j)] = present ? mdof : -1;
     unsigned int bit = present ? (1u << j) : 0u;
     if (bit) atomicOr((unsigned int*)&mask[a], bit);
   }
@@ -1462,7 +1461,7 @@ __global__ void k_add_diag(long long S, const double* damped, double* blocks, do
   FOR_N(3 * S, i) {
     long long a = i / 3;
     int r = (int)(i % 3);
-    double* e = blocks + (13LL * 9 + 4 * r) * S + a;
+    double* e = blocks + blk_at(a, 13 * 9 + 4 * r);
     *e = *e + damped[i];
     diag[i] = *e;
   }

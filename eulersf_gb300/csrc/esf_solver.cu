@@ -1100,21 +1100,22 @@ __global__ void __launch_bounds__(VT) solid_spmv(long long S, const T* __restric
   T accT = 0;
   for (long long a = blockIdx.x * (long long)VT + threadIdx.x; a < S; a += (long long)gridDim.x * VT) {
     T y0 = 0, y1 = 0, y2 = 0;
-    // blocks are stored entry-major, B[(j * 9 + e) * S + a]: consecutive
-    // threads read consecutive words
-    const int* nb = nbr + a;
+    // sliced layout (blk_at/nbr_at): entry je of row a at base + je * 32, so
+    // a warp reads 128 contiguous bytes per entry from one region
+    const int* nb = nbr + nbr_at(a, 0);
+    const T* B0 = blocks + blk_at(a, 0);
     // unrolled by rows of the 3x3x3 neighbourhood so that the loads of nine
     // blocks are in flight together; absent neighbours (m < 0) are skipped,
     // keeping the summation order of the assembled matrix
 #pragma unroll 9
     for (int j = 0; j < 27; j++) {
-      const int m = __ldg(nb + (long long)j * S);
+      const int m = __ldg(nb + 32 * j);
       if (m >= 0) {
         const T v0 = in[3 * (long long)m], v1 = in[3 * (long long)m + 1], v2 = in[3 * (long long)m + 2];
-        const T* Bj = blocks + (long long)j * 9 * S + a;
-        y0 += Bj[0] * v0 + Bj[S] * v1 + Bj[2 * S] * v2;
-        y1 += Bj[3 * S] * v0 + Bj[4 * S] * v1 + Bj[5 * S] * v2;
-        y2 += Bj[6 * S] * v0 + Bj[7 * S] * v1 + Bj[8 * S] * v2;
+        const T* Bj = B0 + 32 * 9 * j;
+        y0 += Bj[0] * v0 + Bj[32] * v1 + Bj[64] * v2;
+        y1 += Bj[96] * v0 + Bj[128] * v1 + Bj[160] * v2;
+        y2 += Bj[192] * v0 + Bj[224] * v1 + Bj[256] * v2;
       }
     }
     T y[3] = {y0, y1, y2};
@@ -1209,7 +1210,7 @@ esf_status solid_work_alloc(SolidWork** out, long long S, int mixed) {
   for (int i = 0; i < 4; i++) ESF_CUDA(cudaEventCreateWithFlags(&w->ev[i], cudaEventDisableTiming));
   ESF_CUDA(cudaStreamCreateWithFlags(&w->capStream, cudaStreamNonBlocking));
   if (mixed) {
-    ESF_CUDA(cudaMalloc(&w->blocks32, w->cap * 243 * 4));
+    ESF_CUDA(cudaMalloc(&w->blocks32, rows32(w->cap) * 243 * 4));
     ESF_CUDA(cudaMalloc(&w->x32, n * 4));
     ESF_CUDA(cudaMalloc(&w->r32, n * 4));
     ESF_CUDA(cudaMalloc(&w->d32, n * 4));
@@ -1345,7 +1346,8 @@ esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const in
     return h.status ? (esf_status)h.status : ESF_OK;
   }
   // mixed: FP32 blocks; x starts at 0 as in the assembled reference variant
-  ESF_COUNTED convert_vec<double, float><<<vec_blocks(S * 243), VT, 0, st>>>(S * 243, blocks, w->blocks32);
+  ESF_COUNTED convert_vec<double, float><<<vec_blocks(rows32(S) * 243), VT, 0, st>>>(rows32(S) * 243, blocks,
+                                                                                   w->blocks32);
   ESF_CUDA(cudaMemsetAsync(x, 0, n * 8, st));
   double bnorm2 = 0;
   {

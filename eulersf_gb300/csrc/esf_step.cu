@@ -743,8 +743,8 @@ static esf_status solid_system(esf_scene* sc, double* energyOut) {
   TRY(sc->solidPC.ensure((3 * S + 1) * 8));
   TRY(sc->solidB1.ensure((3 * S + 1) * 8));
   TRY(sc->sysDiag.ensure((3 * S + 1) * 8));
-  TRY(sc->blocks.ensure((243 * S + 1) * 8));
-  TRY(sc->nbr.ensure((27 * S + 1) * 4));
+  TRY(sc->blocks.ensure((243 * rows32(S) + 1) * 8));
+  TRY(sc->nbr.ensure((27 * rows32(S) + 1) * 4));
   TRY(sc->mask.ensure((S + 1) * 4));
   ESF_CUDA(cudaMemsetAsync(sc->solidF.p, 0, 3 * S * 8 + 8, st));
   ESF_CUDA(cudaMemsetAsync(sc->solidMv.p, 0, 3 * S * 8 + 8, st));
@@ -1214,11 +1214,11 @@ extern "C" esf_status esf_get_field(esf_scene* s, esf_field f, int si, void* hos
   }
   if (r.kind == 5) {  // system blocks: device entry-major -> [node][27][3][3]
     const long long S = s->S;
-    std::vector<double> tmp(243 * S);
+    std::vector<double> tmp(243 * rows32(S));
     if (S) ESF_CUDA(cudaMemcpy(tmp.data(), r.dev, tmp.size() * 8, cudaMemcpyDeviceToHost));
     double* o = (double*)host;
     for (long long a = 0; a < S; a++)
-      for (int je = 0; je < 243; je++) o[243 * a + je] = tmp[je * S + a];
+      for (int je = 0; je < 243; je++) o[243 * a + je] = tmp[blk_at(a, je)];
     return ESF_OK;
   }
   if (r.kind == 4) {  // _gridIdxToSolutionIdx (COUPLED_INTEGRATOR_3D.cpp:123-131)
