@@ -271,27 +271,40 @@ def ours(args):
            "what": "the timed steps themselves, each with the intensity field copied in and the "
                    "velocity field copied out through pinned host buffers (esf_set_field, esf_step, "
                    "esf_get_field)"}
-    # ---- dominant kernel: fused update + stencil + dot of the pressure PCR
+    # ---- dominant kernel of the pressure PCR: the one-pass FP32 iteration
+    # (mixed, rows a multiple of 4 floats) or the update + stencil + dot kernel
     upd, axpy = C.c_double(), C.c_double()
     stt = lib.esf_time_pressure_kernels(I._h, 20, C.byref(upd), C.byref(axpy))
     R = desc.N ** 3
     w = 4 if prec == abi.ESF_MIXED else 8
     peak, peak_kind = read_peaks()
-    algo = 10 * w * R  # P2 + P3 of the 17.6-word per-iteration model
+    one_pass = stt == 0 and w == 4 and axpy.value == 0.0
+    # algorithmic words per row of the 17.6-word per-iteration model: a whole
+    # iteration without the residual check (P1 + P2 + P3) for the one-pass
+    # kernel, P2 + P3 for the update kernel; and the words each must move
+    words, moved = (17, 12) if one_pass else (10, 8)
+    algo = words * w * R
     achieved = algo / (upd.value * 1e-3) / 1e9 if stt == 0 and upd.value > 0 else None
+    moved_gbs = moved * w * R / (upd.value * 1e-3) / 1e9 if achieved else None
     traffic = None
     tp = os.path.join(ROOT, "profiles", "pressure_update_traffic.json")
     if os.path.exists(tp):
         with open(tp) as f:
             tj = json.load(f)
-        traffic = tj.get(f"{'fp32' if w == 4 else 'fp64'}_{desc.N}")
-    kname = ("pressure_update_tma" if (w == 4 and desc.N % 4 == 0) else
-             f"pressure_stencil<{'float' if w == 4 else 'double'}, update>")
+        traffic = tj.get(f"{'fp32' if w == 4 else 'fp64'}_{desc.N}{'_one_pass' if one_pass else ''}")
+    if one_pass:
+        kname = "pcr_iteration_fused"
+    else:
+        kname = ("pressure_update_tma" if (w == 4 and desc.N % 4 == 0) else
+                 f"pressure_stencil<{'float' if w == 4 else 'double'}, update>")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                 "peak_kind": peak_kind, "kernel": kname,
                 "kernel_ms": upd.value, "axpy_kernel_ms": axpy.value,
-                "algorithmic_bytes_per_launch": algo}
+                "algorithmic_bytes_per_launch": algo,
+                "words_per_row": {"algorithmic": words, "moved": moved},
+                "moved_bytes_per_launch": moved * w * R,
+                "frac_of_moved": (moved_gbs / peak) if moved_gbs else None}
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

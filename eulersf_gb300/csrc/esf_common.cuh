@@ -110,6 +110,7 @@ struct PcrState {
   int rebase;        // 1: next update reduction replaces the residual (keeps d)
   int iter0;         // iteration of the last replacement
   int cap;           // inner mode: iterations between replacements (0 = none)
+  int pp;            // one-pass FP32 iteration: which buffer set holds r, t, q
   unsigned int ticket[4];
 };
 

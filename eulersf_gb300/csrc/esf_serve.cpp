@@ -181,8 +181,9 @@ extern "C" size_t esf_scene_footprint(const esf_grid* g, const esf_params* p, in
   const double R = (double)(g->xRes - 1) * (g->yRes - 1) * (g->zRes - 1);
   // integrator and per-solid node fields, pressure vectors (FP64 + FP32);
   // coefficients fitted to scenes measured on GB300 at 48^3, 96^3 and 160^3
-  // (estimate / measured = 1.07, 1.00, 0.99 for a 0.2-radius ball)
-  double bytes = T * (520.0 + 240.0 * ns) + R * 180.0;
+  // (estimate / measured = 1.07, 1.00, 0.99 for a 0.2-radius ball), plus
+  // the one-pass FP32 iteration's second set of r, t, q (12 bytes a row)
+  double bytes = T * (520.0 + 240.0 * ns) + R * 192.0;
   for (int i = 0; i < ns && solids; i++) {
     // solid nodes and particles from the scaled mesh's bounding box
     const esf_solid_desc& d = solids[i];

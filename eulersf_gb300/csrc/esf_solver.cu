@@ -341,6 +341,7 @@ __global__ void __launch_bounds__(NT) pressure_stencil(GridDev g, StencilArgs<T>
 }
 
 #include "esf_tma.cuh"
+#include "esf_pcr_fused.cuh"
 
 // ------------------------------------------------------- vector kernels
 constexpr int VT = 256;
@@ -519,6 +520,11 @@ struct PressureWork {
   int mpitch;
   TmaMaps tmaps;
   bool tmaOk;
+  // one-pass FP32 iteration: second buffer set of r, t = s/diag, q = Ap/diag
+  // (the first set is r32, s32, Ap32)
+  float *r32b, *s32b, *Ap32b;
+  FusedMaps fmaps;
+  bool fusedOk;
 };
 
 // z-chunk depth: deep enough to amortise the two halo layers, shallow
@@ -577,6 +583,9 @@ esf_status pressure_work_alloc(PressureWork** out, const GridDev& g, int mixed) 
     ESF_CUDA(cudaMalloc(&w->minv32, g.T * 4));
     w->mpitch = (g.X + 3) / 4 * 4;
     ESF_CUDA(cudaMalloc(&w->minv32p, (size_t)w->mpitch * g.Y * g.Z * 4));
+    ESF_CUDA(cudaMalloc(&w->r32b, R * 4));
+    ESF_CUDA(cudaMalloc(&w->s32b, R * 4));
+    ESF_CUDA(cudaMalloc(&w->Ap32b, R * 4));
   }
   ESF_CUDA(cudaMalloc(&w->partial, ESF_MAX_PARTIALS * 8));
   ESF_CUDA(cudaMalloc(&w->st, sizeof(PcrState)));
@@ -596,6 +605,7 @@ void pressure_work_free(PressureWork* w) {
   cudaFree(w->r); cudaFree(w->d); cudaFree(w->Ap); cudaFree(w->s); cudaFree(w->invd);
   cudaFree(w->x32); cudaFree(w->r32); cudaFree(w->d32); cudaFree(w->Ap32); cudaFree(w->s32);
   cudaFree(w->invd32); cudaFree(w->b32); cudaFree(w->minv32); cudaFree(w->minv32p);
+  cudaFree(w->r32b); cudaFree(w->s32b); cudaFree(w->Ap32b);
   cudaFree(w->partial); cudaFree(w->st); cudaFree(w->st32); cudaFree(w->stT);
   if (w->hst) cudaFreeHost(w->hst);
   if (w->gFirst) cudaGraphExecDestroy(w->gFirst);
@@ -644,14 +654,24 @@ static esf_status encode3d(CUtensorMap* m, const void* base, long long w, long l
   return ESF_OK;
 }
 
-// Chooses the FP32 update kernel for the mixed path: the TMA-staged one when
-// the cell rows are a multiple of 4 floats (16-byte row strides) unless
-// ESF_PRESSURE_KERNEL=register asks for the register-prefetch kernel (same
-// bits; kept for comparison). Converts m^-1 into the padded layout and
-// builds the maps once per work.
+// FP32 kernels of the mixed path's inner iterations.
+enum Fp32Path {
+  P32_REGISTER = 0,  // pcr_phase_a + pressure_stencil<float, S_UPDATE>
+  P32_TMA = 1,       // pcr_phase_a + pressure_update_tma (same bits as P32_REGISTER)
+  P32_FUSED = 2      // pcr_iteration_fused: the whole iteration in one pass
+};
+
+// Chooses the FP32 kernels for the mixed path. The TMA kernels need cell
+// rows that are a multiple of 4 floats (16-byte row strides); with them the
+// one-pass iteration is the default, and ESF_PRESSURE_KERNEL=tma or
+// =register selects the two-kernel split with the TMA-staged or the
+// register-prefetch update kernel (those two give the same bits; both kept
+// for comparison). Converts m^-1 into the padded layout and builds the maps
+// once per work.
 static esf_status prepare_tma(PressureWork* w, const GridDev& g, const double* minv64,
-                              cudaStream_t st, const TmaMaps** out) {
+                              cudaStream_t st, const TmaMaps** out, int* path = nullptr) {
   *out = nullptr;
+  if (path) *path = P32_REGISTER;
   const char* pick = getenv("ESF_PRESSURE_KERNEL");
   if (g.cX % 4 != 0 || (pick && strcmp(pick, "register") == 0)) return ESF_OK;
   ESF_COUNTED convert_minv_padded<<<vec_blocks((long long)w->mpitch * g.Y * g.Z), VT, 0, st>>>(
@@ -677,7 +697,69 @@ static esf_status prepare_tma(PressureWork* w, const GridDev& g, const double* m
     w->tmaOk = true;
   }
   *out = &w->tmaps;
+  if (path) *path = P32_TMA;
+  const dim3 gr = tma_grid(g, stencil_cz(g));
+  const bool fits = (long long)gr.x * gr.y * gr.z * FU_SUMS <= ESF_MAX_PARTIALS / 2;
+  if (!path || !fits || (pick && strcmp(pick, "tma") == 0)) return ESF_OK;
+  if (!w->fusedOk) {
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        pcr_iteration_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, FU_SMEM);
+    if (attr != cudaSuccess) {
+      set_error("pcr_iteration_fused: %d bytes of shared memory refused: %s", FU_SMEM,
+                cudaGetErrorString(attr));
+      return ESF_ERR_CUDA;
+    }
+    FusedMaps m;
+    esf_status e;
+    float* rs[2] = {w->r32, w->r32b};
+    float* ts[2] = {w->s32, w->s32b};
+    float* qs[2] = {w->Ap32, w->Ap32b};
+    for (int k = 0; k < 2; k++) {
+      if ((e = encode3d(&m.r[k], rs[k], g.cX, g.cY, g.cZ, TMA_HW, TMA_HH))) return e;
+      if ((e = encode3d(&m.t[k], ts[k], g.cX, g.cY, g.cZ, TMA_HW, TMA_HH))) return e;
+      if ((e = encode3d(&m.q[k], qs[k], g.cX, g.cY, g.cZ, TMA_HW, TMA_HH))) return e;
+    }
+    if ((e = encode3d(&m.iv, w->invd32, g.cX, g.cY, g.cZ, TXW, TY))) return e;
+    if ((e = encode3d(&m.x, w->x32, g.cX, g.cY, g.cZ, TXW, TY))) return e;
+    if ((e = encode3d(&m.d, w->d32, g.cX, g.cY, g.cZ, TXW, TY))) return e;
+    if ((e = encode3d(&m.m, w->minv32p, w->mpitch, g.Y, g.Z, TMA_NW, TMA_NH))) return e;
+    w->fmaps = m;
+    w->fusedOk = true;
+  }
+  *path = P32_FUSED;
   return ESF_OK;
+}
+
+// The one-pass FP32 iteration on the work's buffers.
+struct FusedKernels {
+  GridDev g;
+  const FusedMaps* tm;
+  FusedPtrs p;
+  double* partial;
+  PcrState* st;
+  void iteration(cudaStream_t cs) const {
+    const int cz = stencil_cz(g);
+    ESF_COUNTED pcr_iteration_fused<<<tma_grid(g, cz), NT, FU_SMEM, cs>>>(g, *tm, p, partial, st, cz);
+  }
+  // graph capture interface of PressureKernels (inner solves only)
+  void setup_warm(cudaStream_t) const {}
+  void setup_zero(cudaStream_t) const {}
+  void chunk(cudaStream_t cs, int n, bool) const {
+    for (int k = 0; k < n; k++) iteration(cs);
+  }
+};
+static FusedKernels fused_kernels(PressureWork* w, const GridDev& g, PcrState* st) {
+  FusedKernels k;
+  k.g = g;
+  k.tm = &w->fmaps;
+  k.p.r[0] = w->r32; k.p.r[1] = w->r32b;
+  k.p.t[0] = w->s32; k.p.t[1] = w->s32b;
+  k.p.q[0] = w->Ap32; k.p.q[1] = w->Ap32b;
+  k.p.x = w->x32;
+  k.p.d = w->d32;
+  k.partial = w->partial;
+  k.st = st;
+  return k;
 }
 
 // Enqueue iterations of the PCR loop for precision T on stream s.
@@ -870,20 +952,39 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
   // node-collocated grid).
   ESF_COUNTED convert_vec<double, float><<<vec_blocks(g.T), VT, 0, st>>>(g.T, minv64, w->minv32);
   const TmaMaps* tma = nullptr;
+  int path = P32_REGISTER;
   {
-    esf_status e = prepare_tma(w, g, minv64, st, &tma);
+    esf_status e = prepare_tma(w, g, minv64, st, &tma, &path);
     if (e) return e;
   }
   PressureKernels<float> k32{g, w->minv32, w->invd32, w->b32, w->x32, w->r32, w->d32, w->Ap32,
                              w->s32, w->partial, w->st32};
   k32.tma = tma;
-  const void* key[8] = {w->minv32, w->invd32, w->b32, w->x32, tma, nullptr, nullptr, nullptr};
+  const bool fused = path == P32_FUSED;
+  const FusedKernels kf = fused_kernels(w, g, w->st32);
+  const void* key[8] = {w->minv32, w->invd32, w->b32, w->x32, tma, &w->fmaps,
+                        reinterpret_cast<const void*>(static_cast<uintptr_t>(path + 1)), nullptr};
   if (!w->graphsFor32 || memcmp(key, w->keyB, sizeof key) != 0) {
-    esf_status e = capture(w->capStream, k32, false, false, &w->gChunk32, &w->kChunk32);
+    esf_status e = fused ? capture(w->capStream, kf, false, false, &w->gChunk32, &w->kChunk32)
+                         : capture(w->capStream, k32, false, false, &w->gChunk32, &w->kChunk32);
     if (e) return e;
     memcpy(w->keyB, key, sizeof key);
     w->graphsFor32 = true;
   }
+  // start of an inner solve: zero directions (and, one-pass, t of the first
+  // buffer set, which the set-up pass reads), then the set-up pass s = A r
+  auto inner_setup = [&]() -> esf_status {
+    ESF_CUDA(cudaMemsetAsync(w->d32, 0, g.R * 4, st));
+    ESF_CUDA(cudaMemsetAsync(w->Ap32, 0, g.R * 4, st));
+    if (fused) {
+      ESF_CUDA(cudaMemsetAsync(w->s32, 0, g.R * 4, st));
+      kf.iteration(st);
+    } else {
+      k32.update(st);  // s = A r, delta (set-up: alpha = 0)
+    }
+    ESF_LAUNCH_CHECK();
+    return ESF_OK;
+  };
   // ||b||
   {
     esf_status e = init_state(w->st, eps, maxIt, st);
@@ -928,8 +1029,6 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
     conv = 1;
   } else {
     ESF_CUDA(cudaMemsetAsync(w->x32, 0, g.R * 4, st));
-    ESF_CUDA(cudaMemsetAsync(w->d32, 0, g.R * 4, st));
-    ESF_CUDA(cudaMemsetAsync(w->Ap32, 0, g.R * 4, st));
     {
       PcrState h;
       memset(&h, 0, sizeof h);
@@ -940,8 +1039,10 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
       ESF_CUDA(cudaMemcpyAsync(w->st32, &h, sizeof h, cudaMemcpyHostToDevice, st));
       ESF_CUDA(cudaStreamSynchronize(st));
     }
-    k32.update(st);  // s = A r, delta (set-up: alpha = 0)
-    ESF_LAUNCH_CHECK();
+    {
+      esf_status e = inner_setup();
+      if (e) return e;
+    }
     const bool trace = getenv("ESF_TRACE") != nullptr;
     auto t0 = std::chrono::steady_clock::now();
     for (ref = 0; ref < maxRefine; ref++) {
@@ -975,10 +1076,9 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
       }
       if (total >= maxIt) break;
       // restart the inner recurrence from the new residual (iteration count
-      // carries over)
-      ESF_CUDA(cudaMemsetAsync(w->d32, 0, g.R * 4, st));
-      ESF_CUDA(cudaMemsetAsync(w->Ap32, 0, g.R * 4, st));
+      // carries over; the residual is in the first buffer set)
       hi.done = 0;
+      hi.pp = 0;
       hi.converged = 0;
       hi.alpha = 0.0;
       hi.beta = 0.0;
@@ -987,8 +1087,8 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
       memset(hi.ticket, 0, sizeof hi.ticket);
       ESF_CUDA(cudaMemcpyAsync(w->st32, &hi, sizeof hi, cudaMemcpyHostToDevice, st));
       ESF_CUDA(cudaStreamSynchronize(st));
-      k32.update(st);
-      ESF_LAUNCH_CHECK();
+      e = inner_setup();
+      if (e) return e;
     }
   }
   if (!conv && ref >= maxRefine && status == ESF_OK && total < maxIt) {
@@ -1059,6 +1159,46 @@ static esf_status time_kernels_t(PressureWork* w, const GridDev& g, const T* min
   return ESF_OK;
 }
 
+// The one-pass iteration timed on an inner solve of A e = b from e = 0 (the
+// set-up pass and one iteration untimed, then `reps` iterations; the
+// tolerance is 0, so every launch does a full iteration).
+static esf_status time_fused(PressureWork* w, const GridDev& g, int reps, double* ms,
+                             cudaStream_t st) {
+  const long long R = g.R;
+  // r = b/diag in the first buffer set, x = d = q = 0
+  ESF_COUNTED pcr_zero_start<float><<<vec_blocks(R), VT, 0, st>>>(R, w->b32, w->invd32, w->x32, w->r32,
+                                                               w->d32, w->Ap32, w->partial, w->stT);
+  ESF_CUDA(cudaMemsetAsync(w->s32, 0, R * 4, st));
+  PcrState h;
+  memset(&h, 0, sizeof h);
+  h.maxIt = 1 << 30;
+  h.setup = 1;
+  h.inner = 1;
+  ESF_CUDA(cudaMemcpyAsync(w->stT, &h, sizeof h, cudaMemcpyHostToDevice, st));
+  ESF_CUDA(cudaStreamSynchronize(st));
+  const FusedKernels k = fused_kernels(w, g, w->stT);
+  k.iteration(st);
+  k.iteration(st);
+  cudaEvent_t e0, e1;
+  ESF_CUDA(cudaEventCreate(&e0));
+  ESF_CUDA(cudaEventCreate(&e1));
+  ESF_CUDA(cudaEventRecord(e0, st));
+  for (int i = 0; i < reps; i++) k.iteration(st);
+  ESF_CUDA(cudaEventRecord(e1, st));
+  ESF_CUDA(cudaEventSynchronize(e1));
+  float t = 0;
+  cudaEventElapsedTime(&t, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ESF_CUDA(cudaMemcpy(&h, w->stT, sizeof h, cudaMemcpyDeviceToHost));
+  if (h.done || h.status) {
+    set_error("pressure kernel timer: the timed inner solve stopped early (status %d)", h.status);
+    return ESF_ERR_NUMERIC;
+  }
+  *ms = t / reps;
+  return ESF_OK;
+}
+
 esf_status pressure_time_kernels(PressureWork* w, const GridDev& g, const double* minv64,
                                  const double* diag64, const double* b, const double* x,
                                  int precision, int reps, double* update_ms, double* axpy_ms,
@@ -1071,8 +1211,13 @@ esf_status pressure_time_kernels(PressureWork* w, const GridDev& g, const double
     ESF_COUNTED convert_vec<double, float><<<vec_blocks(g.R), VT, 0, st>>>(g.R, b, w->b32);
     ESF_LAUNCH_CHECK();
     const TmaMaps* tma = nullptr;
-    esf_status e = prepare_tma(w, g, minv64, st, &tma);
+    int path = P32_REGISTER;
+    esf_status e = prepare_tma(w, g, minv64, st, &tma, &path);
     if (e) return e;
+    if (path == P32_FUSED) {
+      *axpy_ms = 0.0;
+      return time_fused(w, g, reps, update_ms, st);
+    }
     return time_kernels_t<float>(w, g, w->minv32, w->invd32, w->b32, w->x32, w->r32, w->d32,
                                  w->Ap32, w->s32, reps, update_ms, axpy_ms, st, tma);
   }

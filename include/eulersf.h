@@ -324,10 +324,12 @@ esf_status esf_server_destroy(esf_server* server);
 /* Number of kernels this library has launched in this process (graph
  * replays count every kernel node). */
 uint64_t esf_kernel_launches(void);
-/* Average device time (ms) of the two pressure-PCR kernels on the scene's
- * current pressure problem, timed with CUDA events on the scene's stream:
- * the fused update+stencil+dot kernel and the axpy+norm kernel, at the
- * scene's precision (FP32 for ESF_MIXED). Leaves the scene's state intact. */
+/* Average device time (ms) of the pressure-PCR kernels on the scene's
+ * current pressure problem, timed with CUDA events on the scene's stream, at
+ * the scene's precision (FP32 for ESF_MIXED): the fused update+stencil+dot
+ * kernel and the axpy+norm kernel; where one kernel does the whole FP32
+ * iteration (ESF_MIXED, cell rows a multiple of 4), update_ms is that kernel
+ * and axpy_ms is 0. Leaves the scene's state intact. */
 esf_status esf_time_pressure_kernels(esf_scene* scene, int reps, double* update_ms,
                                      double* axpy_ms);
 
