@@ -223,9 +223,10 @@ __global__ void __launch_bounds__(NT, 4) pcr_iteration_fused(GridDev g, const __
             make_float2(__fmaf_rn(alpha, dn0, xv.x), __fmaf_rn(alpha, dn1, xv.y));
         *reinterpret_cast<float2*>(rOut + o) = make_float2(v0, v1);
         *reinterpret_cast<float2*>(qOut + o) = make_float2(qn0, qn1);
-        // (Ap, q) = (q diag, q)
-        if (iv.x > 0.0f) sOm += (qn0 * qn0) * __frcp_rn(iv.x);
-        if (iv.y > 0.0f) sOm += (qn1 * qn1) * __frcp_rn(iv.y);
+        // (Ap, q) = (q diag, q); an approximate quotient is plenty for a sum
+        // that only sets the step length
+        if (iv.x > 0.0f) sOm += __fdividef(qn0 * qn0, iv.x);
+        if (iv.y > 0.0f) sOm += __fdividef(qn1 * qn1, iv.y);
         qCur0 = qn0;
         qCur1 = qn1;
         ivCur0 = iv.x;

@@ -538,6 +538,16 @@ static int stencil_cz(const GridDev& g) {
   if (cz > g.cZ) cz = g.cZ;
   return (int)cz;
 }
+// z-chunk depth of the one-pass iteration (ESF_PRESSURE_CZ overrides it, for
+// tuning); its reductions do not follow the register kernel's block grid
+static int fused_cz(const GridDev& g) {
+  const char* e = getenv("ESF_PRESSURE_CZ");
+  if (e) {
+    const int v = atoi(e);
+    if (v >= 2) return v < g.cZ ? v : g.cZ;
+  }
+  return stencil_cz(g);
+}
 template <typename T>
 static dim3 stencil_grid(const GridDev& g) {
   int cz = stencil_cz(g);
@@ -698,7 +708,7 @@ static esf_status prepare_tma(PressureWork* w, const GridDev& g, const double* m
   }
   *out = &w->tmaps;
   if (path) *path = P32_TMA;
-  const dim3 gr = tma_grid(g, stencil_cz(g));
+  const dim3 gr = tma_grid(g, fused_cz(g));
   const bool fits = (long long)gr.x * gr.y * gr.z * FU_SUMS <= ESF_MAX_PARTIALS / 2;
   if (!path || !fits || (pick && strcmp(pick, "tma") == 0)) return ESF_OK;
   if (!w->fusedOk) {
@@ -738,7 +748,7 @@ struct FusedKernels {
   double* partial;
   PcrState* st;
   void iteration(cudaStream_t cs) const {
-    const int cz = stencil_cz(g);
+    const int cz = fused_cz(g);
     ESF_COUNTED pcr_iteration_fused<<<tma_grid(g, cz), NT, FU_SMEM, cs>>>(g, *tm, p, partial, st, cz);
   }
   // graph capture interface of PressureKernels (inner solves only)
@@ -963,7 +973,8 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
   const bool fused = path == P32_FUSED;
   const FusedKernels kf = fused_kernels(w, g, w->st32);
   const void* key[8] = {w->minv32, w->invd32, w->b32, w->x32, tma, &w->fmaps,
-                        reinterpret_cast<const void*>(static_cast<uintptr_t>(path + 1)), nullptr};
+                        reinterpret_cast<const void*>(static_cast<uintptr_t>(path + 1)),
+                        reinterpret_cast<const void*>(static_cast<uintptr_t>(fused_cz(g)))};
   if (!w->graphsFor32 || memcmp(key, w->keyB, sizeof key) != 0) {
     esf_status e = fused ? capture(w->capStream, kf, false, false, &w->gChunk32, &w->kChunk32)
                          : capture(w->capStream, k32, false, false, &w->gChunk32, &w->kChunk32);
