@@ -13,6 +13,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <chrono>
+#include <cmath>
 #include <type_traits>
 
 #include <vector>
@@ -538,15 +539,48 @@ static int stencil_cz(const GridDev& g) {
   if (cz > g.cZ) cz = g.cZ;
   return (int)cz;
 }
-// z-chunk depth of the one-pass iteration (ESF_PRESSURE_CZ overrides it, for
-// tuning); its reductions do not follow the register kernel's block grid
+// z-chunk depth of the one-pass iteration: the depth in [4, 64] that best
+// trades the last wave's idle block slots (blocks / slots against its
+// ceiling) for the two halo layers each chunk re-reads, scored as
+// fill x cz / (cz + 4) (at 256^3 this picks 29: 1152 blocks, 1.89 waves of
+// 608 slots; a sweep there measured 148 us per launch at 29, 155-157 us at
+// 19, 32 and 64, and 165-172 us at 8, 10, 43 and 52). ESF_PRESSURE_CZ
+// overrides it, for tuning. The reductions do not follow the register
+// kernel's block grid, so any depth gives a valid sum order.
 static int fused_cz(const GridDev& g) {
   const char* e = getenv("ESF_PRESSURE_CZ");
   if (e) {
     const int v = atoi(e);
     if (v >= 2) return v < g.cZ ? v : g.cZ;
   }
-  return stencil_cz(g);
+  static const int slots = [] {
+    int dev = 0, sms = 152, per = 4;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pcr_iteration_fused, NT, FU_SMEM) !=
+            cudaSuccess ||
+        per < 1)
+      per = 4;
+    return sms * per;
+  }();
+  const long long cols = (long long)((g.cX + TXW - 1) / TXW) * ((g.cY + TY - 1) / TY);
+  // over chunk counts n, each with its balanced depth ceil(cZ / n)
+  int best = g.cZ < 4 ? g.cZ : 4;
+  double bestScore = -1.0;
+  for (int n = 1; n <= g.cZ; n++) {
+    const int cz = (g.cZ + n - 1) / n;
+    if (cz > 64) continue;
+    if (cz < 4) break;
+    const long long blocks = cols * ((g.cZ + cz - 1) / cz);
+    const double waves = (double)blocks / slots;
+    const double fill = waves / std::ceil(waves);
+    const double score = fill * cz / (cz + 4.0);
+    if (score > bestScore + 1e-12) {
+      bestScore = score;
+      best = cz;
+    }
+  }
+  return best;
 }
 template <typename T>
 static dim3 stencil_grid(const GridDev& g) {
