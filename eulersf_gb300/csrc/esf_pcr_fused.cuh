@@ -61,7 +61,6 @@ constexpr int FU_OFF_C = FU_OFF_B + TW_NP * NYN * 4;
 constexpr int FU_OFF_RED = (FU_OFF_C + TW_NP * NYN * 4 + 15) / 16 * 16;
 constexpr int FU_SMEM = FU_OFF_RED + 32 * 8;  // about 47 KB: four blocks per SM
 constexpr int FU_SUMS = 4;                    // delta, mu, nu, omega
-constexpr int FU_PREFETCH = 2;                // L2 prefetch distance beyond the ring, in steps
 
 // Scalars after a fused pass: totals of (r', s'), (s', t'), (s', q), (Ap, q).
 __device__ __forceinline__ void finish_fused(PcrState* st, double dl, double mu, double nu,
@@ -142,26 +141,10 @@ __global__ void __launch_bounds__(NT, 4) pcr_iteration_fused(GridDev g, const __
     }
     if (node) tma_load_3d(s + FU_OFF_M, &tm.m, x0, y0, kk, b);
   };
-  // L2 prefetch of the inputs of step i (issued FU_PREFETCH steps before its
-  // loads, so that they find the layer in L2)
-  auto prefetch = [&](int i) {
-    const int kk = z0 - 1 + i;
-    if (kk < 0 || kk >= g.cZ) return;
-    tma_prefetch_3d(mR, x0 - 4, y0 - 1, kk);
-    tma_prefetch_3d(mT, x0 - 4, y0 - 1, kk);
-    tma_prefetch_3d(mQ, x0 - 4, y0 - 1, kk);
-    if (kk >= z0 && kk < z1) {
-      tma_prefetch_3d(&tm.iv, x0, y0, kk);
-      tma_prefetch_3d(&tm.x, x0, y0, kk);
-      tma_prefetch_3d(&tm.d, x0, y0, kk);
-    }
-    if (kk >= z0) tma_prefetch_3d(&tm.m, x0, y0, kk);
-  };
   if (tid == 0) {
     for (int i = 0; i < TMA_STAGES; i++) mbar_init(&bar[i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     for (int i = 0; i < TMA_STAGES && i < nsteps; i++) issue(i);
-    for (int i = TMA_STAGES; i < TMA_STAGES + FU_PREFETCH && i < nsteps; i++) prefetch(i);
   }
   __syncthreads();
 
@@ -302,7 +285,6 @@ __global__ void __launch_bounds__(NT, 4) pcr_iteration_fused(GridDev g, const __
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       issue(i + TMA_STAGES);
       issued = i + TMA_STAGES + 1;
-      if (i + TMA_STAGES + FU_PREFETCH < nsteps) prefetch(i + TMA_STAGES + FU_PREFETCH);
     }
     // (c) s' and t' = s'/diag at the tile's cells of layer kk-1
     if (kk >= z0 + 1 && cin) {

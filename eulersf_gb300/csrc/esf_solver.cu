@@ -526,7 +526,118 @@ struct PressureWork {
   float *r32b, *s32b, *Ap32b;
   FusedMaps fmaps;
   bool fusedOk;
+  // FP32 vectors mapped through the driver's virtual-memory calls (see
+  // vec_alloc), released by pressure_work_free
+  struct Mapped {
+    CUdeviceptr p;
+    size_t size;
+    CUmemGenericAllocationHandle h;
+  } mapped[16];
+  int nmapped;
 };
+
+// ---- FP32 vectors with an explicit compression attribute. With
+// ESF_VMM_COMP=none or =generic the inner-solve vectors are created with
+// cuMemCreate (compression type as named) and mapped with cuMemMap;
+// otherwise they come from cudaMalloc.
+struct VmmApi {
+  PFN_cuMemGetAllocationGranularity_v10020 gran;
+  PFN_cuMemCreate_v10020 create;
+  PFN_cuMemAddressReserve_v10020 reserve;
+  PFN_cuMemMap_v10020 map;
+  PFN_cuMemSetAccess_v10020 access;
+  PFN_cuMemUnmap_v10020 unmap;
+  PFN_cuMemRelease_v10020 release;
+  PFN_cuMemAddressFree_v10020 addrFree;
+  bool ok;
+};
+static const VmmApi& vmm_api() {
+  static const VmmApi api = [] {
+    VmmApi a;
+    memset(&a, 0, sizeof a);
+    auto get = [](const char* name, void** fn) {
+      cudaDriverEntryPointQueryResult q;
+      return cudaGetDriverEntryPointByVersion(name, fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+             q == cudaDriverEntryPointSuccess && *fn;
+    };
+    a.ok = get("cuMemGetAllocationGranularity", reinterpret_cast<void**>(&a.gran)) &&
+           get("cuMemCreate", reinterpret_cast<void**>(&a.create)) &&
+           get("cuMemAddressReserve", reinterpret_cast<void**>(&a.reserve)) &&
+           get("cuMemMap", reinterpret_cast<void**>(&a.map)) &&
+           get("cuMemSetAccess", reinterpret_cast<void**>(&a.access)) &&
+           get("cuMemUnmap", reinterpret_cast<void**>(&a.unmap)) &&
+           get("cuMemRelease", reinterpret_cast<void**>(&a.release)) &&
+           get("cuMemAddressFree", reinterpret_cast<void**>(&a.addrFree));
+    return a;
+  }();
+  return api;
+}
+static esf_status vec_alloc(PressureWork* w, float** out, size_t bytes) {
+  const char* comp = getenv("ESF_VMM_COMP");
+  if (!comp || w->nmapped >= 16) {
+    ESF_CUDA(cudaMalloc(out, bytes));
+    return ESF_OK;
+  }
+  const VmmApi& api = vmm_api();
+  if (!api.ok) {
+    set_error("driver virtual-memory entry points are not available");
+    return ESF_ERR_CUDA;
+  }
+  int dev = 0;
+  ESF_CUDA(cudaGetDevice(&dev));
+  CUmemAllocationProp prop;
+  memset(&prop, 0, sizeof prop);
+  prop.type = CU_MEM_ALLOCATION_TYPE_PINNED;
+  prop.location.type = CU_MEM_LOCATION_TYPE_DEVICE;
+  prop.location.id = dev;
+  prop.allocFlags.compressionType =
+      strcmp(comp, "generic") == 0 ? CU_MEM_ALLOCATION_COMP_GENERIC : CU_MEM_ALLOCATION_COMP_NONE;
+  size_t gran = 0;
+  if (api.gran(&gran, &prop, CU_MEM_ALLOC_GRANULARITY_RECOMMENDED) != CUDA_SUCCESS || gran == 0) {
+    set_error("cuMemGetAllocationGranularity failed");
+    return ESF_ERR_CUDA;
+  }
+  const size_t size = (bytes + gran - 1) / gran * gran;
+  PressureWork::Mapped m;
+  m.size = size;
+  if (api.create(&m.h, size, &prop, 0) != CUDA_SUCCESS) {
+    set_error("cuMemCreate of %zu bytes failed", size);
+    return ESF_ERR_CUDA;
+  }
+  if (api.reserve(&m.p, size, 0, 0, 0) != CUDA_SUCCESS) {
+    api.release(m.h);
+    set_error("cuMemAddressReserve failed");
+    return ESF_ERR_CUDA;
+  }
+  CUmemAccessDesc acc;
+  memset(&acc, 0, sizeof acc);
+  acc.location.type = CU_MEM_LOCATION_TYPE_DEVICE;
+  acc.location.id = dev;
+  acc.flags = CU_MEM_ACCESS_FLAGS_PROT_READWRITE;
+  if (api.map(m.p, size, 0, m.h, 0) != CUDA_SUCCESS || api.access(m.p, size, &acc, 1) != CUDA_SUCCESS) {
+    api.unmap(m.p, size);
+    api.addrFree(m.p, size);
+    api.release(m.h);
+    set_error("cuMemMap/cuMemSetAccess failed");
+    return ESF_ERR_CUDA;
+  }
+  w->mapped[w->nmapped++] = m;
+  *out = reinterpret_cast<float*>(m.p);
+  return ESF_OK;
+}
+static void vec_free(PressureWork* w, float* p) {
+  if (!p) return;
+  for (int i = 0; i < w->nmapped; i++)
+    if (reinterpret_cast<float*>(w->mapped[i].p) == p) {
+      const VmmApi& api = vmm_api();
+      api.unmap(w->mapped[i].p, w->mapped[i].size);
+      api.addrFree(w->mapped[i].p, w->mapped[i].size);
+      api.release(w->mapped[i].h);
+      w->mapped[i].p = 0;
+      return;
+    }
+  cudaFree(p);
+}
 
 // z-chunk depth: deep enough to amortise the two halo layers, shallow
 // enough to give every SM several tiles.
@@ -617,19 +728,16 @@ esf_status pressure_work_alloc(PressureWork** out, const GridDev& g, int mixed) 
   ESF_CUDA(cudaMalloc(&w->s, R * 8));
   ESF_CUDA(cudaMalloc(&w->invd, R * 8));
   if (mixed) {
-    ESF_CUDA(cudaMalloc(&w->x32, R * 4));
-    ESF_CUDA(cudaMalloc(&w->r32, R * 4));
-    ESF_CUDA(cudaMalloc(&w->d32, R * 4));
-    ESF_CUDA(cudaMalloc(&w->Ap32, R * 4));
-    ESF_CUDA(cudaMalloc(&w->s32, R * 4));
-    ESF_CUDA(cudaMalloc(&w->invd32, R * 4));
-    ESF_CUDA(cudaMalloc(&w->b32, R * 4));
-    ESF_CUDA(cudaMalloc(&w->minv32, g.T * 4));
     w->mpitch = (g.X + 3) / 4 * 4;
-    ESF_CUDA(cudaMalloc(&w->minv32p, (size_t)w->mpitch * g.Y * g.Z * 4));
-    ESF_CUDA(cudaMalloc(&w->r32b, R * 4));
-    ESF_CUDA(cudaMalloc(&w->s32b, R * 4));
-    ESF_CUDA(cudaMalloc(&w->Ap32b, R * 4));
+    float** vecs[] = {&w->x32, &w->r32, &w->d32, &w->Ap32, &w->s32, &w->invd32,
+                      &w->b32, &w->r32b, &w->s32b, &w->Ap32b};
+    for (float** v : vecs) {
+      esf_status e = vec_alloc(w, v, R * 4);
+      if (e) return e;
+    }
+    esf_status e = vec_alloc(w, &w->minv32p, (size_t)w->mpitch * g.Y * g.Z * 4);
+    if (e) return e;
+    ESF_CUDA(cudaMalloc(&w->minv32, g.T * 4));
   }
   ESF_CUDA(cudaMalloc(&w->partial, ESF_MAX_PARTIALS * 8));
   ESF_CUDA(cudaMalloc(&w->st, sizeof(PcrState)));
@@ -647,9 +755,10 @@ esf_status pressure_work_alloc(PressureWork** out, const GridDev& g, int mixed) 
 void pressure_work_free(PressureWork* w) {
   if (!w) return;
   cudaFree(w->r); cudaFree(w->d); cudaFree(w->Ap); cudaFree(w->s); cudaFree(w->invd);
-  cudaFree(w->x32); cudaFree(w->r32); cudaFree(w->d32); cudaFree(w->Ap32); cudaFree(w->s32);
-  cudaFree(w->invd32); cudaFree(w->b32); cudaFree(w->minv32); cudaFree(w->minv32p);
-  cudaFree(w->r32b); cudaFree(w->s32b); cudaFree(w->Ap32b);
+  for (float* v : {w->x32, w->r32, w->d32, w->Ap32, w->s32, w->invd32, w->b32, w->r32b, w->s32b,
+                   w->Ap32b, w->minv32p})
+    vec_free(w, v);
+  cudaFree(w->minv32);
   cudaFree(w->partial); cudaFree(w->st); cudaFree(w->st32); cudaFree(w->stT);
   if (w->hst) cudaFreeHost(w->hst);
   if (w->gFirst) cudaGraphExecDestroy(w->gFirst);

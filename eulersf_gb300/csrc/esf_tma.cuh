@@ -105,14 +105,6 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
-// L2 prefetch of a tile (no shared memory, no completion to wait for)
-__device__ __forceinline__ void tma_prefetch_3d(const CUtensorMap* map, int x, int y, int z) {
-  asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(
-                   reinterpret_cast<unsigned long long>(map)),
-               "r"(x), "r"(y), "r"(z)
-               : "memory");
-}
-
 // Grid of the kernel: 64-cell tiles in x, the register kernel's tiles in y
 // and z (same z-chunks), so that each block's r.s partials can be filed
 // under the two 32-cell tiles of the register kernel's grid.
