@@ -536,10 +536,14 @@ struct PressureWork {
   int nmapped;
 };
 
-// ---- FP32 vectors with an explicit compression attribute. With
-// ESF_VMM_COMP=none or =generic the inner-solve vectors are created with
-// cuMemCreate (compression type as named) and mapped with cuMemMap;
-// otherwise they come from cudaMalloc.
+// ---- FP32 vectors of the inner solves in compressible memory. They are
+// created with cuMemCreate (compression type GENERIC) and mapped with
+// cuMemMap: on GB300 the one-pass iteration runs 8% faster on them (135.5
+// against 147.9 us per launch at 256^3, the same with cudaMalloc and with
+// non-compressible mapped memory); compression is invisible to the kernels.
+// ESF_VMM_COMP=none maps non-compressible memory and =malloc uses
+// cudaMalloc (for comparison); any failure of the mapped path falls back to
+// cudaMalloc.
 struct VmmApi {
   PFN_cuMemGetAllocationGranularity_v10020 gran;
   PFN_cuMemCreate_v10020 create;
@@ -572,57 +576,53 @@ static const VmmApi& vmm_api() {
   }();
   return api;
 }
-static esf_status vec_alloc(PressureWork* w, float** out, size_t bytes) {
-  const char* comp = getenv("ESF_VMM_COMP");
-  if (!comp || w->nmapped >= 16) {
-    ESF_CUDA(cudaMalloc(out, bytes));
-    return ESF_OK;
-  }
+static bool vec_map(PressureWork* w, float** out, size_t bytes, unsigned char comp) {
   const VmmApi& api = vmm_api();
-  if (!api.ok) {
-    set_error("driver virtual-memory entry points are not available");
-    return ESF_ERR_CUDA;
-  }
   int dev = 0;
-  ESF_CUDA(cudaGetDevice(&dev));
+  if (!api.ok || w->nmapped >= 16 || cudaGetDevice(&dev) != cudaSuccess) return false;
   CUmemAllocationProp prop;
   memset(&prop, 0, sizeof prop);
   prop.type = CU_MEM_ALLOCATION_TYPE_PINNED;
   prop.location.type = CU_MEM_LOCATION_TYPE_DEVICE;
   prop.location.id = dev;
-  prop.allocFlags.compressionType =
-      strcmp(comp, "generic") == 0 ? CU_MEM_ALLOCATION_COMP_GENERIC : CU_MEM_ALLOCATION_COMP_NONE;
+  prop.allocFlags.compressionType = comp;
   size_t gran = 0;
-  if (api.gran(&gran, &prop, CU_MEM_ALLOC_GRANULARITY_RECOMMENDED) != CUDA_SUCCESS || gran == 0) {
-    set_error("cuMemGetAllocationGranularity failed");
-    return ESF_ERR_CUDA;
-  }
-  const size_t size = (bytes + gran - 1) / gran * gran;
+  if (api.gran(&gran, &prop, CU_MEM_ALLOC_GRANULARITY_RECOMMENDED) != CUDA_SUCCESS || gran == 0)
+    return false;
   PressureWork::Mapped m;
-  m.size = size;
-  if (api.create(&m.h, size, &prop, 0) != CUDA_SUCCESS) {
-    set_error("cuMemCreate of %zu bytes failed", size);
-    return ESF_ERR_CUDA;
-  }
-  if (api.reserve(&m.p, size, 0, 0, 0) != CUDA_SUCCESS) {
+  m.size = (bytes + gran - 1) / gran * gran;
+  if (api.create(&m.h, m.size, &prop, 0) != CUDA_SUCCESS) return false;
+  if (api.reserve(&m.p, m.size, 0, 0, 0) != CUDA_SUCCESS) {
     api.release(m.h);
-    set_error("cuMemAddressReserve failed");
-    return ESF_ERR_CUDA;
+    return false;
   }
   CUmemAccessDesc acc;
   memset(&acc, 0, sizeof acc);
   acc.location.type = CU_MEM_LOCATION_TYPE_DEVICE;
   acc.location.id = dev;
   acc.flags = CU_MEM_ACCESS_FLAGS_PROT_READWRITE;
-  if (api.map(m.p, size, 0, m.h, 0) != CUDA_SUCCESS || api.access(m.p, size, &acc, 1) != CUDA_SUCCESS) {
-    api.unmap(m.p, size);
-    api.addrFree(m.p, size);
+  if (api.map(m.p, m.size, 0, m.h, 0) != CUDA_SUCCESS) {
+    api.addrFree(m.p, m.size);
     api.release(m.h);
-    set_error("cuMemMap/cuMemSetAccess failed");
-    return ESF_ERR_CUDA;
+    return false;
+  }
+  if (api.access(m.p, m.size, &acc, 1) != CUDA_SUCCESS) {
+    api.unmap(m.p, m.size);
+    api.addrFree(m.p, m.size);
+    api.release(m.h);
+    return false;
   }
   w->mapped[w->nmapped++] = m;
   *out = reinterpret_cast<float*>(m.p);
+  return true;
+}
+static esf_status vec_alloc(PressureWork* w, float** out, size_t bytes) {
+  const char* mode = getenv("ESF_VMM_COMP");
+  const bool malloc_only = mode && strcmp(mode, "malloc") == 0;
+  const unsigned char comp =
+      (mode && strcmp(mode, "none") == 0) ? CU_MEM_ALLOCATION_COMP_NONE : CU_MEM_ALLOCATION_COMP_GENERIC;
+  if (!malloc_only && vec_map(w, out, bytes, comp)) return ESF_OK;
+  ESF_CUDA(cudaMalloc(out, bytes));
   return ESF_OK;
 }
 static void vec_free(PressureWork* w, float* p) {
