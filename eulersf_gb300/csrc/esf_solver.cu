@@ -1170,6 +1170,7 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
   const double bnorm = sqrt(bnorm2);
   double rel = bnorm > 0 ? sqrt(resid2) / bnorm : sqrt(resid2);
   int total = 0, ref = 0, conv = 0;
+  bool fp64Tail = false;
   esf_status status = ESF_OK;
   // inner stopping ratio on delta/delta0 for the next inner solve
   auto trigger = [&](double r2) {
@@ -1198,14 +1199,8 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
       if (e) return e;
     }
     const bool trace = getenv("ESF_TRACE") != nullptr;
-    // tail regime: once the residual is within tailAt x eps, each inner
-    // solve runs a fixed budget of iterations at the tight inner tolerance;
-    // a tail refinement that leaves a larger residual is undone and the
-    // budget halved
-    const char* capEnv = getenv("ESF_TAIL_CAP");
-    const char* atEnv = getenv("ESF_TAIL_AT");
-    int tailCap = capEnv ? atoi(capEnv) : 0;
-    const double tailAt = atEnv ? atof(atEnv) : 5.0;
+    const char* tailEnv = getenv("ESF_FP64_TAIL");
+    const double tail = tailEnv ? atof(tailEnv) : 0.0;
     auto t0 = std::chrono::steady_clock::now();
     for (ref = 0; ref < maxRefine; ref++) {
       if (trace) {
@@ -1222,11 +1217,8 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
         break;
       }
       // refinement: fold the FP32 partial solution into x, recompute r
-      const bool tailSolve = hi.cap > 0;
-      if (tailSolve) ESF_CUDA(cudaMemcpyAsync(w->d, x, g.R * 8, cudaMemcpyDeviceToDevice, st));
       ESF_COUNTED add_correction<<<vec_blocks(g.R), VT, 0, st>>>(g.R, x, w->x32);
       ESF_CUDA(cudaMemsetAsync(w->x32, 0, g.R * 4, st));
-      const double relBefore = rel;
       e = true_residual(&resid2, &bnorm2);
       if (e) return e;
       rel = bnorm > 0 ? sqrt(resid2) / bnorm : sqrt(resid2);
@@ -1234,21 +1226,17 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
         status = ESF_ERR_NUMERIC;
         break;
       }
-      if (tailSolve && rel >= relBefore) {
-        // the budget ran past what FP32 can resolve: undo, halve it
-        ESF_CUDA(cudaMemcpyAsync(x, w->d, g.R * 8, cudaMemcpyDeviceToDevice, st));
-        e = true_residual(&resid2, &bnorm2);
-        if (e) return e;
-        rel = bnorm > 0 ? sqrt(resid2) / bnorm : sqrt(resid2);
-        tailCap = tailCap / 2 > 50 ? tailCap / 2 : 50;
-        if (trace) fprintf(stderr, "[esf] tail refinement undone; budget now %d\n", tailCap);
-      }
       if (sqrt(resid2) < eps * bnorm) {
         conv = 1;
         ref++;
         break;
       }
       if (total >= maxIt) break;
+      if (rel < tail * eps) {
+        fp64Tail = true;
+        ref++;
+        break;
+      }
       // restart the inner recurrence from the new residual (iteration count
       // carries over; the residual is in the first buffer set)
       hi.done = 0;
@@ -1258,11 +1246,6 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
       hi.beta = 0.0;
       hi.setup = 1;
       hi.eps = trigger(resid2);
-      hi.cap = 0;
-      if (tailCap > 0 && rel < tailAt * eps) {
-        hi.eps = innerEps;
-        hi.cap = tailCap;
-      }
       memset(hi.ticket, 0, sizeof hi.ticket);
       ESF_CUDA(cudaMemcpyAsync(w->st32, &hi, sizeof hi, cudaMemcpyHostToDevice, st));
       ESF_CUDA(cudaStreamSynchronize(st));
@@ -1270,7 +1253,7 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
       if (e) return e;
     }
   }
-  if (!conv && ref >= maxRefine && status == ESF_OK && total < maxIt) {
+  if (!conv && (ref >= maxRefine || fp64Tail) && status == ESF_OK && total < maxIt) {
     // FP64 finish from the refined iterate
     PcrState h;
     esf_status e = fp64_solve(maxIt - total, &h);
