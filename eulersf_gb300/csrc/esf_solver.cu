@@ -1170,7 +1170,6 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
   const double bnorm = sqrt(bnorm2);
   double rel = bnorm > 0 ? sqrt(resid2) / bnorm : sqrt(resid2);
   int total = 0, ref = 0, conv = 0;
-  bool fp64Tail = false;
   esf_status status = ESF_OK;
   // inner stopping ratio on delta/delta0 for the next inner solve
   auto trigger = [&](double r2) {
@@ -1199,8 +1198,6 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
       if (e) return e;
     }
     const bool trace = getenv("ESF_TRACE") != nullptr;
-    const char* tailEnv = getenv("ESF_FP64_TAIL");
-    const double tail = tailEnv ? atof(tailEnv) : 0.0;
     auto t0 = std::chrono::steady_clock::now();
     for (ref = 0; ref < maxRefine; ref++) {
       if (trace) {
@@ -1232,11 +1229,6 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
         break;
       }
       if (total >= maxIt) break;
-      if (rel < tail * eps) {
-        fp64Tail = true;
-        ref++;
-        break;
-      }
       // restart the inner recurrence from the new residual (iteration count
       // carries over; the residual is in the first buffer set)
       hi.done = 0;
@@ -1253,7 +1245,7 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
       if (e) return e;
     }
   }
-  if (!conv && (ref >= maxRefine || fp64Tail) && status == ESF_OK && total < maxIt) {
+  if (!conv && ref >= maxRefine && status == ESF_OK && total < maxIt) {
     // FP64 finish from the refined iterate
     PcrState h;
     esf_status e = fp64_solve(maxIt - total, &h);
