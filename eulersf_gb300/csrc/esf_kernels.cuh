@@ -316,157 +316,24 @@ __device__ __forceinline__ void solve_distance(double p, double q, double r, dou
   if (nd < *v) *v = nd;
 }
 
-// One Gauss-Seidel sweep pass as a wavefront: node (i,j,k) only reads its
-// three upwind neighbours, so the hyperplanes a+b+c = const of the sweep's
-// local coordinates can be processed in order, each plane in parallel, and
-// give the sequential loop's exact result. Single block.
+// A Gauss-Seidel sweep pass (sweepPhi, sweepOnePass): node (i,j,k) reads
+// its three upwind neighbours as updated in the same pass, so every order in
+// which each node comes after its three upwind neighbours gives the
+// sequential loop's result bit for bit. The pass runs as a wavefront of
+// tiles (k_sweep_tile below).
 struct Sweep {
   int i0, j0, k0;   // first index in sweep order
   int di, dj, dk;   // +1 / -1
   int ni, nj, nk;   // counts
 };
 
-__device__ void sweep_phi_pass(const GridDev& g, double* ph, const double* ms, const Sweep& w) {
-  const int planes = w.ni + w.nj + w.nk - 2;
-  const long long nab = (long long)w.ni * w.nj;
-  for (int p = 0; p < planes; p++) {
-    for (long long t = threadIdx.x; t < nab; t += blockDim.x) {
-      int a = (int)(t % w.ni), b = (int)(t / w.ni);
-      int c = p - a - b;
-      if (c < 0 || c >= w.nk) continue;
-      int i = w.i0 + a * w.di, j = w.j0 + b * w.dj, k = w.k0 + c * w.dk;
-      long long n = nidx(g, i, j, k);
-      if (ms[n] == 0)
-        solve_distance(ph[nidx(g, i - w.di, j, k)], ph[nidx(g, i, j - w.dj, k)],
-                       ph[nidx(g, i, j, k - w.dk)], &ph[n]);
-    }
-    __syncthreads();
-  }
-}
-
-// One hyperplane a+b+c = p of a sweepPhi pass, all blocks in parallel.
-__global__ void k_sweep_phi_plane(GridDev g, double* ph, const double* ms, Sweep w, int p) {
-  const long long nab = (long long)w.ni * w.nj;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nab;
-       t += (long long)gridDim.x * blockDim.x) {
-    int a = (int)(t % w.ni), b = (int)(t / w.ni);
-    int c = p - a - b;
-    if (c < 0 || c >= w.nk) continue;
-    int i = w.i0 + a * w.di, j = w.j0 + b * w.dj, k = w.k0 + c * w.dk;
-    long long n = nidx(g, i, j, k);
-    if (ms[n] == 0)
-      solve_distance(ph[nidx(g, i - w.di, j, k)], ph[nidx(g, i, j - w.dj, k)],
-                     ph[nidx(g, i, j, k - w.dk)], &ph[n]);
-  }
-}
-
-// DEFOR_SOLID_3D::sweepPhi x2 (DEFOR_SOLID_3D.cpp:397-455, 267).
-__global__ void k_sweep_phi(GridDev g, SolidDev s, Box ex, int repeats) {
-  for (int rep = 0; rep < repeats; rep++)
-    for (int dir = 0; dir < 8; dir++) {
-      Sweep w;
-      w.dj = (dir & 1) ? -1 : 1;
-      w.di = (dir & 2) ? -1 : 1;
-      w.dk = (dir & 4) ? -1 : 1;
-      w.i0 = w.di > 0 ? ex.lo[0] + 1 : ex.hi[0] - 2;
-      w.j0 = w.dj > 0 ? ex.lo[1] + 1 : ex.hi[1] - 2;
-      w.k0 = w.dk > 0 ? ex.lo[2] + 1 : ex.hi[2] - 2;
-      w.ni = ex.hi[0] - ex.lo[0] - 1;
-      w.nj = ex.hi[1] - ex.lo[1] - 1;
-      w.nk = ex.hi[2] - ex.lo[2] - 1;
-      if (w.ni <= 0 || w.nj <= 0 || w.nk <= 0) continue;
-      sweep_phi_pass(g, s.phi, s.mass, w);
-    }
-}
-
 // ---------------------------------------------- velocity extension (a19)
-__device__ __forceinline__ double block_min_ll(long long v, long long* sh) {
-  __syncthreads();
-  for (int o = 16; o > 0; o >>= 1) {
-    long long w = __shfl_down_sync(0xffffffffu, v, o);
-    v = w < v ? w : v;
-  }
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    v = (threadIdx.x < blockDim.x / 32) ? sh[threadIdx.x] : LLONG_MAX;
-    for (int o = 16; o > 0; o >>= 1) {
-      long long w = __shfl_down_sync(0xffffffffu, v, o);
-      v = w < v ? w : v;
-    }
-    if (threadIdx.x == 0) sh[0] = v;
-  }
-  __syncthreads();
-  double r = (double)sh[0];
-  __syncthreads();
-  return r;
-}
-
 // DEFOR_SOLID_3D::sweepOnePass (DEFOR_SOLID_3D.cpp:457-519). Its
 // solvableX/Y/Z flags live for the whole pass and, once cleared, stay
 // cleared: a node sees a flag cleared iff some node at or before it in loop
 // order triggered it. Triggers depend on phi and mass only (constant during
 // the pass), so the first trigger rank of each flag is found by a min
 // reduction before the wavefront runs.
-__device__ void sweep_vec_pass(const GridDev& g, double* f, const double* ph, const double* ms,
-                               const Sweep& w, long long* sh) {
-  const long long nij = (long long)w.ni * w.nj, total = nij * w.nk;
-  long long rx = LLONG_MAX, ry = LLONG_MAX, rz = LLONG_MAX;
-  for (long long t = threadIdx.x; t < total; t += blockDim.x) {
-    int a = (int)(t % w.ni), b = (int)((t / w.ni) % w.nj), c = (int)(t / nij);
-    int i = w.i0 + a * w.di, j = w.j0 + b * w.dj, k = w.k0 + c * w.dk;
-    long long n = nidx(g, i, j, k);
-    if (ms[n] != 0) continue;
-    double pn = ph[n];
-    double dp = pn - ph[nidx(g, i - w.di, j, k)], dpn = pn - ph[nidx(g, i + w.di, j, k)];
-    if (dp < 0 && dpn >= 0) continue;
-    if (dp < 0 && dpn < 0 && t < rx) rx = t;
-    double dq = pn - ph[nidx(g, i, j - w.dj, k)], dqn = pn - ph[nidx(g, i, j + w.dj, k)];
-    if (dq < 0 && dqn >= 0) continue;
-    if (dq < 0 && dqn < 0 && t < ry) ry = t;
-    double dr = pn - ph[nidx(g, i, j, k - w.dk)], drn = pn - ph[nidx(g, i, j, k + w.dk)];
-    if (dr < 0 && drn >= 0) continue;
-    if (dr < 0 && drn < 0 && t < rz) rz = t;
-  }
-  rx = (long long)block_min_ll(rx, sh);
-  ry = (long long)block_min_ll(ry, sh);
-  rz = (long long)block_min_ll(rz, sh);
-  const int planes = w.ni + w.nj + w.nk - 2;
-  for (int p = 0; p < planes; p++) {
-    for (long long t = threadIdx.x; t < nij; t += blockDim.x) {
-      int a = (int)(t % w.ni), b = (int)(t / w.ni);
-      int c = p - a - b;
-      if (c < 0 || c >= w.nk) continue;
-      int i = w.i0 + a * w.di, j = w.j0 + b * w.dj, k = w.k0 + c * w.dk;
-      long long n = nidx(g, i, j, k);
-      if (ms[n] != 0) continue;
-      long long rank = a + (long long)b * w.ni + (long long)c * nij;
-      double pn = ph[n];
-      double dp = pn - ph[nidx(g, i - w.di, j, k)], dpn = pn - ph[nidx(g, i + w.di, j, k)];
-      if (dp < 0 && dpn >= 0) continue;
-      double dq = pn - ph[nidx(g, i, j - w.dj, k)], dqn = pn - ph[nidx(g, i, j + w.dj, k)];
-      if (dq < 0 && dqn >= 0) continue;
-      double dr = pn - ph[nidx(g, i, j, k - w.dk)], drn = pn - ph[nidx(g, i, j, k + w.dk)];
-      if (dr < 0 && drn >= 0) continue;
-      if (rank >= rx) dp = 0;
-      if (rank >= ry) dq = 0;
-      if (rank >= rz) dr = 0;
-      double alpha, beta;
-      if (dp + dq + dr < 1e-3) {
-        alpha = 0.333;
-        beta = 0.333;
-      } else {
-        alpha = dp / (dp + dq + dr);
-        beta = dq / (dp + dq + dr);
-      }
-      long long ea = nidx(g, i - w.di, j, k), eb = nidx(g, i, j - w.dj, k), ec = nidx(g, i, j, k - w.dk);
-#pragma unroll
-      for (int q = 0; q < 3; q++)
-        f[3 * n + q] = (alpha * f[3 * ea + q] + beta * f[3 * eb + q]) + (1 - alpha - beta) * f[3 * ec + q];
-    }
-    __syncthreads();
-  }
-}
 
 // First trigger rank of the three pass-long flags of sweepOnePass, by
 // atomicMin over all nodes of the pass (ranks: long long loop order).
@@ -501,44 +368,114 @@ __global__ void k_sweep_vec_ranks(GridDev g, const double* ph, const double* ms,
   __syncthreads();
   if (threadIdx.x < 3 && sm[threadIdx.x] != ~0ull) atomicMin(&ranks[threadIdx.x], sm[threadIdx.x]);
 }
-// One hyperplane of a sweepOnePass pass (flags resolved from the ranks).
-__global__ void k_sweep_vec_plane(GridDev g, double* f, const double* ph, const double* ms, Sweep w,
-                                  int p, const unsigned long long* ranks) {
-  const long long nij = (long long)w.ni * w.nj;
-  const unsigned long long rx = ranks[0], ry = ranks[1], rz = ranks[2];
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nij;
-       t += (long long)gridDim.x * blockDim.x) {
-    int a = (int)(t % w.ni), b = (int)(t / w.ni);
-    int c = p - a - b;
-    if (c < 0 || c >= w.nk) continue;
-    int i = w.i0 + a * w.di, j = w.j0 + b * w.dj, k = w.k0 + c * w.dk;
-    long long n = nidx(g, i, j, k);
-    if (ms[n] != 0) continue;
-    unsigned long long rank = (unsigned long long)(a + (long long)b * w.ni + (long long)c * nij);
-    double pn = ph[n];
-    double dp = pn - ph[nidx(g, i - w.di, j, k)], dpn = pn - ph[nidx(g, i + w.di, j, k)];
-    if (dp < 0 && dpn >= 0) continue;
-    double dq = pn - ph[nidx(g, i, j - w.dj, k)], dqn = pn - ph[nidx(g, i, j + w.dj, k)];
-    if (dq < 0 && dqn >= 0) continue;
-    double dr = pn - ph[nidx(g, i, j, k - w.dk)], drn = pn - ph[nidx(g, i, j, k + w.dk)];
-    if (dr < 0 && drn >= 0) continue;
-    if (rank >= rx) dp = 0;
-    if (rank >= ry) dq = 0;
-    if (rank >= rz) dr = 0;
-    double alpha, beta;
-    if (dp + dq + dr < 1e-3) {
-      alpha = 0.333;
-      beta = 0.333;
-    } else {
-      alpha = dp / (dp + dq + dr);
-      beta = dq / (dp + dq + dr);
-    }
-    long long ea = nidx(g, i - w.di, j, k), eb = nidx(g, i, j - w.dj, k), ec = nidx(g, i, j, k - w.dk);
+// One launch of a sweep pass as a tile wavefront: the pass's nodes in
+// sweep coordinates (a, b, c) are cut into ST^3 tiles, and launch P runs
+// every tile (I, J, K) with I + J + K = P, whose three upwind tiles ran in
+// launch P - 1. A block copies its tile and the upwind layer of each axis
+// into shared memory, sweeps the tile's sub-planes a'+b'+c' = q in order
+// (a barrier between sub-planes), and writes the tile back. PHI: the
+// distance update of sweepPhi (DEFOR_SOLID_3D.cpp:397-455) on phi; VEC: the
+// sweepOnePass update (DEFOR_SOLID_3D.cpp:457-519) of the three velocity
+// components, with the pass-long flags resolved from the ranks found by
+// k_sweep_vec_ranks. phi and the mass do not change during a VEC pass and
+// are read from global memory.
+constexpr int ST = 8;           // tile edge
+constexpr int SP = ST + 1;      // tile plus the upwind layer
+constexpr int SWEEP_THREADS = 128;
+static_assert(ST * ST <= SWEEP_THREADS, "one thread per (a', b') of a tile");
+template <bool VEC>
+__global__ void __launch_bounds__(SWEEP_THREADS) k_sweep_tile(GridDev g, double* f, double* ph,
+                                                              const double* ms, Sweep w, int P,
+                                                              const unsigned long long* ranks) {
+  constexpr int NC = VEC ? 3 : 1;
+  __shared__ double sv[NC * SP * SP * SP];
+  const int nti = (w.ni + ST - 1) / ST, ntj = (w.nj + ST - 1) / ST, ntk = (w.nk + ST - 1) / ST;
+  const int I = blockIdx.x % nti, J = blockIdx.x / nti, K = P - I - J;
+  if (J >= ntj || K < 0 || K >= ntk) return;
+  const int a0 = I * ST, b0 = J * ST, c0 = K * ST;
+  const int na = min(ST, w.ni - a0), nb = min(ST, w.nj - b0), nc = min(ST, w.nk - c0);
+  double* const src = VEC ? f : ph;
+  // tile and upwind layers: local -1 .. n-1 on each axis (local -1 of the
+  // first tile is the node before the pass's first, inside the box)
+  for (int t = threadIdx.x; t < SP * SP * SP; t += SWEEP_THREADS) {
+    const int la = t % SP - 1, lb = (t / SP) % SP - 1, lc = t / (SP * SP) - 1;
+    if (la >= na || lb >= nb || lc >= nc) continue;
+    const long long n = nidx(g, w.i0 + (a0 + la) * w.di, w.j0 + (b0 + lb) * w.dj, w.k0 + (c0 + lc) * w.dk);
 #pragma unroll
-    for (int q = 0; q < 3; q++)
-      f[3 * n + q] = (alpha * f[3 * ea + q] + beta * f[3 * eb + q]) + (1 - alpha - beta) * f[3 * ec + q];
+    for (int q = 0; q < NC; q++) sv[NC * t + q] = src[NC * n + q];
+  }
+  unsigned long long rx = 0, ry = 0, rz = 0;
+  if (VEC) {
+    rx = ranks[0];
+    ry = ranks[1];
+    rz = ranks[2];
+  }
+  const long long nij = (long long)w.ni * w.nj;
+  __syncthreads();
+  const int la = threadIdx.x % ST, lb = threadIdx.x / ST;
+  const bool mine = threadIdx.x < ST * ST && la < na && lb < nb;
+  for (int q = 0; q <= (na - 1) + (nb - 1) + (nc - 1); q++) {
+    const int lc = q - la - lb;
+    if (mine && lc >= 0 && lc < nc) {
+      const int a = a0 + la, b = b0 + lb, c = c0 + lc;
+      const int i = w.i0 + a * w.di, j = w.j0 + b * w.dj, k = w.k0 + c * w.dk;
+      const long long n = nidx(g, i, j, k);
+      const int s = (la + 1) + (lb + 1) * SP + (lc + 1) * SP * SP;
+      const int sa = s - 1, sb = s - SP, sc = s - SP * SP;  // upwind in a, b, c
+      if (!VEC) {
+        if (ms[n] == 0) solve_distance(sv[sa], sv[sb], sv[sc], &sv[s]);
+      } else if (ms[n] == 0) {
+        const unsigned long long rank = (unsigned long long)(a + (long long)b * w.ni + (long long)c * nij);
+        const double pn = ph[n];
+        double dp = pn - ph[nidx(g, i - w.di, j, k)], dpn = pn - ph[nidx(g, i + w.di, j, k)];
+        bool skip = dp < 0 && dpn >= 0;
+        double dq = 0, dqn = 0, dr = 0, drn = 0;
+        if (!skip) {
+          dq = pn - ph[nidx(g, i, j - w.dj, k)];
+          dqn = pn - ph[nidx(g, i, j + w.dj, k)];
+          skip = dq < 0 && dqn >= 0;
+        }
+        if (!skip) {
+          dr = pn - ph[nidx(g, i, j, k - w.dk)];
+          drn = pn - ph[nidx(g, i, j, k + w.dk)];
+          skip = dr < 0 && drn >= 0;
+        }
+        if (!skip) {
+          if (rank >= rx) dp = 0;
+          if (rank >= ry) dq = 0;
+          if (rank >= rz) dr = 0;
+          double alpha, beta;
+          if (dp + dq + dr < 1e-3) {
+            alpha = 0.333;
+            beta = 0.333;
+          } else {
+            alpha = dp / (dp + dq + dr);
+            beta = dq / (dp + dq + dr);
+          }
+#pragma unroll
+          for (int e = 0; e < 3; e++)
+            sv[3 * s + e] = (alpha * sv[3 * sa + e] + beta * sv[3 * sb + e]) + (1 - alpha - beta) * sv[3 * sc + e];
+        }
+      }
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < SP * SP * SP; t += SWEEP_THREADS) {
+    const int ta = t % SP - 1, tb = (t / SP) % SP - 1, tc = t / (SP * SP) - 1;
+    if (ta < 0 || tb < 0 || tc < 0 || ta >= na || tb >= nb || tc >= nc) continue;
+    const long long n = nidx(g, w.i0 + (a0 + ta) * w.di, w.j0 + (b0 + tb) * w.dj, w.k0 + (c0 + tc) * w.dk);
+#pragma unroll
+    for (int e = 0; e < NC; e++) src[NC * n + e] = sv[NC * t + e];
   }
 }
+// Launches of one sweep pass as a tile wavefront.
+inline int sweep_tile_launches(const Sweep& w) {
+  return (w.ni + ST - 1) / ST + (w.nj + ST - 1) / ST + (w.nk + ST - 1) / ST - 2;
+}
+inline int sweep_tile_blocks(const Sweep& w) {
+  return ((w.ni + ST - 1) / ST) * ((w.nj + ST - 1) / ST);
+}
+
 // Face copies of sweepVectorField (DEFOR_SOLID_3D.cpp:544-563), one axis
 // per launch, in the order z, y, x.
 __global__ void k_extend_faces(GridDev g, double* f, const double* ms, Box ex, int axis) {
@@ -572,62 +509,6 @@ __global__ void k_extend_faces(GridDev g, double* f, const double* ms, Box ex, i
     B = nidx(g, cc[0], cc[1], cc[2]);
     if (ms[A] == 0)
       for (int q = 0; q < 3; q++) f[3 * A + q] = f[3 * B + q];
-  }
-}
-
-// extendVectorField = 4 x sweepVectorField (DEFOR_SOLID_3D.cpp:521-574).
-__global__ void __launch_bounds__(1024) k_extend_velocity(GridDev g, SolidDev s, Box ex) {
-  __shared__ long long sh[32];
-  const int xn = ex.lo[0], xm = ex.hi[0], yn = ex.lo[1], ym = ex.hi[1], zn = ex.lo[2], zm = ex.hi[2];
-  double* f = s.vel;
-  for (int rep = 0; rep < 4; rep++) {
-    // the 8 calls of sweepVectorField in order: (x, y, z) = (f,f,f) (f,r,f)
-    // (r,f,f) (r,r,f) then the same with z reversed
-    for (int dir = 0; dir < 8; dir++) {
-      Sweep w;
-      w.dj = (dir & 1) ? -1 : 1;
-      w.di = (dir & 2) ? -1 : 1;
-      w.dk = (dir & 4) ? -1 : 1;
-      w.i0 = w.di > 0 ? xn + 1 : xm - 2;
-      w.j0 = w.dj > 0 ? yn + 1 : ym - 2;
-      w.k0 = w.dk > 0 ? zn + 1 : zm - 2;
-      w.ni = xm - xn - 2;
-      w.nj = ym - yn - 2;
-      w.nk = zm - zn - 2;
-      if (w.ni <= 0 || w.nj <= 0 || w.nk <= 0) continue;
-      sweep_vec_pass(g, f, s.phi, s.mass, w, sh);
-    }
-    // face copies: z faces, then y faces, then x faces (:544-563)
-    const long long nxy = (long long)(xm - xn) * (ym - yn);
-    for (long long t = threadIdx.x; t < nxy; t += blockDim.x) {
-      int i = xn + (int)(t % (xm - xn)), j = yn + (int)(t / (xm - xn));
-      long long a = nidx(g, i, j, zn), b = nidx(g, i, j, zm - 1);
-      if (s.mass[a] == 0)
-        for (int q = 0; q < 3; q++) f[3 * a + q] = f[3 * nidx(g, i, j, zn + 1) + q];
-      if (s.mass[b] == 0)
-        for (int q = 0; q < 3; q++) f[3 * b + q] = f[3 * nidx(g, i, j, zm - 2) + q];
-    }
-    __syncthreads();
-    const long long nxz = (long long)(xm - xn) * (zm - zn);
-    for (long long t = threadIdx.x; t < nxz; t += blockDim.x) {
-      int i = xn + (int)(t % (xm - xn)), k = zn + (int)(t / (xm - xn));
-      long long a = nidx(g, i, yn, k), b = nidx(g, i, ym - 1, k);
-      if (s.mass[a] == 0)
-        for (int q = 0; q < 3; q++) f[3 * a + q] = f[3 * nidx(g, i, yn + 1, k) + q];
-      if (s.mass[b] == 0)
-        for (int q = 0; q < 3; q++) f[3 * b + q] = f[3 * nidx(g, i, ym - 2, k) + q];
-    }
-    __syncthreads();
-    const long long nyz = (long long)(ym - yn) * (zm - zn);
-    for (long long t = threadIdx.x; t < nyz; t += blockDim.x) {
-      int j = yn + (int)(t % (ym - yn)), k = zn + (int)(t / (ym - yn));
-      long long a = nidx(g, xn, j, k), b = nidx(g, xm - 1, j, k);
-      if (s.mass[a] == 0)
-        for (int q = 0; q < 3; q++) f[3 * a + q] = f[3 * nidx(g, xn + 1, j, k) + q];
-      if (s.mass[b] == 0)
-        for (int q = 0; q < 3; q++) f[3 * b + q] = f[3 * nidx(g, xm - 2, j, k) + q];
-    }
-    __syncthreads();
   }
 }
 

@@ -552,7 +552,7 @@ static esf_status compute_sdf(esf_scene* sc, Solid* d) {
   d->ex[4] = std::min(ymax + exn, G.Y);
   d->ex[5] = std::min(zmax + exn, G.Z);
   Box ex = mkbox(d->ex[0], d->ex[1], d->ex[2], d->ex[3], d->ex[4], d->ex[5]);
-  // 2 x sweepPhi: 8 passes each, every pass a sequence of hyperplanes
+  // 2 x sweepPhi: 8 passes each, every pass a wavefront of 8^3 tiles
   for (int rep = 0; rep < 2; rep++)
     for (int dir = 0; dir < 8; dir++) {
       Sweep w;
@@ -566,10 +566,10 @@ static esf_status compute_sdf(esf_scene* sc, Solid* d) {
       w.nj = ex.hi[1] - ex.lo[1] - 1;
       w.nk = ex.hi[2] - ex.lo[2] - 1;
       if (w.ni <= 0 || w.nj <= 0 || w.nk <= 0) continue;
-      const int planes = w.ni + w.nj + w.nk - 2;
-      const int blocks = kblocks((long long)w.ni * w.nj);
-      for (int pl = 0; pl < planes; pl++)
-        ESF_COUNTED k_sweep_phi_plane<<<blocks, KT, 0, st>>>(G, d->d.phi, d->d.mass, w, pl);
+      const int launches = sweep_tile_launches(w), blocks = sweep_tile_blocks(w);
+      for (int P = 0; P < launches; P++)
+        ESF_COUNTED k_sweep_tile<false><<<blocks, SWEEP_THREADS, 0, st>>>(G, nullptr, d->d.phi, d->d.mass, w,
+                                                                        P, nullptr);
     }
   ESF_LAUNCH_CHECK();
   return ESF_OK;
@@ -1028,10 +1028,10 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
         ESF_CUDA(cudaMemsetAsync(ranks, 0xff, 3 * 8, st));
         const long long total = (long long)w.ni * w.nj * w.nk;
         ESF_COUNTED k_sweep_vec_ranks<<<kblocks(total), KT, 0, st>>>(G, d->d.phi, d->d.mass, w, ranks);
-        const int planes = w.ni + w.nj + w.nk - 2;
-        const int blocks = kblocks((long long)w.ni * w.nj);
-        for (int pl = 0; pl < planes; pl++)
-          ESF_COUNTED k_sweep_vec_plane<<<blocks, KT, 0, st>>>(G, d->d.vel, d->d.phi, d->d.mass, w, pl, ranks);
+        const int launches = sweep_tile_launches(w), blocks = sweep_tile_blocks(w);
+        for (int P = 0; P < launches; P++)
+          ESF_COUNTED k_sweep_tile<true><<<blocks, SWEEP_THREADS, 0, st>>>(G, d->d.vel, d->d.phi, d->d.mass, w,
+                                                                         P, ranks);
       }
       for (int axis = 2; axis >= 0; axis--) {
         const long long nf = boxn(ex) / (ex.hi[axis] - ex.lo[axis]);
