@@ -372,13 +372,15 @@ __global__ void k_sweep_vec_ranks(GridDev g, const double* ph, const double* ms,
 // sweep coordinates (a, b, c) are cut into ST^3 tiles, and launch P runs
 // every tile (I, J, K) with I + J + K = P, whose three upwind tiles ran in
 // launch P - 1. A block copies its tile and the upwind layer of each axis
-// into shared memory, sweeps the tile's sub-planes a'+b'+c' = q in order
-// (a barrier between sub-planes), and writes the tile back. PHI: the
-// distance update of sweepPhi (DEFOR_SOLID_3D.cpp:397-455) on phi; VEC: the
-// sweepOnePass update (DEFOR_SOLID_3D.cpp:457-519) of the three velocity
-// components, with the pass-long flags resolved from the ranks found by
-// k_sweep_vec_ranks. phi and the mass do not change during a VEC pass and
-// are read from global memory.
+// into shared memory, settles for each of its nodes what does not change
+// during the pass (all nodes at once), sweeps the tile's sub-planes
+// a'+b'+c' = q in order in shared memory (a barrier between sub-planes), and
+// writes the tile back. PHI: the distance update of sweepPhi
+// (DEFOR_SOLID_3D.cpp:397-455) on phi, for nodes without solid mass. VEC:
+// the sweepOnePass update (DEFOR_SOLID_3D.cpp:457-519) of the three velocity
+// components; its skip tests and blend weights depend on phi, the mass and
+// the pass-long flags (resolved from the ranks of k_sweep_vec_ranks) only,
+// none of which change during the pass, so they are formed up front.
 constexpr int ST = 8;           // tile edge
 constexpr int SP = ST + 1;      // tile plus the upwind layer
 constexpr int SWEEP_THREADS = 128;
@@ -389,6 +391,8 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep_tile(GridDev g, double*
                                                               const unsigned long long* ranks) {
   constexpr int NC = VEC ? 3 : 1;
   __shared__ double sv[NC * SP * SP * SP];
+  __shared__ double sAlpha[VEC ? ST * ST * ST : 1], sBeta[VEC ? ST * ST * ST : 1];
+  __shared__ unsigned char sUpd[ST * ST * ST];
   const int nti = (w.ni + ST - 1) / ST, ntj = (w.nj + ST - 1) / ST, ntk = (w.nk + ST - 1) / ST;
   const int I = blockIdx.x % nti, J = blockIdx.x / nti, K = P - I - J;
   if (J >= ntj || K < 0 || K >= ntk) return;
@@ -404,54 +408,69 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep_tile(GridDev g, double*
 #pragma unroll
     for (int q = 0; q < NC; q++) sv[NC * t + q] = src[NC * n + q];
   }
-  unsigned long long rx = 0, ry = 0, rz = 0;
-  if (VEC) {
-    rx = ranks[0];
-    ry = ranks[1];
-    rz = ranks[2];
-  }
+  // per node of the tile: update or not, and (VEC) the blend weights
   const long long nij = (long long)w.ni * w.nj;
+  for (int t = threadIdx.x; t < ST * ST * ST; t += SWEEP_THREADS) {
+    const int la = t % ST, lb = (t / ST) % ST, lc = t / (ST * ST);
+    unsigned char upd = 0;
+    if (la < na && lb < nb && lc < nc) {
+      const int a = a0 + la, b = b0 + lb, c = c0 + lc;
+      const int i = w.i0 + a * w.di, j = w.j0 + b * w.dj, k = w.k0 + c * w.dk;
+      const long long n = nidx(g, i, j, k);
+      if (ms[n] == 0) {
+        if (!VEC) {
+          upd = 1;
+        } else {
+          const unsigned long long rank = (unsigned long long)(a + (long long)b * w.ni + (long long)c * nij);
+          const double pn = ph[n];
+          double dp = pn - ph[nidx(g, i - w.di, j, k)], dpn = pn - ph[nidx(g, i + w.di, j, k)];
+          bool skip = dp < 0 && dpn >= 0;
+          double dq = 0, dqn = 0, dr = 0, drn = 0;
+          if (!skip) {
+            dq = pn - ph[nidx(g, i, j - w.dj, k)];
+            dqn = pn - ph[nidx(g, i, j + w.dj, k)];
+            skip = dq < 0 && dqn >= 0;
+          }
+          if (!skip) {
+            dr = pn - ph[nidx(g, i, j, k - w.dk)];
+            drn = pn - ph[nidx(g, i, j, k + w.dk)];
+            skip = dr < 0 && drn >= 0;
+          }
+          if (!skip) {
+            if (rank >= ranks[0]) dp = 0;
+            if (rank >= ranks[1]) dq = 0;
+            if (rank >= ranks[2]) dr = 0;
+            double alpha, beta;
+            if (dp + dq + dr < 1e-3) {
+              alpha = 0.333;
+              beta = 0.333;
+            } else {
+              alpha = dp / (dp + dq + dr);
+              beta = dq / (dp + dq + dr);
+            }
+            sAlpha[t] = alpha;
+            sBeta[t] = beta;
+            upd = 1;
+          }
+        }
+      }
+    }
+    sUpd[t] = upd;
+  }
   __syncthreads();
   const int la = threadIdx.x % ST, lb = threadIdx.x / ST;
   const bool mine = threadIdx.x < ST * ST && la < na && lb < nb;
   for (int q = 0; q <= (na - 1) + (nb - 1) + (nc - 1); q++) {
     const int lc = q - la - lb;
     if (mine && lc >= 0 && lc < nc) {
-      const int a = a0 + la, b = b0 + lb, c = c0 + lc;
-      const int i = w.i0 + a * w.di, j = w.j0 + b * w.dj, k = w.k0 + c * w.dk;
-      const long long n = nidx(g, i, j, k);
-      const int s = (la + 1) + (lb + 1) * SP + (lc + 1) * SP * SP;
-      const int sa = s - 1, sb = s - SP, sc = s - SP * SP;  // upwind in a, b, c
-      if (!VEC) {
-        if (ms[n] == 0) solve_distance(sv[sa], sv[sb], sv[sc], &sv[s]);
-      } else if (ms[n] == 0) {
-        const unsigned long long rank = (unsigned long long)(a + (long long)b * w.ni + (long long)c * nij);
-        const double pn = ph[n];
-        double dp = pn - ph[nidx(g, i - w.di, j, k)], dpn = pn - ph[nidx(g, i + w.di, j, k)];
-        bool skip = dp < 0 && dpn >= 0;
-        double dq = 0, dqn = 0, dr = 0, drn = 0;
-        if (!skip) {
-          dq = pn - ph[nidx(g, i, j - w.dj, k)];
-          dqn = pn - ph[nidx(g, i, j + w.dj, k)];
-          skip = dq < 0 && dqn >= 0;
-        }
-        if (!skip) {
-          dr = pn - ph[nidx(g, i, j, k - w.dk)];
-          drn = pn - ph[nidx(g, i, j, k + w.dk)];
-          skip = dr < 0 && drn >= 0;
-        }
-        if (!skip) {
-          if (rank >= rx) dp = 0;
-          if (rank >= ry) dq = 0;
-          if (rank >= rz) dr = 0;
-          double alpha, beta;
-          if (dp + dq + dr < 1e-3) {
-            alpha = 0.333;
-            beta = 0.333;
-          } else {
-            alpha = dp / (dp + dq + dr);
-            beta = dq / (dp + dq + dr);
-          }
+      const int u = la + lb * ST + lc * ST * ST;
+      if (sUpd[u]) {
+        const int s = (la + 1) + (lb + 1) * SP + (lc + 1) * SP * SP;
+        const int sa = s - 1, sb = s - SP, sc = s - SP * SP;  // upwind in a, b, c
+        if (!VEC) {
+          solve_distance(sv[sa], sv[sb], sv[sc], &sv[s]);
+        } else {
+          const double alpha = sAlpha[u], beta = sBeta[u];
 #pragma unroll
           for (int e = 0; e < 3; e++)
             sv[3 * s + e] = (alpha * sv[3 * sa + e] + beta * sv[3 * sb + e]) + (1 - alpha - beta) * sv[3 * sc + e];
