@@ -1480,128 +1480,6 @@ __global__ void __launch_bounds__(VT) pcr_update_xr(long long n, T* x, const T* 
 }
 
 
-// One-pass FP32 CR iteration of the solid system (inner solves of the mixed
-// path): the recurrence of pcr_iteration_fused on the assembled 27-block
-// rows. Per solid node, r, t = s/diag and q = Ap/diag of its three DOFs are
-// packed as three float4 (r0 r1 r2 -, t0 t1 t2 -, q0 q1 q2 -), double-
-// buffered; d, x and 1/diag stay plain per-DOF arrays read and written at the
-// row's own DOFs only. Row a: q = t + beta q, d = r + beta d, x += alpha d,
-// r' = r - alpha q at its own DOFs and, on the fly, at each neighbour the
-// block row touches; s = A r', t' = s/diag; the sums (r', s), (s, t'),
-// (s, q), (q, q diag) go to finish_fused as for the pressure.
-__device__ __forceinline__ float3 solid_rnew(const float4* pk, long long m, float alpha, float beta) {
-  const float4 R = pk[3 * m], T = pk[3 * m + 1], Q = pk[3 * m + 2];
-  return make_float3(__fmaf_rn(-alpha, __fmaf_rn(beta, Q.x, T.x), R.x),
-                     __fmaf_rn(-alpha, __fmaf_rn(beta, Q.y, T.y), R.y),
-                     __fmaf_rn(-alpha, __fmaf_rn(beta, Q.z, T.z), R.z));
-}
-__global__ void __launch_bounds__(VT) solid_iteration_fused(long long S, const float* __restrict__ blocks,
-                                                            const int* __restrict__ nbr,
-                                                            const float4* pk0, const float4* pk1,
-                                                            float4* out0, float4* out1, float* d, float* x,
-                                                            const float* invd, double* partial,
-                                                            PcrState* st) {
-  __shared__ double sred[32];
-  __shared__ bool amLast;
-  if (st->done) return;
-  if (st->iter >= st->maxIt) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) st->done = 1;
-    return;
-  }
-  const int pin = st->pp & 1;
-  const float4* pk = pin ? pk1 : pk0;
-  float4* out = pin ? out0 : out1;
-  const float alpha = (float)st->alpha, beta = (float)st->beta;
-  float sDl = 0, sMu = 0, sNu = 0, sOm = 0;
-  for (long long a = blockIdx.x * (long long)VT + threadIdx.x; a < S; a += (long long)gridDim.x * VT) {
-    const float4 R = pk[3 * a], T = pk[3 * a + 1], Q = pk[3 * a + 2];
-    const float qn[3] = {__fmaf_rn(beta, Q.x, T.x), __fmaf_rn(beta, Q.y, T.y), __fmaf_rn(beta, Q.z, T.z)};
-    const float rv[3] = {R.x, R.y, R.z};
-    float rn[3], iv[3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      const long long i = 3 * a + c;
-      const float dn = __fmaf_rn(beta, d[i], rv[c]);
-      d[i] = dn;
-      x[i] = __fmaf_rn(alpha, dn, x[i]);
-      rn[c] = __fmaf_rn(-alpha, qn[c], rv[c]);
-      iv[c] = invd[i];
-      if (iv[c] > 0.0f) sOm += __fdividef(qn[c] * qn[c], iv[c]);
-    }
-    float y0 = 0, y1 = 0, y2 = 0;
-    const int* nb = nbr + nbr_at(a, 0);
-    const float* B0 = blocks + blk_at(a, 0);
-#pragma unroll 9
-    for (int j = 0; j < 27; j++) {
-      const int m = __ldg(nb + 32 * j);
-      if (m >= 0) {
-        const float3 v = solid_rnew(pk, m, alpha, beta);
-        const float* Bj = B0 + 32 * 9 * j;
-        y0 += Bj[0] * v.x + Bj[32] * v.y + Bj[64] * v.z;
-        y1 += Bj[96] * v.x + Bj[128] * v.y + Bj[160] * v.z;
-        y2 += Bj[192] * v.x + Bj[224] * v.y + Bj[256] * v.z;
-      }
-    }
-    const float y[3] = {y0, y1, y2};
-    float t[3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      t[c] = __fmul_rn(iv[c], y[c]);
-      sDl += rn[c] * y[c];
-      sMu += y[c] * t[c];
-      sNu += y[c] * qn[c];
-    }
-    out[3 * a] = make_float4(rn[0], rn[1], rn[2], 0.0f);
-    out[3 * a + 1] = make_float4(t[0], t[1], t[2], 0.0f);
-    out[3 * a + 2] = make_float4(qn[0], qn[1], qn[2], 0.0f);
-  }
-  const int nb = gridDim.x;
-  const double pDl = block_sum<VT>((double)sDl, sred);
-  const double pMu = block_sum<VT>((double)sMu, sred);
-  const double pNu = block_sum<VT>((double)sNu, sred);
-  const double pOm = block_sum<VT>((double)sOm, sred);
-  if (threadIdx.x == 0) {
-    partial[blockIdx.x] = pDl;
-    partial[nb + blockIdx.x] = pMu;
-    partial[2 * nb + blockIdx.x] = pNu;
-    partial[3 * nb + blockIdx.x] = pOm;
-    __threadfence();
-    const unsigned t = atomicAdd(&st->ticket[1], 1u);
-    amLast = (t + 1 == (unsigned)nb);
-  }
-  __syncthreads();
-  if (!amLast) return;
-  __threadfence();
-  auto fold = [&](int h) {
-    double acc = 0;
-    for (int q = threadIdx.x; q < nb; q += VT) acc += __ldcg(partial + h * nb + q);
-    return block_sum<VT>(acc, sred);
-  };
-  const double tDl = fold(0), tMu = fold(1), tNu = fold(2), tOm = fold(3);
-  if (threadIdx.x == 0) {
-    st->ticket[1] = 0;
-    finish_fused(st, tDl, tMu, tNu, tOm);
-  }
-}
-// Zero start of a one-pass solid inner solve: r = b/diag (packed set 0),
-// t = q = 0, d = x = 0.
-__global__ void __launch_bounds__(VT) solid_fused_start(long long S, const float* b, const float* invd,
-                                                        float4* pk, float* d, float* x) {
-  for (long long a = blockIdx.x * (long long)VT + threadIdx.x; a < S; a += (long long)gridDim.x * VT) {
-    float r[3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      const long long i = 3 * a + c;
-      r[c] = b[i] * invd[i];
-      d[i] = 0.0f;
-      x[i] = 0.0f;
-    }
-    pk[3 * a] = make_float4(r[0], r[1], r[2], 0.0f);
-    pk[3 * a + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    pk[3 * a + 2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  }
-}
-
 struct SolidWork {
   long long S;
   PcrState* hst;      // pinned state copies [4]
@@ -1616,12 +1494,7 @@ struct SolidWork {
   float *blocks32, *x32, *r32, *d32, *Ap32, *s32, *invd32, *b32;
   PcrState *st, *st32;
   long long cap;
-  // one-pass FP32 iteration: packed r, t, q (two sets) and its chunk graph
-  float *pk[2];
-  cudaGraphExec_t gFused;
-  unsigned long long kFused;
-  const void* keyFused[8];
-  MappedSet mapped;  // blocks32 and the packed sets
+  MappedSet mapped;  // blocks32 in compressible memory (vec_alloc)
 };
 
 esf_status solid_work_alloc(SolidWork** out, long long S, int mixed) {
@@ -1642,12 +1515,10 @@ esf_status solid_work_alloc(SolidWork** out, long long S, int mixed) {
   for (int i = 0; i < 4; i++) ESF_CUDA(cudaEventCreateWithFlags(&w->ev[i], cudaEventDisableTiming));
   ESF_CUDA(cudaStreamCreateWithFlags(&w->capStream, cudaStreamNonBlocking));
   if (mixed) {
+    // the FP32 blocks in compressible memory: 166 against 171 ms of solid
+    // solves per 256^3 step with cudaMalloc
     esf_status e = vec_alloc(&w->mapped, &w->blocks32, rows32(w->cap) * 243 * 4);
     if (e) return e;
-    for (int k = 0; k < 2; k++) {
-      e = vec_alloc(&w->mapped, &w->pk[k], (size_t)w->cap * 12 * 4);
-      if (e) return e;
-    }
     ESF_CUDA(cudaMalloc(&w->x32, n * 4));
     ESF_CUDA(cudaMalloc(&w->r32, n * 4));
     ESF_CUDA(cudaMalloc(&w->d32, n * 4));
@@ -1665,9 +1536,6 @@ void solid_work_free(SolidWork* w) {
   cudaFree(w->r); cudaFree(w->d); cudaFree(w->Ap); cudaFree(w->s); cudaFree(w->invd);
   cudaFree(w->partial); cudaFree(w->st); cudaFree(w->st32);
   vec_free(&w->mapped, w->blocks32);
-  vec_free(&w->mapped, w->pk[0]);
-  vec_free(&w->mapped, w->pk[1]);
-  if (w->gFused) cudaGraphExecDestroy(w->gFused);
   cudaFree(w->x32); cudaFree(w->r32); cudaFree(w->d32); cudaFree(w->Ap32); cudaFree(w->s32);
   cudaFree(w->invd32); cudaFree(w->b32);
   if (w->hst) cudaFreeHost(w->hst);
@@ -1760,46 +1628,6 @@ static esf_status solid_pcr_graph(SolidWork* w, int slot, long long S, const T* 
                          w->kChunk[slot], maxIt, st, out);
 }
 
-// One-pass FP32 inner solve of the solid system (A e = b32 from e = 0,
-// stopping on delta like the split path), chunks of 5 iterations as a graph.
-struct SolidFusedKernels {
-  long long S;
-  const float* blocks;
-  const int* nbr;
-  float4 *p0, *p1;
-  float *d, *x;
-  const float* invd;
-  double* partial;
-  PcrState* st;
-  void iteration(cudaStream_t cs) const {
-    ESF_COUNTED solid_iteration_fused<<<vec_blocks(S), VT, 0, cs>>>(S, blocks, nbr, p0, p1, p0, p1, d, x, invd,
-                                                                  partial, st);
-  }
-  void setup_warm(cudaStream_t) const {}
-  void setup_zero(cudaStream_t) const {}
-  void chunk(cudaStream_t cs, int n, bool) const {
-    for (int k = 0; k < n; k++) iteration(cs);
-  }
-};
-static esf_status solid_fused_solve(SolidWork* w, long long S, const int* nbr, double innerEps, int maxIt,
-                                    cudaStream_t st, PcrState* out) {
-  SolidFusedKernels k{S, w->blocks32, nbr, reinterpret_cast<float4*>(w->pk[0]),
-                      reinterpret_cast<float4*>(w->pk[1]), w->d32, w->x32, w->invd32, w->partial, w->st32};
-  const void* key[8] = {(const void*)(intptr_t)S, w->blocks32, nbr, w->pk[0], w->pk[1], w->d32, w->x32,
-                        w->invd32};
-  if (!w->gFused || memcmp(key, w->keyFused, sizeof key) != 0) {
-    esf_status e = capture(w->capStream, k, false, false, &w->gFused, &w->kFused);
-    if (e) return e;
-    memcpy(w->keyFused, key, sizeof key);
-  }
-  esf_status e = init_state(w->st32, innerEps, maxIt, st, 1);
-  if (e) return e;
-  ESF_COUNTED solid_fused_start<<<vec_blocks(S), VT, 0, st>>>(S, w->b32, w->invd32, k.p0, w->d32, w->x32);
-  k.iteration(st);  // set-up pass: s = A r, delta (alpha = beta = 0)
-  ESF_LAUNCH_CHECK();
-  return run_graph_solve(w->hst, w->ev, w->st32, nullptr, w->gFused, 0, w->kFused, maxIt, st, out);
-}
-
 esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const int* nbr,
                        const double* diag, const double* b, double* x, double eps, int maxIt,
                        int precision, double innerEps, int maxRefine, int* iters, double* relres,
@@ -1844,10 +1672,6 @@ esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const in
   int total = 0, ref = 0, conv = 0;
   double rel = 0;
   esf_status status = ESF_OK;
-  // inner solves: the one-pass FP32 iteration, or (ESF_SOLID_KERNEL=split)
-  // the reference's three kernels per iteration in FP32, for comparison
-  const char* pick = getenv("ESF_SOLID_KERNEL");
-  const bool oneP = !(pick && strcmp(pick, "split") == 0);
   for (ref = 0; ref <= maxRefine; ref++) {
     init_state(w->st, eps, maxIt, st);
     ESF_COUNTED solid_spmv<double, S_RESID64><<<vec_blocks(S), VT, 0, st>>>(S, blocks, nbr, x, b, w->r,
@@ -1868,10 +1692,9 @@ esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const in
     }
     if (ref == maxRefine || total >= maxIt) break;
     PcrState hi;
-    esf_status e = oneP ? solid_fused_solve(w, S, nbr, innerEps, maxIt - total, st, &hi)
-                        : solid_pcr_graph<float>(w, 1, S, w->blocks32, nbr, w->invd32, w->b32, w->x32,
-                                                 w->r32, w->d32, w->Ap32, w->s32, w->st32, innerEps,
-                                                 maxIt - total, st, &hi, 1);
+    esf_status e = solid_pcr_graph<float>(w, 1, S, w->blocks32, nbr, w->invd32, w->b32, w->x32, w->r32,
+                                          w->d32, w->Ap32, w->s32, w->st32, innerEps, maxIt - total,
+                                          st, &hi, 1);
     if (e) return e;
     total += hi.iter;
     if (hi.status) {
