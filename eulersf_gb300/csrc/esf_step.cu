@@ -11,6 +11,7 @@
 
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
+#include <chrono>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -35,6 +36,28 @@ void set_error(const char* fmt, ...) {
   vsnprintf(g_err, sizeof g_err, fmt, ap);
   va_end(ap);
 }
+
+// ESF_TRACE: host-clock breakdown inside a phase, printed to stderr. Each
+// mark synchronises the stream, so traced steps run slower; for finding
+// where a phase's time goes.
+struct TraceMarks {
+  cudaStream_t st;
+  bool on;
+  std::chrono::steady_clock::time_point t0;
+  explicit TraceMarks(cudaStream_t s) : st(s), on(getenv("ESF_TRACE") != nullptr) {
+    if (on) {
+      cudaStreamSynchronize(st);
+      t0 = std::chrono::steady_clock::now();
+    }
+  }
+  void mark(const char* what) {
+    if (!on) return;
+    cudaStreamSynchronize(st);
+    const auto t = std::chrono::steady_clock::now();
+    fprintf(stderr, "[esf]   %s %.3f ms\n", what, std::chrono::duration<double, std::milli>(t - t0).count());
+    t0 = t;
+  }
+};
 
 static int kblocks(long long n, int per = KT) {
   long long b = (n + per - 1) / per;
@@ -1058,12 +1081,19 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
   ESF_CUDA(cudaEventRecord(sc->ph[10], st));
   for (int i = 0; i < sc->ns; i++) TRY(compute_solid_mass(sc, sc->s[i], 1));
   ESF_CUDA(cudaEventRecord(sc->ph[11], st));
-  for (int i = 0; i < sc->ns; i++) TRY(advect_mesh(sc, sc->s[i]));
-  for (int i = 0; i < sc->ns; i++) {
-    TRY(compute_sdf(sc, sc->s[i]));
-    TRY(init_particles(sc, sc->s[i]));
+  {
+    TraceMarks tm(st);
+    for (int i = 0; i < sc->ns; i++) TRY(advect_mesh(sc, sc->s[i]));
+    tm.mark("mesh advection");
+    for (int i = 0; i < sc->ns; i++) {
+      TRY(compute_sdf(sc, sc->s[i]));
+      tm.mark("sdf");
+      TRY(init_particles(sc, sc->s[i]));
+      tm.mark("particles");
+    }
+    TRY(gather_solid_masses(sc));
+    tm.mark("gather solid masses");
   }
-  TRY(gather_solid_masses(sc));
   ESF_CUDA(cudaEventRecord(sc->ph[12], st));
   ESF_COUNTED k_advect_velocity<<<kblocks(G.T), KT, 0, st>>>(G, sc->solidMass, sc->vel, sc->vws, dt);
   std::swap(sc->vel, sc->vws);
