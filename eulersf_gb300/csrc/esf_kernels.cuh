@@ -3,6 +3,8 @@
 // cell flags, DOF maps, mass fractions and particle seeding reproduce the
 // reference's (non-FMA, x86-64) arithmetic bit for bit.
 #pragma once
+#include <climits>
+
 #include "esf_common.cuh"
 
 namespace esf {
@@ -271,21 +273,46 @@ __global__ void k_mass_gather(GridDev g, SolidDev s, Box cells, Box nodes) {
 
 // ------------------------------------------------------------- SDF (a18)
 // DEFOR_SOLID_3D::computeSDF (DEFOR_SOLID_3D.cpp:216-241): phi and the
-// bounding box of the massive nodes (ints: xmin ymin zmin -xmax -ymax -zmax).
-__global__ void k_phi_init(GridDev g, SolidDev s, double large, int* bbox) {
+// bounding box of the massive nodes (ints: xmin ymin zmin xmax ymax zmax).
+// The box is reduced per warp and per block first: one atomic per block and
+// bound instead of one per massive node (~237k nodes at 256^3 all hitting
+// the same six words).
+__global__ void __launch_bounds__(256) k_phi_init(GridDev g, SolidDev s, double large, int* bbox) {
+  __shared__ int sb[6];
+  if (threadIdx.x < 6) sb[threadIdx.x] = threadIdx.x < 3 ? INT_MAX : INT_MIN;
+  __syncthreads();
+  int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
   FOR_N(g.T, n) {
     if (s.mass[n] > 0) {
       s.phi[n] = -0.5;
-      int x = (int)(n % g.X), y = (int)((n / g.X) % g.Y), z = (int)(n / g.slab);
-      atomicMin(&bbox[0], x);
-      atomicMin(&bbox[1], y);
-      atomicMin(&bbox[2], z);
-      atomicMax(&bbox[3], x);
-      atomicMax(&bbox[4], y);
-      atomicMax(&bbox[5], z);
+      const int c[3] = {(int)(n % g.X), (int)((n / g.X) % g.Y), (int)(n / g.slab)};
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        lo[q] = min(lo[q], c[q]);
+        hi[q] = max(hi[q], c[q]);
+      }
     } else {
       s.phi[n] = large;
     }
+  }
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[q] = min(lo[q], __shfl_down_sync(0xffffffffu, lo[q], o));
+      hi[q] = max(hi[q], __shfl_down_sync(0xffffffffu, hi[q], o));
+    }
+  }
+  if ((threadIdx.x & 31) == 0 && lo[0] != INT_MAX) {
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      atomicMin(&sb[q], lo[q]);
+      atomicMax(&sb[3 + q], hi[q]);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 6 && sb[0] != INT_MAX) {
+    if (threadIdx.x < 3) atomicMin(&bbox[threadIdx.x], sb[threadIdx.x]);
+    else atomicMax(&bbox[threadIdx.x], sb[threadIdx.x]);
   }
 }
 

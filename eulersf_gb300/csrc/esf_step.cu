@@ -555,10 +555,12 @@ static esf_status compute_sdf(esf_scene* sc, Solid* d) {
   memcpy(sc->hInts, init, sizeof init);
   ESF_CUDA(cudaMemcpyAsync(sc->dInts, sc->hInts, sizeof init, cudaMemcpyHostToDevice, st));
   double large = G.X + G.Y + G.Z + 2;
-  ESF_COUNTED k_phi_init<<<kblocks(G.T), KT, 0, st>>>(G, d->d, large, sc->dInts);
+  TraceMarks tm(st);
+  ESF_COUNTED k_phi_init<<<kblocks(G.T), 256, 0, st>>>(G, d->d, large, sc->dInts);
   ESF_LAUNCH_CHECK();
   ESF_CUDA(cudaMemcpyAsync(sc->hInts, sc->dInts, sizeof init, cudaMemcpyDeviceToHost, st));
   ESF_CUDA(cudaStreamSynchronize(st));
+  tm.mark("sdf: phi and box");
   int xmin = sc->hInts[0], ymin = sc->hInts[1], zmin = sc->hInts[2];
   int xmax = sc->hInts[3], ymax = sc->hInts[4], zmax = sc->hInts[5];
   int tb = sc->p.tight_border, exn = sc->p.extrapolation_cells;
@@ -595,6 +597,7 @@ static esf_status compute_sdf(esf_scene* sc, Solid* d) {
                                                                         P, nullptr);
     }
   ESF_LAUNCH_CHECK();
+  tm.mark("sdf: 2 x sweepPhi");
   return ESF_OK;
 }
 
