@@ -514,6 +514,93 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep_tile(GridDev g, double*
     for (int e = 0; e < NC; e++) src[NC * n + e] = sv[NC * t + e];
   }
 }
+// A whole sweep pass in one cooperative launch: the blocks walk the pass's
+// hyperplanes a + b + c = p in order, each plane split over all threads, with
+// a grid-wide barrier between planes. Values written in this pass by other
+// blocks are read through L2 (ld.cg); the barrier is a counter and a
+// generation word in global memory, its wait bounded (a block that gives up
+// sets *err and carries on, so the launch always ends; the host reports it).
+// Same per-node operations as k_sweep_tile, each node after its three
+// upwind neighbours, so the same bits; the critical path is the 3n planes
+// rather than the tile wavefront's ~9n sub-planes.
+constexpr unsigned WAVE_WAIT_LIMIT = 1u << 22;
+__device__ __forceinline__ void wave_barrier(unsigned* bar, int* err) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    volatile unsigned* vb = bar;
+    const unsigned gen = vb[1];
+    if (atomicAdd(&bar[0], 1u) == gridDim.x - 1) {
+      bar[0] = 0;
+      __threadfence();
+      atomicAdd(&bar[1], 1u);
+    } else {
+      unsigned it = 0;
+      while (vb[1] == gen && ++it < WAVE_WAIT_LIMIT) {
+      }
+      if (it >= WAVE_WAIT_LIMIT) *err = 1;
+    }
+    __threadfence();
+  }
+  __syncthreads();
+}
+template <bool VEC>
+__global__ void __launch_bounds__(SWEEP_THREADS) k_sweep_wave(GridDev g, double* f, double* ph,
+                                                              const double* ms, Sweep w,
+                                                              const unsigned long long* ranks,
+                                                              unsigned* bar, int* err) {
+  const long long nij = (long long)w.ni * w.nj;
+  const int planes = w.ni + w.nj + w.nk - 2;
+  unsigned long long rx = 0, ry = 0, rz = 0;
+  if (VEC) {
+    rx = ranks[0];
+    ry = ranks[1];
+    rz = ranks[2];
+  }
+  for (int p = 0; p < planes; p++) {
+    for (long long t = blockIdx.x * (long long)SWEEP_THREADS + threadIdx.x; t < nij;
+         t += (long long)gridDim.x * SWEEP_THREADS) {
+      const int a = (int)(t % w.ni), b = (int)(t / w.ni);
+      const int c = p - a - b;
+      if (c < 0 || c >= w.nk) continue;
+      const int i = w.i0 + a * w.di, j = w.j0 + b * w.dj, k = w.k0 + c * w.dk;
+      const long long n = nidx(g, i, j, k);
+      if (ms[n] != 0) continue;
+      const long long ea = nidx(g, i - w.di, j, k), eb = nidx(g, i, j - w.dj, k), ec = nidx(g, i, j, k - w.dk);
+      if (!VEC) {
+        double v = __ldcg(ph + n);
+        solve_distance(__ldcg(ph + ea), __ldcg(ph + eb), __ldcg(ph + ec), &v);
+        ph[n] = v;
+        continue;
+      }
+      const unsigned long long rank = (unsigned long long)(a + (long long)b * w.ni + (long long)c * nij);
+      const double pn = ph[n];
+      double dp = pn - ph[ea], dpn = pn - ph[nidx(g, i + w.di, j, k)];
+      if (dp < 0 && dpn >= 0) continue;
+      double dq = pn - ph[eb], dqn = pn - ph[nidx(g, i, j + w.dj, k)];
+      if (dq < 0 && dqn >= 0) continue;
+      double dr = pn - ph[ec], drn = pn - ph[nidx(g, i, j, k + w.dk)];
+      if (dr < 0 && drn >= 0) continue;
+      if (rank >= rx) dp = 0;
+      if (rank >= ry) dq = 0;
+      if (rank >= rz) dr = 0;
+      double alpha, beta;
+      if (dp + dq + dr < 1e-3) {
+        alpha = 0.333;
+        beta = 0.333;
+      } else {
+        alpha = dp / (dp + dq + dr);
+        beta = dq / (dp + dq + dr);
+      }
+#pragma unroll
+      for (int e = 0; e < 3; e++)
+        f[3 * n + e] = (alpha * __ldcg(f + 3 * ea + e) + beta * __ldcg(f + 3 * eb + e)) +
+                       (1 - alpha - beta) * __ldcg(f + 3 * ec + e);
+    }
+    wave_barrier(bar, err);
+  }
+}
+
 // Launches of one sweep pass as a tile wavefront.
 inline int sweep_tile_launches(const Sweep& w) {
   return (w.ni + ST - 1) / ST + (w.nj + ST - 1) / ST + (w.nk + ST - 1) / ST - 2;

@@ -547,6 +547,62 @@ static esf_status compute_solid_mass(esf_scene* sc, Solid* d, int usesdf) {
   return ESF_OK;
 }
 
+// One Gauss-Seidel sweep pass (sweepPhi when !VEC, sweepOnePass of the
+// velocity when VEC): the cooperative hyperplane wave (k_sweep_wave, one
+// launch per pass) where the device runs cooperative launches, else the
+// tile wavefront (k_sweep_tile, ~3n/8 launches); ESF_SWEEP=tiles picks the
+// tile wavefront. Both give the bits of the sequential loop. A wave whose
+// grid barrier timed out raises the scene's sweep error word (dInts[42]),
+// checked when the step or init ends.
+constexpr int kSweepBar = 40, kSweepErr = 42;
+template <bool VEC>
+static esf_status sweep_pass(esf_scene* sc, Solid* d, const Sweep& w, const unsigned long long* ranks) {
+  cudaStream_t st = sc->stream;
+  static const int coopBlocks = [] {
+    int dev = 0, coop = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (!coop || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_wave<VEC>, SWEEP_THREADS, 0) !=
+                     cudaSuccess)
+      return 0;
+    return sms * per;
+  }();
+  const char* pick = getenv("ESF_SWEEP");
+  double* f = VEC ? d->d.vel : nullptr;
+  double* ph = d->d.phi;
+  const double* ms = d->d.mass;
+  if (coopBlocks > 0 && !(pick && strcmp(pick, "tiles") == 0)) {
+    const long long nij = (long long)w.ni * w.nj;
+    const int blocks = (int)std::min<long long>(coopBlocks, (nij + SWEEP_THREADS - 1) / SWEEP_THREADS);
+    unsigned* bar = reinterpret_cast<unsigned*>(sc->dInts + kSweepBar);
+    int* err = sc->dInts + kSweepErr;
+    ESF_CUDA(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st));
+    GridDev g = sc->g;
+    Sweep ww = w;
+    void* args[] = {&g, &f, &ph, (void*)&ms, &ww, (void*)&ranks, &bar, &err};
+    note_launch();
+    ESF_CUDA(cudaLaunchCooperativeKernel((const void*)k_sweep_wave<VEC>, dim3(blocks), dim3(SWEEP_THREADS),
+                                         args, 0, st));
+    return ESF_OK;
+  }
+  const int launches = sweep_tile_launches(w), blocks = sweep_tile_blocks(w);
+  for (int P = 0; P < launches; P++)
+    ESF_COUNTED k_sweep_tile<VEC><<<blocks, SWEEP_THREADS, 0, st>>>(sc->g, f, ph, ms, w, P, ranks);
+  ESF_LAUNCH_CHECK();
+  return ESF_OK;
+}
+// Reads the sweep error word (after the stream has been synchronised).
+static esf_status check_sweeps(esf_scene* sc) {
+  int e = 0;
+  ESF_CUDA(cudaMemcpy(&e, sc->dInts + kSweepErr, sizeof e, cudaMemcpyDeviceToHost));
+  if (e) {
+    set_error("a sweep's grid barrier timed out");
+    return ESF_ERR_CUDA;
+  }
+  return ESF_OK;
+}
+
 // computeSDF (DEFOR_SOLID_3D.cpp:216-268): phi, the boxes, 2 x sweepPhi.
 static esf_status compute_sdf(esf_scene* sc, Solid* d) {
   const GridDev& G = sc->g;
@@ -591,10 +647,7 @@ static esf_status compute_sdf(esf_scene* sc, Solid* d) {
       w.nj = ex.hi[1] - ex.lo[1] - 1;
       w.nk = ex.hi[2] - ex.lo[2] - 1;
       if (w.ni <= 0 || w.nj <= 0 || w.nk <= 0) continue;
-      const int launches = sweep_tile_launches(w), blocks = sweep_tile_blocks(w);
-      for (int P = 0; P < launches; P++)
-        ESF_COUNTED k_sweep_tile<false><<<blocks, SWEEP_THREADS, 0, st>>>(G, nullptr, d->d.phi, d->d.mass, w,
-                                                                        P, nullptr);
+      TRY(sweep_pass<false>(sc, d, w, nullptr));
     }
   ESF_LAUNCH_CHECK();
   tm.mark("sdf: 2 x sweepPhi");
@@ -726,6 +779,7 @@ extern "C" esf_status esf_init(esf_scene* sc) {
   }
   cudaSetDevice(sc->device);
   const GridDev& G = sc->g;
+  ESF_CUDA(cudaMemsetAsync(sc->dInts + kSweepErr, 0, sizeof(int), sc->stream));
   // DEFOR_SOLID_3D::init (DEFOR_SOLID_3D.cpp:269-331)
   for (int i = 0; i < sc->ns; i++) {
     Solid* d = sc->s[i];
@@ -745,6 +799,7 @@ extern "C" esf_status esf_init(esf_scene* sc) {
   TRY(gather_solid_masses(sc));
   TRY(recover_velocity(sc));
   ESF_CUDA(cudaStreamSynchronize(sc->stream));
+  TRY(check_sweeps(sc));
   sc->inited = true;
   return ESF_OK;
 }
@@ -840,6 +895,7 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
   const GridDev& G = sc->g;
   cudaStream_t st = sc->stream;
   sc->status = ESF_OK;
+  ESF_CUDA(cudaMemsetAsync(sc->dInts + kSweepErr, 0, sizeof(int), st));
   ESF_CUDA(cudaEventRecord(sc->e0, st));
   ESF_CUDA(cudaEventRecord(sc->ph[0], st));
   // ---- broad phase (COUPLED_INTEGRATOR_3D.cpp:378-411)
@@ -1054,10 +1110,7 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
         ESF_CUDA(cudaMemsetAsync(ranks, 0xff, 3 * 8, st));
         const long long total = (long long)w.ni * w.nj * w.nk;
         ESF_COUNTED k_sweep_vec_ranks<<<kblocks(total), KT, 0, st>>>(G, d->d.phi, d->d.mass, w, ranks);
-        const int launches = sweep_tile_launches(w), blocks = sweep_tile_blocks(w);
-        for (int P = 0; P < launches; P++)
-          ESF_COUNTED k_sweep_tile<true><<<blocks, SWEEP_THREADS, 0, st>>>(G, d->d.vel, d->d.phi, d->d.mass, w,
-                                                                         P, ranks);
+        TRY(sweep_pass<true>(sc, d, w, ranks));
       }
       for (int axis = 2; axis >= 0; axis--) {
         const long long nf = boxn(ex) / (ex.hi[axis] - ex.lo[axis]);
@@ -1108,6 +1161,7 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
   ESF_CUDA(cudaEventRecord(sc->ph[13], st));
   ESF_CUDA(cudaEventRecord(sc->e1, st));
   ESF_CUDA(cudaStreamSynchronize(st));
+  TRY(check_sweeps(sc));
   if (rep) {
     memset(rep, 0, sizeof *rep);
     rep->dt = dt;
