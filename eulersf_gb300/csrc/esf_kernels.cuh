@@ -316,7 +316,11 @@ __global__ void __launch_bounds__(256) k_phi_init(GridDev g, SolidDev s, double 
   }
 }
 
-// solveDistance (DEFOR_SOLID_3D.cpp:369-394)
+// solveDistance (DEFOR_SOLID_3D.cpp:369-394). The reference's loop tries
+// the 3-, 2- and 1-neighbour solutions in turn; the three candidates depend
+// only on the sorted inputs, so they are formed independently (their square
+// roots and divisions overlap instead of chaining) and the loop's tests are
+// replayed on them: the same operations on the same values, the same bits.
 __device__ __forceinline__ void solve_distance(double p, double q, double r, double* v) {
   // std::min / std::max semantics: (b < a) ? b : a
   double ds[3];
@@ -331,14 +335,20 @@ __device__ __forceinline__ void solve_distance(double p, double q, double r, dou
     b[x] = ds[x] + b[x - 1];
     c[x] = ds[x] * ds[x] + c[x - 1];
   }
-  int i = 2;
-  double discrim = b[i] * b[i] - (double)(i + 1) * c[i];
-  double nd = (b[i] + sqrt(discrim)) / (double)(i + 1);
-  while ((discrim < 0.0f || nd < ds[i]) && i != -1) {
-    i--;
-    if (i < 0) break;
-    discrim = b[i] * b[i] - (double)(i + 1) * c[i];
-    if (discrim > 0.0f) nd = (b[i] + sqrt(discrim)) / (double)(i + 1);
+  double dis[3], cand[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    dis[i] = b[i] * b[i] - (double)(i + 1) * c[i];
+    cand[i] = (b[i] + sqrt(dis[i])) / (double)(i + 1);
+  }
+  // the loop: i = 2 always takes its candidate; i = 1, 0 only when their
+  // discriminant is positive
+  double nd = cand[2];
+  if (dis[2] < 0.0f || nd < ds[2]) {
+    if (dis[1] > 0.0f) nd = cand[1];
+    if (dis[1] < 0.0f || nd < ds[1]) {
+      if (dis[0] > 0.0f) nd = cand[0];
+    }
   }
   if (nd < *v) *v = nd;
 }

@@ -549,9 +549,10 @@ static esf_status compute_solid_mass(esf_scene* sc, Solid* d, int usesdf) {
 
 // One Gauss-Seidel sweep pass (sweepPhi when !VEC, sweepOnePass of the
 // velocity when VEC): the cooperative hyperplane wave (k_sweep_wave, one
-// launch per pass) where the device runs cooperative launches, else the
-// tile wavefront (k_sweep_tile, ~3n/8 launches); ESF_SWEEP=tiles picks the
-// tile wavefront. Both give the bits of the sequential loop. A wave whose
+// launch per pass, sweepPhi) or the tile wavefront (k_sweep_tile, ~3n/8
+// launches, the velocity passes, and sweepPhi where the device has no
+// cooperative launch); ESF_SWEEP=wave or =tiles forces one for both. Both
+// give the bits of the sequential loop. A wave whose
 // grid barrier timed out raises the scene's sweep error word (dInts[42]),
 // checked when the step or init ends.
 constexpr int kSweepBar = 40, kSweepErr = 42;
@@ -568,11 +569,18 @@ static esf_status sweep_pass(esf_scene* sc, Solid* d, const Sweep& w, const unsi
       return 0;
     return sms * per;
   }();
+  // sweepPhi's per-node work (FP64 square roots and divisions) makes its
+  // critical path the cost: the wave (3n steps) beats the tiles (~9n
+  // sub-plane steps), 28.7 against 37.6 ms for 2 x 8 passes per 256^3 step.
+  // The velocity pass is a blend of three values: there the wave's grid
+  // barrier per plane costs more than the tiles' extra sub-planes in shared
+  // memory, 47.5 against 26.2 ms for 4 x 8 passes.
   const char* pick = getenv("ESF_SWEEP");
+  const bool wave = pick ? strcmp(pick, "wave") == 0 : !VEC;
   double* f = VEC ? d->d.vel : nullptr;
   double* ph = d->d.phi;
   const double* ms = d->d.mass;
-  if (coopBlocks > 0 && !(pick && strcmp(pick, "tiles") == 0)) {
+  if (coopBlocks > 0 && wave) {
     const long long nij = (long long)w.ni * w.nj;
     const int blocks = (int)std::min<long long>(coopBlocks, (nij + SWEEP_THREADS - 1) / SWEEP_THREADS);
     unsigned* bar = reinterpret_cast<unsigned*>(sc->dInts + kSweepBar);
