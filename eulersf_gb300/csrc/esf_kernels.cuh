@@ -316,11 +316,7 @@ __global__ void __launch_bounds__(256) k_phi_init(GridDev g, SolidDev s, double 
   }
 }
 
-// solveDistance (DEFOR_SOLID_3D.cpp:369-394). The reference's loop tries
-// the 3-, 2- and 1-neighbour solutions in turn; the three candidates depend
-// only on the sorted inputs, so they are formed independently (their square
-// roots and divisions overlap instead of chaining) and the loop's tests are
-// replayed on them: the same operations on the same values, the same bits.
+// solveDistance (DEFOR_SOLID_3D.cpp:369-394)
 __device__ __forceinline__ void solve_distance(double p, double q, double r, double* v) {
   // std::min / std::max semantics: (b < a) ? b : a
   double ds[3];
@@ -335,20 +331,14 @@ __device__ __forceinline__ void solve_distance(double p, double q, double r, dou
     b[x] = ds[x] + b[x - 1];
     c[x] = ds[x] * ds[x] + c[x - 1];
   }
-  double dis[3], cand[3];
-#pragma unroll
-  for (int i = 0; i < 3; i++) {
-    dis[i] = b[i] * b[i] - (double)(i + 1) * c[i];
-    cand[i] = (b[i] + sqrt(dis[i])) / (double)(i + 1);
-  }
-  // the loop: i = 2 always takes its candidate; i = 1, 0 only when their
-  // discriminant is positive
-  double nd = cand[2];
-  if (dis[2] < 0.0f || nd < ds[2]) {
-    if (dis[1] > 0.0f) nd = cand[1];
-    if (dis[1] < 0.0f || nd < ds[1]) {
-      if (dis[0] > 0.0f) nd = cand[0];
-    }
+  int i = 2;
+  double discrim = b[i] * b[i] - (double)(i + 1) * c[i];
+  double nd = (b[i] + sqrt(discrim)) / (double)(i + 1);
+  while ((discrim < 0.0f || nd < ds[i]) && i != -1) {
+    i--;
+    if (i < 0) break;
+    discrim = b[i] * b[i] - (double)(i + 1) * c[i];
+    if (discrim > 0.0f) nd = (b[i] + sqrt(discrim)) / (double)(i + 1);
   }
   if (nd < *v) *v = nd;
 }
@@ -527,30 +517,26 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep_tile(GridDev g, double*
 // A whole sweep pass in one cooperative launch: the blocks walk the pass's
 // hyperplanes a + b + c = p in order, each plane split over all threads, with
 // a grid-wide barrier between planes. Values written in this pass by other
-// blocks are read through L2 (ld.cg); the barrier is a counter and a
-// generation word in global memory, its wait bounded (a block that gives up
-// sets *err and carries on, so the launch always ends; the host reports it).
+// blocks are read through L2 (ld.cg); the barrier is one growing counter in
+// global memory, its wait bounded (a block that gives up sets *err and
+// carries on, so the launch always ends; the host reports it).
 // Same per-node operations as k_sweep_tile, each node after its three
 // upwind neighbours, so the same bits; the critical path is the 3n planes
 // rather than the tile wavefront's ~9n sub-planes.
 constexpr unsigned WAVE_WAIT_LIMIT = 1u << 22;
-__device__ __forceinline__ void wave_barrier(unsigned* bar, int* err) {
+// Arrival p of every block: a release add on a counter that only grows (the
+// host zeroes it before the launch), then acquire loads until it reaches
+// (p + 1) x blocks.
+__device__ __forceinline__ void wave_barrier(unsigned* count, unsigned target, int* err) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    __threadfence();
-    volatile unsigned* vb = bar;
-    const unsigned gen = vb[1];
-    if (atomicAdd(&bar[0], 1u) == gridDim.x - 1) {
-      bar[0] = 0;
-      __threadfence();
-      atomicAdd(&bar[1], 1u);
-    } else {
-      unsigned it = 0;
-      while (vb[1] == gen && ++it < WAVE_WAIT_LIMIT) {
-      }
-      if (it >= WAVE_WAIT_LIMIT) *err = 1;
-    }
-    __threadfence();
+    unsigned cur;
+    asm volatile("atom.add.release.gpu.global.u32 %0, [%1], 1;" : "=r"(cur) : "l"(count) : "memory");
+    cur += 1;
+    unsigned it = 0;
+    while (cur < target && ++it < WAVE_WAIT_LIMIT)
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(count) : "memory");
+    if (cur < target) *err = 1;
   }
   __syncthreads();
 }
@@ -607,7 +593,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep_wave(GridDev g, double*
         f[3 * n + e] = (alpha * __ldcg(f + 3 * ea + e) + beta * __ldcg(f + 3 * eb + e)) +
                        (1 - alpha - beta) * __ldcg(f + 3 * ec + e);
     }
-    wave_barrier(bar, err);
+    wave_barrier(bar, (unsigned)(p + 1) * gridDim.x, err);
   }
 }
 
