@@ -575,11 +575,57 @@ static esf_status sweep_pass(esf_scene* sc, Solid* d, const Sweep& w, const unsi
   // The velocity pass is a blend of three values: there the wave's grid
   // barrier per plane costs more than the tiles' extra sub-planes in shared
   // memory, 47.5 against 26.2 ms for 4 x 8 passes.
+  // one cluster of up to 16 blocks of 1024 threads, where the device
+  // schedules it (0: no cluster launch)
+  static const int clusterBlocks = [] {
+    for (int c = 16; c >= 8; c /= 2) {
+      if (c > 8 && cudaFuncSetAttribute(k_sweep_cluster<VEC>, cudaFuncAttributeNonPortableClusterSizeAllowed,
+                                        1) != cudaSuccess) {
+        cudaGetLastError();
+        continue;
+      }
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(c);
+      cfg.blockDim = dim3(CLUSTER_THREADS);
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = c;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int n = 0;
+      if (cudaOccupancyMaxActiveClusters(&n, k_sweep_cluster<VEC>, &cfg) == cudaSuccess && n > 0) return c;
+      cudaGetLastError();
+    }
+    return 0;
+  }();
   const char* pick = getenv("ESF_SWEEP");
-  const bool wave = pick ? strcmp(pick, "wave") == 0 : !VEC;
+  const bool wave = pick ? strcmp(pick, "wave") == 0 : false;
+  const bool cluster = pick ? strcmp(pick, "cluster") == 0 : true;
   double* f = VEC ? d->d.vel : nullptr;
   double* ph = d->d.phi;
   const double* ms = d->d.mass;
+  if (clusterBlocks > 0 && cluster) {
+    const long long nij = (long long)w.ni * w.nj;
+    long long want = (nij + CLUSTER_THREADS - 1) / CLUSTER_THREADS;
+    int blocks = clusterBlocks;
+    while (blocks > 1 && (blocks / 2) >= want) blocks /= 2;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(CLUSTER_THREADS);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = blocks;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    note_launch();
+    ESF_CUDA(cudaLaunchKernelEx(&cfg, k_sweep_cluster<VEC>, sc->g, f, ph, ms, w, ranks));
+    return ESF_OK;
+  }
   if (coopBlocks > 0 && wave) {
     const long long nij = (long long)w.ni * w.nj;
     const int blocks = (int)std::min<long long>(coopBlocks, (nij + SWEEP_THREADS - 1) / SWEEP_THREADS);
