@@ -540,8 +540,8 @@ __device__ __forceinline__ void wave_barrier(unsigned* count, unsigned target, i
   }
   __syncthreads();
 }
-template <bool VEC>
-__global__ void __launch_bounds__(SWEEP_THREADS) k_sweep_wave(GridDev g, double* f, double* ph,
+template <bool VEC, int NTH>
+__global__ void __launch_bounds__(NTH) k_sweep_wave(GridDev g, double* f, double* ph,
                                                               const double* ms, Sweep w,
                                                               const unsigned long long* ranks,
                                                               unsigned* bar, int* err) {
@@ -554,8 +554,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep_wave(GridDev g, double*
     rz = ranks[2];
   }
   for (int p = 0; p < planes; p++) {
-    for (long long t = blockIdx.x * (long long)SWEEP_THREADS + threadIdx.x; t < nij;
-         t += (long long)gridDim.x * SWEEP_THREADS) {
+    for (long long t = blockIdx.x * (long long)NTH + threadIdx.x; t < nij; t += (long long)gridDim.x * NTH) {
       const int a = (int)(t % w.ni), b = (int)(t / w.ni);
       const int c = p - a - b;
       if (c < 0 || c >= w.nk) continue;
@@ -594,71 +593,6 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep_wave(GridDev g, double*
                        (1 - alpha - beta) * __ldcg(f + 3 * ec + e);
     }
     wave_barrier(bar, (unsigned)(p + 1) * gridDim.x, err);
-  }
-}
-
-// A whole sweep pass in one thread-block cluster (up to 16 blocks of 1024
-// threads, co-scheduled by the hardware): the hyperplanes in order as in
-// k_sweep_wave, with the hardware cluster barrier (release/acquire at
-// cluster scope) between planes instead of a counter in global memory.
-// Every thread reaches every barrier (the plane loop has no early exit).
-constexpr int CLUSTER_THREADS = 1024;
-__device__ __forceinline__ void cluster_barrier() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-template <bool VEC>
-__global__ void __launch_bounds__(CLUSTER_THREADS) k_sweep_cluster(GridDev g, double* f, double* ph,
-                                                                   const double* ms, Sweep w,
-                                                                   const unsigned long long* ranks) {
-  const long long nij = (long long)w.ni * w.nj;
-  const int planes = w.ni + w.nj + w.nk - 2;
-  unsigned long long rx = 0, ry = 0, rz = 0;
-  if (VEC) {
-    rx = ranks[0];
-    ry = ranks[1];
-    rz = ranks[2];
-  }
-  for (int p = 0; p < planes; p++) {
-    for (long long t = blockIdx.x * (long long)CLUSTER_THREADS + threadIdx.x; t < nij;
-         t += (long long)gridDim.x * CLUSTER_THREADS) {
-      const int a = (int)(t % w.ni), b = (int)(t / w.ni);
-      const int c = p - a - b;
-      if (c < 0 || c >= w.nk) continue;
-      const int i = w.i0 + a * w.di, j = w.j0 + b * w.dj, k = w.k0 + c * w.dk;
-      const long long n = nidx(g, i, j, k);
-      if (ms[n] != 0) continue;
-      const long long ea = nidx(g, i - w.di, j, k), eb = nidx(g, i, j - w.dj, k), ec = nidx(g, i, j, k - w.dk);
-      if (!VEC) {
-        double v = __ldcg(ph + n);
-        solve_distance(__ldcg(ph + ea), __ldcg(ph + eb), __ldcg(ph + ec), &v);
-        ph[n] = v;
-        continue;
-      }
-      const unsigned long long rank = (unsigned long long)(a + (long long)b * w.ni + (long long)c * nij);
-      const double pn = ph[n];
-      double dp = pn - ph[ea], dpn = pn - ph[nidx(g, i + w.di, j, k)];
-      if (dp < 0 && dpn >= 0) continue;
-      double dq = pn - ph[eb], dqn = pn - ph[nidx(g, i, j + w.dj, k)];
-      if (dq < 0 && dqn >= 0) continue;
-      double dr = pn - ph[ec], drn = pn - ph[nidx(g, i, j, k + w.dk)];
-      if (dr < 0 && drn >= 0) continue;
-      if (rank >= rx) dp = 0;
-      if (rank >= ry) dq = 0;
-      if (rank >= rz) dr = 0;
-      double alpha, beta;
-      if (dp + dq + dr < 1e-3) {
-        alpha = 0.333;
-        beta = 0.333;
-      } else {
-        alpha = dp / (dp + dq + dr);
-        beta = dq / (dp + dq + dr);
-      }
-#pragma unroll
-      for (int e = 0; e < 3; e++)
-        f[3 * n + e] = (alpha * __ldcg(f + 3 * ea + e) + beta * __ldcg(f + 3 * eb + e)) +
-                       (1 - alpha - beta) * __ldcg(f + 3 * ec + e);
-    }
-    cluster_barrier();
   }
 }
 
