@@ -540,8 +540,8 @@ __device__ __forceinline__ void wave_barrier(unsigned* count, unsigned target, i
   }
   __syncthreads();
 }
-template <bool VEC, int NTH>
-__global__ void __launch_bounds__(NTH) k_sweep_wave(GridDev g, double* f, double* ph,
+template <bool VEC>
+__global__ void __launch_bounds__(SWEEP_THREADS) k_sweep_wave(GridDev g, double* f, double* ph,
                                                               const double* ms, Sweep w,
                                                               const unsigned long long* ranks,
                                                               unsigned* bar, int* err) {
@@ -554,7 +554,8 @@ __global__ void __launch_bounds__(NTH) k_sweep_wave(GridDev g, double* f, double
     rz = ranks[2];
   }
   for (int p = 0; p < planes; p++) {
-    for (long long t = blockIdx.x * (long long)NTH + threadIdx.x; t < nij; t += (long long)gridDim.x * NTH) {
+    for (long long t = blockIdx.x * (long long)SWEEP_THREADS + threadIdx.x; t < nij;
+         t += (long long)gridDim.x * SWEEP_THREADS) {
       const int a = (int)(t % w.ni), b = (int)(t / w.ni);
       const int c = p - a - b;
       if (c < 0 || c >= w.nk) continue;

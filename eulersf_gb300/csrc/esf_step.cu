@@ -559,32 +559,25 @@ constexpr int kSweepBar = 40, kSweepErr = 42;
 template <bool VEC>
 static esf_status sweep_pass(esf_scene* sc, Solid* d, const Sweep& w, const unsigned long long* ranks) {
   cudaStream_t st = sc->stream;
-  // blocks of WT threads per plane: small blocks spread a plane's FP64 work
-  // (square roots and divisions, slow on this part) over more SMs
-  const char* wt = getenv("ESF_WAVE_THREADS");
-  const int WT = wt ? atoi(wt) : 32;
-  auto coop_blocks = [](const void* k, int threads) {
+  static const int coopBlocks = [] {
     int dev = 0, coop = 0, sms = 0, per = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (!coop || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, threads, 0) != cudaSuccess) return 0;
+    if (!coop || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_wave<VEC>, SWEEP_THREADS, 0) !=
+                     cudaSuccess)
+      return 0;
     return sms * per;
-  };
-  static const int coop32 = coop_blocks((const void*)k_sweep_wave<VEC, 32>, 32);
-  static const int coop64 = coop_blocks((const void*)k_sweep_wave<VEC, 64>, 64);
-  static const int coop128 = coop_blocks((const void*)k_sweep_wave<VEC, 128>, 128);
-  const int coopBlocks = WT == 128 ? coop128 : WT == 64 ? coop64 : coop32;
-  const void* waveKernel = WT == 128 ? (const void*)k_sweep_wave<VEC, 128>
-                           : WT == 64 ? (const void*)k_sweep_wave<VEC, 64>
-                                      : (const void*)k_sweep_wave<VEC, 32>;
-  const int waveThreads = WT == 128 ? 128 : WT == 64 ? 64 : 32;
+  }();
   // sweepPhi's per-node work (FP64 square roots and divisions) makes its
   // critical path the cost: the wave (3n steps) beats the tiles (~9n
-  // sub-plane steps), 28.7 against 37.6 ms for 2 x 8 passes per 256^3 step.
-  // The velocity pass is a blend of three values: there the wave's grid
-  // barrier per plane costs more than the tiles' extra sub-planes in shared
-  // memory, 47.5 against 26.2 ms for 4 x 8 passes.
+  // sub-plane steps), 23.3 against 37.6 ms for 2 x 8 passes per 256^3 step
+  // (blocks of 32, 64 or 128 threads: the same). The velocity pass is a
+  // blend of three values: there the wave's ~5 us per plane (grid barrier,
+  // L2 round trips) costs more than the tiles' extra sub-planes in shared
+  // memory, 37.6 against 26.0 ms for 4 x 8 passes. One cluster of 8 blocks
+  // of 1024 threads with the hardware cluster barrier measured 82 ms for
+  // sweepPhi: FP64 work of a plane on 8 SMs.
   const char* pick = getenv("ESF_SWEEP");
   const bool wave = pick ? strcmp(pick, "wave") == 0 : !VEC;
   double* f = VEC ? d->d.vel : nullptr;
@@ -592,7 +585,7 @@ static esf_status sweep_pass(esf_scene* sc, Solid* d, const Sweep& w, const unsi
   const double* ms = d->d.mass;
   if (coopBlocks > 0 && wave) {
     const long long nij = (long long)w.ni * w.nj;
-    const int blocks = (int)std::min<long long>(coopBlocks, (nij + waveThreads - 1) / waveThreads);
+    const int blocks = (int)std::min<long long>(coopBlocks, (nij + SWEEP_THREADS - 1) / SWEEP_THREADS);
     unsigned* bar = reinterpret_cast<unsigned*>(sc->dInts + kSweepBar);
     int* err = sc->dInts + kSweepErr;
     ESF_CUDA(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st));
@@ -600,7 +593,8 @@ static esf_status sweep_pass(esf_scene* sc, Solid* d, const Sweep& w, const unsi
     Sweep ww = w;
     void* args[] = {&g, &f, &ph, (void*)&ms, &ww, (void*)&ranks, &bar, &err};
     note_launch();
-    ESF_CUDA(cudaLaunchCooperativeKernel(waveKernel, dim3(blocks), dim3(waveThreads), args, 0, st));
+    ESF_CUDA(cudaLaunchCooperativeKernel((const void*)k_sweep_wave<VEC>, dim3(blocks), dim3(SWEEP_THREADS),
+                                         args, 0, st));
     return ESF_OK;
   }
   const int launches = sweep_tile_launches(w), blocks = sweep_tile_blocks(w);
