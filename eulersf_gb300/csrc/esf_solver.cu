@@ -490,70 +490,6 @@ __global__ void add_correction(long long n, double* x, const float* e) {
     x[i] += (double)e[i];
 }
 
-// ---- FP64 vector kernels of the flexible-CG outer loop
-constexpr int FCG_MAXV = 12;
-struct DotArgs {  // out[q] = (a[q], b[q]) for q < k
-  const double* a[FCG_MAXV];
-  const double* b[FCG_MAXV];
-  int k;
-};
-__global__ void __launch_bounds__(256) vec_dots(long long n, DotArgs d, double* partial, unsigned* ticket,
-                                                double* out) {
-  __shared__ double sred[32];
-  __shared__ bool amLast;
-  double acc[FCG_MAXV];
-#pragma unroll
-  for (int q = 0; q < FCG_MAXV; q++) acc[q] = 0;
-  for (long long i = blockIdx.x * 256LL + threadIdx.x; i < n; i += (long long)gridDim.x * 256) {
-#pragma unroll
-    for (int q = 0; q < FCG_MAXV; q++)
-      if (q < d.k) acc[q] += d.a[q][i] * d.b[q][i];
-  }
-  const int nb = gridDim.x;
-#pragma unroll
-  for (int q = 0; q < FCG_MAXV; q++) {
-    if (q < d.k) {  // d.k is the same in every thread: the barriers inside stay uniform
-      const double v = block_sum<256>(acc[q], sred);
-      if (threadIdx.x == 0) partial[q * nb + blockIdx.x] = v;
-    }
-  }
-  if (threadIdx.x == 0) {
-    __threadfence();
-    amLast = atomicAdd(ticket, 1u) == (unsigned)nb - 1;
-  }
-  __syncthreads();
-  if (!amLast) return;
-  __threadfence();
-  for (int q = 0; q < d.k; q++) {
-    double a = 0;
-    for (int j = threadIdx.x; j < nb; j += 256) a += __ldcg(partial + q * nb + j);
-    const double t = block_sum<256>(a, sred);
-    if (threadIdx.x == 0) out[q] = t;
-  }
-  if (threadIdx.x == 0) *ticket = 0;
-}
-struct CombArgs {  // y = c0 y + sum_q c[q] x[q] (c0 = 0: y is not read)
-  const double* x[FCG_MAXV];
-  double c[FCG_MAXV];
-  int k;
-  double c0;
-};
-__global__ void __launch_bounds__(256) vec_combine(long long n, double* y, CombArgs a) {
-  for (long long i = blockIdx.x * 256LL + threadIdx.x; i < n; i += (long long)gridDim.x * 256) {
-    double v = a.c0 != 0.0 ? a.c0 * y[i] : 0.0;
-#pragma unroll
-    for (int q = 0; q < FCG_MAXV; q++)
-      if (q < a.k) v += a.c[q] * a.x[q][i];
-    y[i] = v;
-  }
-}
-// r32 = r/diag in FP32, the inner solve's start (as the FP64 residual
-// stencil forms it)
-__global__ void __launch_bounds__(256) inner_rhs(long long n, const double* r, const double* invd, float* r32) {
-  for (long long i = blockIdx.x * 256LL + threadIdx.x; i < n; i += (long long)gridDim.x * 256)
-    r32[i] = (float)(r[i] * invd[i]);
-}
-
 static int vec_blocks(long long n) {
   long long b = (n + VT - 1) / VT;
   int cap = 152 * 8;  // 8 resident blocks of 256 threads per SM
@@ -602,11 +538,6 @@ struct PressureWork {
   FusedMaps fmaps;
   bool fusedOk;
   MappedSet mapped;  // FP32 vectors mapped by vec_alloc
-  // flexible-CG outer loop: z, A z and a window of directions p and A p
-  // (FP64, allocated on first use); dot results on the device
-  double* fcg[2 + 2 * FCG_MAXV];
-  int fcgWindow;
-  double* dots;
 };
 
 // ---- FP32 vectors of the inner solves in compressible memory. They are
@@ -833,8 +764,6 @@ void pressure_work_free(PressureWork* w) {
     vec_free(&w->mapped, v);
   cudaFree(w->minv32);
   cudaFree(w->partial); cudaFree(w->st); cudaFree(w->st32); cudaFree(w->stT);
-  for (double* v : w->fcg) cudaFree(v);
-  cudaFree(w->dots);
   if (w->hst) cudaFreeHost(w->hst);
   if (w->gFirst) cudaGraphExecDestroy(w->gFirst);
   if (w->gChunk) cudaGraphExecDestroy(w->gChunk);
@@ -1252,177 +1181,10 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
     double target = (r2 > 0) ? 0.5 * eps * bnorm / sqrt(r2) : 0.0;  // predicted convergence
     return (target > t) ? target : t;
   };
-  const char* outerEnv = getenv("ESF_OUTER");
-  const bool fcgOuter = outerEnv && strcmp(outerEnv, "fcg") == 0;
   if (!(resid2 == resid2)) {
     status = ESF_ERR_NUMERIC;
   } else if (sqrt(resid2) < eps * bnorm) {
     conv = 1;
-  } else if (fcgOuter) {
-    // ---- flexible CG in FP64 around the FP32 inner solves: each inner
-    // solve's answer z is a search direction, A-orthogonalised against the
-    // last m directions (Notay's truncated FCG), so the outer iteration
-    // keeps what earlier inner solves found about the slow modes instead of
-    // restarting from the bare residual. r is the FP64 recursive residual;
-    // convergence is confirmed on the true residual.
-    const char* mEnv = getenv("ESF_FCG_M");
-    const char* capEnv = getenv("ESF_FCG_CAP");
-    const int m = std::max(1, std::min(FCG_MAXV - 2, mEnv ? atoi(mEnv) : 8));
-    const int cap = capEnv ? atoi(capEnv) : 0;
-    if (w->fcgWindow < m) {
-      for (int i = 0; i < 2 + 2 * FCG_MAXV; i++) {
-        if (!w->fcg[i] && i < 2 + 2 * m) ESF_CUDA(cudaMalloc(&w->fcg[i], g.R * 8));
-      }
-      if (!w->dots) ESF_CUDA(cudaMalloc(&w->dots, FCG_MAXV * 8));
-      w->fcgWindow = m;
-    }
-    double* z = w->fcg[0];
-    double* az = w->fcg[1];
-    double** P = w->fcg + 2;
-    double** AP = w->fcg + 2 + FCG_MAXV;
-    for (int i = 0; i < m; i++) {
-      if (!P[i]) ESF_CUDA(cudaMalloc(&P[i], g.R * 8));
-      if (!AP[i]) ESF_CUDA(cudaMalloc(&AP[i], g.R * 8));
-    }
-    double pAp[FCG_MAXV];
-    int nW = 0, head = 0;
-    const int vb = vec_blocks(g.R);
-    auto dots = [&](const DotArgs& d, double* out) -> esf_status {
-      ESF_COUNTED vec_dots<<<vb, 256, 0, st>>>(g.R, d, w->partial, &w->st->ticket[2], w->dots);
-      ESF_LAUNCH_CHECK();
-      ESF_CUDA(cudaMemcpyAsync(out, w->dots, d.k * 8, cudaMemcpyDeviceToHost, st));
-      ESF_CUDA(cudaStreamSynchronize(st));
-      return ESF_OK;
-    };
-    const bool trace = getenv("ESF_TRACE") != nullptr;
-    for (ref = 0; ref < maxRefine * 8 && total < maxIt; ref++) {
-      // inner solve of A e = r from e = 0 (r32 = r/diag is in place)
-      ESF_CUDA(cudaMemsetAsync(w->x32, 0, g.R * 4, st));
-      PcrState h;
-      memset(&h, 0, sizeof h);
-      h.eps = innerEps;
-      h.maxIt = maxIt;
-      h.iter = total;
-      h.setup = 1;
-      h.inner = 1;
-      h.cap = cap;
-      ESF_CUDA(cudaMemcpyAsync(w->st32, &h, sizeof h, cudaMemcpyHostToDevice, st));
-      ESF_CUDA(cudaStreamSynchronize(st));
-      esf_status e = inner_setup();
-      if (e) return e;
-      PcrState hi;
-      e = run_graph_solve(w->hst, w->ev, w->st32, nullptr, w->gChunk32, 0, w->kChunk32, maxIt, st, &hi);
-      if (e) return e;
-      total = hi.iter;
-      if (hi.status) {
-        status = (esf_status)hi.status;
-        break;
-      }
-      ESF_COUNTED convert_vec<float, double><<<vb, VT, 0, st>>>(g.R, w->x32, z);
-      e = pressure_apply<double>(g, minv64, z, az, st);
-      if (e) return e;
-      // p = z - sum gamma_j p_j, A p alike, gamma_j = (z, A p_j)/(p_j, A p_j)
-      const int slot = head % m;
-      CombArgs cp, cap2;
-      memset(&cp, 0, sizeof cp);
-      memset(&cap2, 0, sizeof cap2);
-      cp.x[0] = z;
-      cp.c[0] = 1.0;
-      cap2.x[0] = az;
-      cap2.c[0] = 1.0;
-      cp.k = cap2.k = 1;
-      if (nW > 0) {
-        DotArgs d;
-        memset(&d, 0, sizeof d);
-        for (int j = 0; j < nW; j++) {
-          const int sj = (head - 1 - j + m) % m;
-          d.a[j] = z;
-          d.b[j] = AP[sj];
-        }
-        d.k = nW;
-        double g_[FCG_MAXV];
-        e = dots(d, g_);
-        if (e) return e;
-        for (int j = 0; j < nW; j++) {
-          const int sj = (head - 1 - j + m) % m;
-          const double gam = g_[j] / pAp[sj];
-          cp.x[cp.k] = P[sj];
-          cp.c[cp.k++] = -gam;
-          cap2.x[cap2.k] = AP[sj];
-          cap2.c[cap2.k++] = -gam;
-        }
-      }
-      // the slot being replaced is not among the directions combined (nW < m
-      // or it is the oldest, j = m - 1, which the window drops): write it last
-      if (nW == m) {
-        cp.k--;
-        cap2.k--;
-      }
-      ESF_COUNTED vec_combine<<<vb, 256, 0, st>>>(g.R, P[slot], cp);
-      ESF_COUNTED vec_combine<<<vb, 256, 0, st>>>(g.R, AP[slot], cap2);
-      double pr[2];
-      {
-        DotArgs d;
-        memset(&d, 0, sizeof d);
-        d.a[0] = P[slot];
-        d.b[0] = AP[slot];
-        d.a[1] = P[slot];
-        d.b[1] = w->r;
-        d.k = 2;
-        e = dots(d, pr);
-        if (e) return e;
-      }
-      if (!(pr[0] > 0.0)) {
-        set_error("flexible CG: direction with (p, Ap) = %g", pr[0]);
-        status = ESF_ERR_NUMERIC;
-        break;
-      }
-      const double alpha = pr[1] / pr[0];
-      pAp[slot] = pr[0];
-      {
-        CombArgs c;
-        memset(&c, 0, sizeof c);
-        c.c0 = 1.0;
-        c.k = 1;
-        c.x[0] = P[slot];
-        c.c[0] = alpha;
-        ESF_COUNTED vec_combine<<<vb, 256, 0, st>>>(g.R, x, c);
-        c.x[0] = AP[slot];
-        c.c[0] = -alpha;
-        ESF_COUNTED vec_combine<<<vb, 256, 0, st>>>(g.R, w->r, c);
-      }
-      head++;
-      if (nW < m) nW++;
-      double rr;
-      {
-        DotArgs d;
-        memset(&d, 0, sizeof d);
-        d.a[0] = w->r;
-        d.b[0] = w->r;
-        d.k = 1;
-        e = dots(d, &rr);
-        if (e) return e;
-      }
-      rel = bnorm > 0 ? sqrt(rr) / bnorm : sqrt(rr);
-      if (trace) fprintf(stderr, "[esf] fcg %d: inner %d iters (total %d) rel %.3e\n", ref, hi.iter - h.iter, total, rel);
-      if (!(rr == rr)) {
-        status = ESF_ERR_NUMERIC;
-        break;
-      }
-      if (rel < eps) {
-        e = true_residual(&resid2, &bnorm2);
-        if (e) return e;
-        rel = bnorm > 0 ? sqrt(resid2) / bnorm : sqrt(resid2);
-        if (rel < eps) {
-          conv = 1;
-          ref++;
-          break;
-        }
-        nW = 0;  // the true residual replaces the recursive one: restart
-      } else {
-        ESF_COUNTED inner_rhs<<<vb, 256, 0, st>>>(g.R, w->r, w->invd, w->r32);
-      }
-    }
   } else {
     ESF_CUDA(cudaMemsetAsync(w->x32, 0, g.R * 4, st));
     {
