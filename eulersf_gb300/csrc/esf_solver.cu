@@ -1242,12 +1242,6 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
       hi.beta = 0.0;
       hi.setup = 1;
       hi.eps = trigger(resid2);
-      hi.cap = 0;
-      {
-        const char* capEnv = getenv("ESF_TAIL_CAP");
-        const int tailCap = capEnv ? atoi(capEnv) : 0;
-        if (tailCap > 0 && rel < 10.0 * eps) hi.cap = tailCap;
-      }
       memset(hi.ticket, 0, sizeof hi.ticket);
       ESF_CUDA(cudaMemcpyAsync(w->st32, &hi, sizeof hi, cudaMemcpyHostToDevice, st));
       ESF_CUDA(cudaStreamSynchronize(st));
