@@ -798,8 +798,15 @@ __global__ void k_grid_to_particle(GridDev g, SolidDev s, long long np, double* 
 // P2G binning: key = stencil base node shifted by +3 per axis on an
 // (X+3)(Y+3)(Z+3) lattice; particles whose stencil misses the grid get the
 // key `nkeys` (sorted last, never gathered).
-__global__ void k_p2g_keys(GridDev g, long long np, const double* part, unsigned int* keys,
-                           unsigned int* vals, int* pbox, double* pw) {
+// Keys, stencil weights and the particles' index box (reduced per warp and
+// block, one atomic per block and bound; the box words start at
+// +/- 2^30 on the host).
+__global__ void __launch_bounds__(256) k_p2g_keys(GridDev g, long long np, const double* part, unsigned int* keys,
+                                                  unsigned int* vals, int* pbox, double* pw) {
+  __shared__ int sb[6];
+  if (threadIdx.x < 6) sb[threadIdx.x] = threadIdx.x < 3 ? INT_MAX : INT_MIN;
+  __syncthreads();
+  int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
   const long long KX = g.X + 3, KY = g.Y + 3, KZ = g.Z + 3;
   FOR_N(np, c) {
     const double* P = part + 10 * c;
@@ -811,15 +818,34 @@ __global__ void k_p2g_keys(GridDev g, long long np, const double* part, unsigned
     unsigned int key = (unsigned int)(KX * KY * KZ);
     if (i >= -3 && i <= g.X - 1 && j >= -3 && j <= g.Y - 1 && k >= -3 && k <= g.Z - 1) {
       key = (unsigned int)((i + 3) + KX * ((j + 3) + KY * (k + 3)));
-      atomicMin(&pbox[0], i);
-      atomicMin(&pbox[1], j);
-      atomicMin(&pbox[2], k);
-      atomicMax(&pbox[3], i);
-      atomicMax(&pbox[4], j);
-      atomicMax(&pbox[5], k);
+      lo[0] = min(lo[0], i);
+      lo[1] = min(lo[1], j);
+      lo[2] = min(lo[2], k);
+      hi[0] = max(hi[0], i);
+      hi[1] = max(hi[1], j);
+      hi[2] = max(hi[2], k);
     }
     keys[c] = key;
     vals[c] = (unsigned int)c;
+  }
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[q] = min(lo[q], __shfl_down_sync(0xffffffffu, lo[q], o));
+      hi[q] = max(hi[q], __shfl_down_sync(0xffffffffu, hi[q], o));
+    }
+  }
+  if ((threadIdx.x & 31) == 0 && lo[0] != INT_MAX) {
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      atomicMin(&sb[q], lo[q]);
+      atomicMax(&sb[3 + q], hi[q]);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 6 && sb[0] != INT_MAX) {
+    if (threadIdx.x < 3) atomicMin(&pbox[threadIdx.x], sb[threadIdx.x]);
+    else atomicMax(&pbox[threadIdx.x], sb[threadIdx.x]);
   }
 }
 __global__ void k_bucket_bounds(long long np, const unsigned int* skeys, int* bstart, int* bend,

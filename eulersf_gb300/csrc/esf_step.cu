@@ -1062,6 +1062,7 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
   ESF_CUDA(cudaEventRecord(sc->ph[7], st));
   for (int i = 0; i < sc->ns; i++) {  // particleToGrid
     Solid* d = sc->s[i];
+    TraceMarks tm(st);
     ESF_CUDA(cudaMemsetAsync(d->d.mass, 0, G.T * 8, st));
     if (d->np == 0) continue;
     const long long np = d->np;
@@ -1076,8 +1077,9 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     int pinit[6] = {1 << 30, 1 << 30, 1 << 30, -(1 << 30), -(1 << 30), -(1 << 30)};
     memcpy(sc->hInts, pinit, sizeof pinit);
     ESF_CUDA(cudaMemcpyAsync(sc->dInts, sc->hInts, sizeof pinit, cudaMemcpyHostToDevice, st));
-    ESF_COUNTED k_p2g_keys<<<kblocks(np), KT, 0, st>>>(G, np, d->part.as<double>(), sc->keys.as<unsigned int>(),
+    ESF_COUNTED k_p2g_keys<<<kblocks(np), 256, 0, st>>>(G, np, d->part.as<double>(), sc->keys.as<unsigned int>(),
                                            sc->vals.as<unsigned int>(), sc->dInts, sc->pweights.as<double>());
+    tm.mark("p2g: keys and weights");
     int bits = 1;
     while (bits < 32 && (1ull << bits) <= nkeys) bits++;
     size_t tb = 0;
@@ -1086,6 +1088,7 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     TRY(sc->cubTmp.ensure(tb));
     cub::DeviceRadixSort::SortPairs(sc->cubTmp.p, tb, sc->keys.as<unsigned int>(), sc->skeys.as<unsigned int>(),
                                     sc->vals.as<unsigned int>(), sc->svals.as<unsigned int>(), (int)np, 0, bits, st);
+    tm.mark("p2g: sort");
     ESF_CUDA(cudaMemsetAsync(sc->bstart.p, 0, (size_t)nkeys * 4, st));
     ESF_CUDA(cudaMemsetAsync(sc->bend.p, 0, (size_t)nkeys * 4, st));
     ESF_COUNTED k_bucket_bounds<<<kblocks(np), KT, 0, st>>>(np, sc->skeys.as<unsigned int>(), sc->bstart.as<int>(),
@@ -1094,10 +1097,12 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     ESF_CUDA(cudaStreamSynchronize(st));
     Box nb = mkbox(std::max(sc->hInts[0], 0), std::max(sc->hInts[1], 0), std::max(sc->hInts[2], 0),
                    std::min(sc->hInts[3] + 4, G.X), std::min(sc->hInts[4] + 4, G.Y), std::min(sc->hInts[5] + 4, G.Z));
+    tm.mark("p2g: bucket bounds");
     if (boxn(nb) > 0)
       ESF_COUNTED k_p2g_gather<<<kblocks(boxn(nb)), KT, 0, st>>>(G, d->d, nb, d->part.as<double>(), sc->pweights.as<double>(), sc->svals.as<unsigned int>(),
                                                      sc->bstart.as<int>(), sc->bend.as<int>(), sc->p.flip_cutoff);
     ESF_LAUNCH_CHECK();
+    tm.mark("p2g: gather");
   }
   ESF_CUDA(cudaEventRecord(sc->ph[8], st));
   for (int i = 0; i < sc->ns; i++) {  // extendVectorField = 4 x sweepVectorField
