@@ -1467,59 +1467,6 @@ __global__ void __launch_bounds__(VT) solid_spmv(long long S, const T* __restric
   }
 }
 
-// Lower half of the (symmetric) solid system in FP32 for the inner solves:
-// blocks j = 0..13 of the 27 (j = 13 the diagonal block; the mirror of
-// neighbour j is 26 - j), entry je = 9 j + e of row a at
-// ((a / 32) * 126 + je) * 32 + a % 32. Block (a, j) for j > 13 is the
-// transpose of block (m, 26 - j), m the neighbour: read from row m.
-ESF_HD long long half_at(long long a, int je) { return (((a >> 5) * 126 + je) << 5) + (a & 31); }
-__global__ void solid_half_from_full(long long S, const double* __restrict__ full, float* __restrict__ half) {
-  const long long n = rows32(S) * 126;
-  for (long long t = blockIdx.x * (long long)VT + threadIdx.x; t < n; t += (long long)gridDim.x * VT) {
-    const long long a = ((t >> 5) / 126) * 32 + (t & 31);
-    const int je = (int)((t >> 5) % 126);
-    half[t] = (float)full[blk_at(a, je)];
-  }
-}
-// s = A r with the half matrix and r.s, as solid_spmv<float, S_UPDATE>.
-__global__ void __launch_bounds__(VT) solid_spmv_half(long long S, const float* __restrict__ half,
-                                                      const int* __restrict__ nbr, const float* in,
-                                                      float* out, double* partial, PcrState* st) {
-  __shared__ double sred[32];
-  if (st->done) return;
-  float accT = 0;
-  for (long long a = blockIdx.x * (long long)VT + threadIdx.x; a < S; a += (long long)gridDim.x * VT) {
-    float y0 = 0, y1 = 0, y2 = 0;
-    const int* nb = nbr + nbr_at(a, 0);
-#pragma unroll 9
-    for (int j = 0; j < 27; j++) {
-      const int m = __ldg(nb + 32 * j);
-      if (m >= 0) {
-        const float v0 = in[3 * (long long)m], v1 = in[3 * (long long)m + 1], v2 = in[3 * (long long)m + 2];
-        if (j <= 13) {
-          const float* B = half + half_at(a, 9 * j);
-          y0 += B[0] * v0 + B[32] * v1 + B[64] * v2;
-          y1 += B[96] * v0 + B[128] * v1 + B[160] * v2;
-          y2 += B[192] * v0 + B[224] * v1 + B[256] * v2;
-        } else {
-          const float* B = half + half_at(m, 9 * (26 - j));  // transpose of the mirror block
-          y0 += B[0] * v0 + B[96] * v1 + B[192] * v2;
-          y1 += B[32] * v0 + B[128] * v1 + B[224] * v2;
-          y2 += B[64] * v0 + B[160] * v1 + B[256] * v2;
-        }
-      }
-    }
-    out[3 * a] = y0;
-    out[3 * a + 1] = y1;
-    out[3 * a + 2] = y2;
-    accT += in[3 * a] * y0 + in[3 * a + 1] * y1 + in[3 * a + 2] * y2;
-  }
-  const double bs = block_sum<VT>((double)accT, sred);
-  double total;
-  if (last_block_sum<VT>(bs, partial, &st->ticket[1], gridDim.x, &total, sred) && threadIdx.x == 0)
-    finish_update(st, total);
-}
-
 // x += alpha d; r -= alpha Ap/diag (pointwise part of phase B).
 template <typename T>
 __global__ void __launch_bounds__(VT) pcr_update_xr(long long n, T* x, const T* d, T* r, const T* Ap,
@@ -1568,9 +1515,9 @@ esf_status solid_work_alloc(SolidWork** out, long long S, int mixed) {
   for (int i = 0; i < 4; i++) ESF_CUDA(cudaEventCreateWithFlags(&w->ev[i], cudaEventDisableTiming));
   ESF_CUDA(cudaStreamCreateWithFlags(&w->capStream, cudaStreamNonBlocking));
   if (mixed) {
-    // the FP32 lower half of the blocks (solid_spmv_half) in compressible
-    // memory
-    esf_status e = vec_alloc(&w->mapped, &w->blocks32, rows32(w->cap) * 126 * 4);
+    // the FP32 blocks in compressible memory: 166 against 171 ms of solid
+    // solves per 256^3 step with cudaMalloc
+    esf_status e = vec_alloc(&w->mapped, &w->blocks32, rows32(w->cap) * 243 * 4);
     if (e) return e;
     ESF_CUDA(cudaMalloc(&w->x32, n * 4));
     ESF_CUDA(cudaMalloc(&w->r32, n * 4));
@@ -1613,19 +1560,11 @@ struct SolidKernels {
   T *x, *r, *d, *Ap, *s;
   double* partial;
   PcrState* st;
-  // s = A r and r.s: FP32 inner solves use the lower-half matrix
-  void spmv_update(cudaStream_t cs) const {
-    if constexpr (std::is_same<T, float>::value) {
-      ESF_COUNTED solid_spmv_half<<<vec_blocks(S), VT, 0, cs>>>(S, blocks, nbr, r, s, partial, st);
-    } else {
-      ESF_COUNTED solid_spmv<T, S_UPDATE><<<vec_blocks(S), VT, 0, cs>>>(S, blocks, nbr, r, nullptr, nullptr, s,
-                                                                        nullptr, partial, st);
-    }
-  }
   void setup_zero(cudaStream_t cs) const {
     const long long n = 3 * S;
     ESF_COUNTED pcr_zero_start<T><<<vec_blocks(n), VT, 0, cs>>>(n, b, invd, x, r, d, Ap, partial, st);
-    spmv_update(cs);
+    ESF_COUNTED solid_spmv<T, S_UPDATE><<<vec_blocks(S), VT, 0, cs>>>(S, blocks, nbr, r, nullptr, nullptr, s,
+                                                                      nullptr, partial, st);
   }
   void chunk(cudaStream_t cs, int n_it, bool check) const {
     const long long n = 3 * S;
@@ -1633,7 +1572,8 @@ struct SolidKernels {
     for (int k = 0; k < n_it; k++) {
       ESF_COUNTED pcr_phase_a<T, false><<<vb, VT, 0, cs>>>(n, d, r, Ap, s, invd, partial, st);
       ESF_COUNTED pcr_update_xr<T><<<vb, VT, 0, cs>>>(n, x, d, r, Ap, invd, st);
-      spmv_update(cs);
+      ESF_COUNTED solid_spmv<T, S_UPDATE><<<sb, VT, 0, cs>>>(S, blocks, nbr, r, nullptr, nullptr, s, nullptr,
+                                                             partial, st);
     }
     if (check)
       ESF_COUNTED solid_spmv<T, S_CHECK><<<sb, VT, 0, cs>>>(S, blocks, nbr, x, b, nullptr, nullptr, nullptr,
@@ -1715,7 +1655,8 @@ esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const in
     return h.status ? (esf_status)h.status : ESF_OK;
   }
   // mixed: FP32 blocks; x starts at 0 as in the assembled reference variant
-  ESF_COUNTED solid_half_from_full<<<vec_blocks(rows32(S) * 126), VT, 0, st>>>(S, blocks, w->blocks32);
+  ESF_COUNTED convert_vec<double, float><<<vec_blocks(rows32(S) * 243), VT, 0, st>>>(rows32(S) * 243, blocks,
+                                                                                   w->blocks32);
   ESF_CUDA(cudaMemsetAsync(x, 0, n * 8, st));
   double bnorm2 = 0;
   {
