@@ -860,21 +860,9 @@ __global__ void k_bucket_bounds(long long np, const unsigned int* skeys, int* bs
 // DEFOR_SOLID_3D::particleToGrid (DEFOR_SOLID_3D.cpp:1036-1107) as a
 // per-node gather over the 4^3 buckets whose stencils reach the node, in
 // bucket order then particle order (deterministic).
-// The particles' P2G data in sorted (bucket, then particle) order: per
-// sorted slot e, the 12 stencil weights and the velocity of particle
-// sval[e], so the gather below reads each bucket contiguously.
-__global__ void k_p2g_sorted(long long np, const double* part, const double* pw, const unsigned int* sval,
-                             double* spw, double* svel) {
-  FOR_N(np, e) {
-    const long long pi = sval[e];
-#pragma unroll
-    for (int q = 0; q < 12; q++) spw[12 * e + q] = pw[12 * pi + q];
-#pragma unroll
-    for (int q = 0; q < 3; q++) svel[3 * e + q] = part[10 * pi + 3 + q];
-  }
-}
-__global__ void k_p2g_gather(GridDev g, SolidDev s, Box nodes, const double* spw, const double* svel,
-                             const int* bstart, const int* bend, int cutoff) {
+__global__ void k_p2g_gather(GridDev g, SolidDev s, Box nodes, const double* part,
+                             const double* pw, const unsigned int* sval, const int* bstart,
+                             const int* bend, int cutoff) {
   const long long KX = g.X + 3, KY = g.Y + 3;
   FOR_BOX(nodes, x, y, z) {
     double acc[4] = {0, 0, 0, 0};
@@ -887,13 +875,14 @@ __global__ void k_p2g_gather(GridDev g, SolidDev s, Box nodes, const double* spw
           int b0 = bstart[key], b1 = bend[key];
           const int ox = x - bx, oy = 4 + y - by, oz = 8 + z - bz;
           for (int e = b0; e < b1; e++) {
-            const double* W = spw + 12 * (long long)e;
-            const double* V = svel + 3 * (long long)e;
+            const long long pi = sval[e];
+            const double* P = part + 10 * pi;
+            const double* W = pw + 12 * pi;
             double w = W[ox] * W[oy] * W[oz];
             touched = true;
-            acc[0] += w * V[0];
-            acc[1] += w * V[1];
-            acc[2] += w * V[2];
+            acc[0] += w * P[3];
+            acc[1] += w * P[4];
+            acc[2] += w * P[5];
             acc[3] += w;
           }
         }

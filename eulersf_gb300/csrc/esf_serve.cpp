@@ -197,9 +197,7 @@ extern "C" size_t esf_scene_footprint(const esf_grid* g, const esf_params* p, in
     double cells = 1.0;
     for (int q = 0; q < 3; q++) cells *= std::max(0.0, (hi[q] - lo[q]) / g->dh + 2.0);
     const double solidNodes = 0.55 * cells;  // sphere / box volume, plus a margin
-    // particles: the fitted 80 bytes, plus the P2G gather's sorted copy of
-    // their weights and velocities (120 bytes)
-    bytes += solidNodes * (27 * 9 * 8 * 1.5 + 27 * 4 + 400) + solidNodes * p->particles_per_cell * 200.0;
+    bytes += solidNodes * (27 * 9 * 8 * 1.5 + 27 * 4 + 400) + solidNodes * p->particles_per_cell * 80.0;
   }
   return (size_t)(bytes * 1.1) + (140u << 20);
 }

@@ -142,7 +142,7 @@ struct esf_scene {
   esf::DBuf sNode, solidF, solidMv, damped, solidV0, solidPC, solidB1, sysDiag, blocks, nbr, mask;
   esf::DBuf Ke, nf, energy;
   // scratch
-  esf::DBuf cubTmp, keys, vals, skeys, svals, bstart, bend, mt, pweights, spweights, svel;
+  esf::DBuf cubTmp, keys, vals, skeys, svals, bstart, bend, mt, pweights;
   long long mtLen = 0;
   int *dInts = nullptr, *hInts = nullptr;
   unsigned long long* dU64 = nullptr;
@@ -346,7 +346,7 @@ extern "C" esf_status esf_destroy(esf_scene* s) {
   DBuf* bufs[] = {&s->sNode, &s->solidF, &s->solidMv, &s->damped, &s->solidV0, &s->solidPC,
                   &s->solidB1, &s->sysDiag, &s->blocks, &s->nbr, &s->mask, &s->Ke, &s->nf,
                   &s->energy, &s->cubTmp, &s->keys, &s->vals, &s->skeys, &s->svals, &s->bstart,
-                  &s->bend, &s->mt, &s->pweights, &s->spweights, &s->svel};
+                  &s->bend, &s->mt, &s->pweights};
   for (DBuf* b : bufs) b->release();
   pressure_work_free(s->pw);
   solid_work_free(s->sw);
@@ -1074,8 +1074,6 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     TRY(sc->bstart.ensure((size_t)nkeys * 4));
     TRY(sc->bend.ensure((size_t)nkeys * 4));
     TRY(sc->pweights.ensure((size_t)np * 96));
-    TRY(sc->spweights.ensure((size_t)np * 96));
-    TRY(sc->svel.ensure((size_t)np * 24));
     int pinit[6] = {1 << 30, 1 << 30, 1 << 30, -(1 << 30), -(1 << 30), -(1 << 30)};
     memcpy(sc->hInts, pinit, sizeof pinit);
     ESF_CUDA(cudaMemcpyAsync(sc->dInts, sc->hInts, sizeof pinit, cudaMemcpyHostToDevice, st));
@@ -1099,14 +1097,10 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     ESF_CUDA(cudaStreamSynchronize(st));
     Box nb = mkbox(std::max(sc->hInts[0], 0), std::max(sc->hInts[1], 0), std::max(sc->hInts[2], 0),
                    std::min(sc->hInts[3] + 4, G.X), std::min(sc->hInts[4] + 4, G.Y), std::min(sc->hInts[5] + 4, G.Z));
-    ESF_COUNTED k_p2g_sorted<<<kblocks(np), KT, 0, st>>>(np, d->part.as<double>(), sc->pweights.as<double>(),
-                                                         sc->svals.as<unsigned int>(), sc->spweights.as<double>(),
-                                                         sc->svel.as<double>());
-    tm.mark("p2g: bucket bounds, sorted copy");
+    tm.mark("p2g: bucket bounds");
     if (boxn(nb) > 0)
-      ESF_COUNTED k_p2g_gather<<<kblocks(boxn(nb)), KT, 0, st>>>(G, d->d, nb, sc->spweights.as<double>(),
-                                                                 sc->svel.as<double>(), sc->bstart.as<int>(),
-                                                                 sc->bend.as<int>(), sc->p.flip_cutoff);
+      ESF_COUNTED k_p2g_gather<<<kblocks(boxn(nb)), KT, 0, st>>>(G, d->d, nb, d->part.as<double>(), sc->pweights.as<double>(), sc->svals.as<unsigned int>(),
+                                                     sc->bstart.as<int>(), sc->bend.as<int>(), sc->p.flip_cutoff);
     ESF_LAUNCH_CHECK();
     tm.mark("p2g: gather");
   }
