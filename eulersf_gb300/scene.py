@@ -74,7 +74,7 @@ class SolidDesc:
 
 @dataclass
 class SceneDesc:
-    """One coupled scene (the rubber-ball family of BASELINE-style configs)."""
+    """One coupled scene (the rubber-ball family of the benchmark configurations)."""
     N: int = 64
     solids: list = field(default_factory=lambda: [SolidDesc()])
     fluid_height: float = 0.3

@@ -31,7 +31,7 @@ def scenes():
     """name -> (SceneDesc, frames)."""
     out = {}
     out["ball16"] = (SceneDesc(N=16, mass_sample_dh=(1 / 16) / 4), 3)
-    # vorticity confinement and buoyancy on (the BASELINE scenes turn both off)
+    # vorticity confinement and buoyancy on (the benchmark scenes turn both off)
     out["ball20_vort"] = (SceneDesc(N=20, mass_sample_dh=(1 / 20) / 4, vorticity_eps=1.5,
                                     buoyancy=0.1, noise_seed=3), 2)
     # ball resting one cell above the floor, moving down: CFL factor 0.6 and
