@@ -130,11 +130,16 @@ def barrier(pg):
         pg.barrier()
 
 
+def _reduce_device(pg):
+    # NCCL reduces device tensors; gloo (ESF_BENCH_GLOO, the CPU tests) host ones
+    return "cuda" if pg.get_backend() == "nccl" else "cpu"
+
+
 def max_over_ranks(pg, v):
     if pg is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    t = torch.tensor([v], dtype=torch.float64, device=_reduce_device(pg))
     pg.all_reduce(t, op=pg.ReduceOp.MAX)
     return float(t.item())
 
@@ -143,7 +148,7 @@ def sum_over_ranks(pg, v):
     if pg is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    t = torch.tensor([v], dtype=torch.float64, device=_reduce_device(pg))
     pg.all_reduce(t)
     return float(t.item())
 

@@ -131,3 +131,69 @@ def test_server_without_gpu_and_footprint_model(lib):
         q, keep = request_for(SceneDesc(N=n), 1)
         sizes.append(lib.esf_scene_footprint(C.byref(q.grid), C.byref(q.params), q.num_solids, q.solids))
     assert 0 < sizes[0] < sizes[1] and sizes[1] > 2 * sizes[0]
+
+
+def _free_port():
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port, out):
+    import os
+    os.environ.update({"RANK": str(rank), "WORLD_SIZE": str(world), "LOCAL_RANK": str(rank),
+                       "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port), "ESF_BENCH_GLOO": "1"})
+    import bench
+    r, w, pg = bench.dist_setup(world)
+    bench.barrier(pg)
+    mx = bench.max_over_ranks(pg, 10.0 * (r + 1))
+    sm = bench.sum_over_ranks(pg, float(r + 1))
+    bench.barrier(pg)
+    out.put((r, w, mx, sm))
+    pg.destroy_process_group()
+
+
+def test_bench_rank_reductions_two_ranks_gloo():
+    """bench.py's replica bookkeeping on two gloo ranks: every rank sees the
+    maximum time and the summed work of all ranks."""
+    import multiprocessing as mp
+    import os
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert res == [(0, 2, 20.0, 3.0), (1, 2, 20.0, 3.0)]
+
+
+def test_reference_arm_two_ranks_prints_one_line(tmp_path):
+    """`bench.py --impl reference` launched as two ranks (torchrun, gloo):
+    rank 0 times the CPU port and prints the one JSON line, the other rank
+    exits 0 without work."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, ESF_BENCH_GLOO="1", OMP_NUM_THREADS="2")
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
+           "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), "bench.py",
+           "--impl", "reference", "--gpus", "2", "--size", "24", "--steps", "1", "--warmup", "0",
+           "--cpu-iters", "2"]
+    p = subprocess.run(cmd, cwd=root, env=env, capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [l for l in p.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, p.stdout
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
