@@ -410,10 +410,11 @@ __global__ void k_sweep_vec_ranks(GridDev g, const double* ph, const double* ms,
 // none of which change during the pass, so they are formed up front.
 constexpr int ST = 8;           // tile edge
 constexpr int SP = ST + 1;      // tile plus the upwind layer
-constexpr int SWEEP_THREADS = 128;
-static_assert(ST * ST <= SWEEP_THREADS, "one thread per (a', b') of a tile");
+constexpr int SWEEP_THREADS = 128;  // blocks of the wave kernel
+constexpr int TILE_THREADS = ST * ST * ST;  // one thread per node of a tile
+static_assert(ST * ST <= TILE_THREADS, "one thread per (a', b') of a tile");
 template <bool VEC>
-__global__ void __launch_bounds__(SWEEP_THREADS) k_sweep_tile(GridDev g, double* f, double* ph,
+__global__ void __launch_bounds__(TILE_THREADS) k_sweep_tile(GridDev g, double* f, double* ph,
                                                               const double* ms, Sweep w, int P,
                                                               const unsigned long long* ranks) {
   constexpr int NC = VEC ? 3 : 1;
@@ -428,7 +429,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep_tile(GridDev g, double*
   double* const src = VEC ? f : ph;
   // tile and upwind layers: local -1 .. n-1 on each axis (local -1 of the
   // first tile is the node before the pass's first, inside the box)
-  for (int t = threadIdx.x; t < SP * SP * SP; t += SWEEP_THREADS) {
+  for (int t = threadIdx.x; t < SP * SP * SP; t += TILE_THREADS) {
     const int la = t % SP - 1, lb = (t / SP) % SP - 1, lc = t / (SP * SP) - 1;
     if (la >= na || lb >= nb || lc >= nc) continue;
     const long long n = nidx(g, w.i0 + (a0 + la) * w.di, w.j0 + (b0 + lb) * w.dj, w.k0 + (c0 + lc) * w.dk);
@@ -437,7 +438,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep_tile(GridDev g, double*
   }
   // per node of the tile: update or not, and (VEC) the blend weights
   const long long nij = (long long)w.ni * w.nj;
-  for (int t = threadIdx.x; t < ST * ST * ST; t += SWEEP_THREADS) {
+  for (int t = threadIdx.x; t < ST * ST * ST; t += TILE_THREADS) {
     const int la = t % ST, lb = (t / ST) % ST, lc = t / (ST * ST);
     unsigned char upd = 0;
     if (la < na && lb < nb && lc < nc) {
@@ -506,7 +507,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep_tile(GridDev g, double*
     }
     __syncthreads();
   }
-  for (int t = threadIdx.x; t < SP * SP * SP; t += SWEEP_THREADS) {
+  for (int t = threadIdx.x; t < SP * SP * SP; t += TILE_THREADS) {
     const int ta = t % SP - 1, tb = (t / SP) % SP - 1, tc = t / (SP * SP) - 1;
     if (ta < 0 || tb < 0 || tc < 0 || ta >= na || tb >= nb || tc >= nc) continue;
     const long long n = nidx(g, w.i0 + (a0 + ta) * w.di, w.j0 + (b0 + tb) * w.dj, w.k0 + (c0 + tc) * w.dk);

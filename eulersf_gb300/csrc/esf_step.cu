@@ -599,7 +599,7 @@ static esf_status sweep_pass(esf_scene* sc, Solid* d, const Sweep& w, const unsi
   }
   const int launches = sweep_tile_launches(w), blocks = sweep_tile_blocks(w);
   for (int P = 0; P < launches; P++)
-    ESF_COUNTED k_sweep_tile<VEC><<<blocks, SWEEP_THREADS, 0, st>>>(sc->g, f, ph, ms, w, P, ranks);
+    ESF_COUNTED k_sweep_tile<VEC><<<blocks, TILE_THREADS, 0, st>>>(sc->g, f, ph, ms, w, P, ranks);
   ESF_LAUNCH_CHECK();
   return ESF_OK;
 }
