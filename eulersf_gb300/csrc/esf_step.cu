@@ -575,7 +575,7 @@ static esf_status sweep_pass(esf_scene* sc, Solid* d, const Sweep& w, const unsi
   // (blocks of 32, 64 or 128 threads: the same). The velocity pass is a
   // blend of three values: there the wave's ~5 us per plane (grid barrier,
   // L2 round trips) costs more than the tiles' extra sub-planes in shared
-  // memory, 37.6 against 26.0 ms for 4 x 8 passes. One cluster of 8 blocks
+  // memory, 37.6 against 21.1 ms for 4 x 8 passes. One cluster of 8 blocks
   // of 1024 threads with the hardware cluster barrier measured 82 ms for
   // sweepPhi: FP64 work of a plane on 8 SMs.
   const char* pick = getenv("ESF_SWEEP");
