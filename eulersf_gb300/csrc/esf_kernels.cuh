@@ -720,7 +720,7 @@ struct ContactParams {
 
 // DEFOR_SOLID_3D::gridToParticle (DEFOR_SOLID_3D.cpp:891-1034): FLIP/PIC
 // blend, wall contact impulses, then p += v dt.
-__global__ void __launch_bounds__(256, 4) k_grid_to_particle(GridDev g, SolidDev s, long long np, double* part,
+__global__ void k_grid_to_particle(GridDev g, SolidDev s, long long np, double* part,
                                    ContactParams cp, const double* const* otherPhi, int nOther,
                                    int* unsupported) {
   FOR_N(np, c) {
