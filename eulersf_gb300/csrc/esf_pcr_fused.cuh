@@ -35,7 +35,6 @@
 struct FusedMaps {
   CUtensorMap r[2], t[2], q[2];  // box 72 x 10 at (x0 - 4, y0 - 1)
   CUtensorMap iv, x, d;          // box 64 x 8 at (x0, y0)
-  CUtensorMap iv16;              // 1/diag in BF16 (ESF_IV16), box 64 x 8
   CUtensorMap m;                 // padded node m^-1, box 68 x 9 at (x0, y0)
 };
 struct FusedPtrs {
@@ -97,10 +96,6 @@ __device__ __forceinline__ void finish_fused(PcrState* st, double dl, double mu,
   }
 }
 
-// IV16: 1/diag read as BF16 (half the bytes of that input; any positive
-// diagonal is a valid preconditioner, and the whole inner solve then uses
-// the rounded one)
-template <bool IV16>
 __global__ void __launch_bounds__(NT, 4) pcr_iteration_fused(GridDev g, const __grid_constant__ FusedMaps tm,
                                                              FusedPtrs p, double* partial, PcrState* st,
                                                              int cz) {
@@ -135,13 +130,12 @@ __global__ void __launch_bounds__(NT, 4) pcr_iteration_fused(GridDev g, const __
     unsigned long long* b = &bar[i % TMA_STAGES];
     const bool own = kk >= z0 && kk < z1;
     const bool node = kk >= z0;
-    constexpr int ownBytes = (IV16 ? TMA_OWN_BYTES / 2 : TMA_OWN_BYTES) + 2 * TMA_OWN_BYTES;
-    mbar_expect_tx(b, 3 * TMA_HALO_BYTES + (own ? ownBytes : 0) + (node ? TMA_NODE_BYTES : 0));
+    mbar_expect_tx(b, 3 * TMA_HALO_BYTES + (own ? 3 * TMA_OWN_BYTES : 0) + (node ? TMA_NODE_BYTES : 0));
     tma_load_3d(s + FU_OFF_R, mR, x0 - 4, y0 - 1, kk, b);
     tma_load_3d(s + FU_OFF_T, mT, x0 - 4, y0 - 1, kk, b);
     tma_load_3d(s + FU_OFF_Q, mQ, x0 - 4, y0 - 1, kk, b);
     if (own) {
-      tma_load_3d(s + FU_OFF_IV, IV16 ? &tm.iv16 : &tm.iv, x0, y0, kk, b);
+      tma_load_3d(s + FU_OFF_IV, &tm.iv, x0, y0, kk, b);
       tma_load_3d(s + FU_OFF_X, &tm.x, x0, y0, kk, b);
       tma_load_3d(s + FU_OFF_D, &tm.d, x0, y0, kk, b);
     }
@@ -219,11 +213,7 @@ __global__ void __launch_bounds__(NT, 4) pcr_iteration_fused(GridDev g, const __
       prev0 = v0;
       prev1 = v1;
       if (kk >= z0 && kk < z1 && cin) {
-        float2 iv;
-        if (IV16)
-          iv = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(s + FU_OFF_IV + 2 * oM));
-        else
-          iv = *reinterpret_cast<const float2*>(s + FU_OFF_IV + 4 * oM);
+        const float2 iv = *reinterpret_cast<const float2*>(s + FU_OFF_IV + 4 * oM);
         const float2 xv = *reinterpret_cast<const float2*>(s + FU_OFF_X + 4 * oM);
         const float2 dv = *reinterpret_cast<const float2*>(s + FU_OFF_D + 4 * oM);
         const float dn0 = __fmaf_rn(beta, dv.x, r2.x), dn1 = __fmaf_rn(beta, dv.y, r2.y);

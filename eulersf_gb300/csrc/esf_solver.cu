@@ -19,7 +19,6 @@
 #include <vector>
 
 #include <cuda.h>
-#include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
 #include "esf_common.cuh"
@@ -479,18 +478,9 @@ __global__ void convert_minv_padded(GridDev g, const double* in, float* out, int
     out[i] = v;
   }
 }
-// 1/diag; with out16 (the mixed path's BF16 preconditioner, ESF_IV16) every
-// copy holds the BF16-rounded value, so the FP64 residual scaling and the
-// FP32 recurrence use one and the same diagonal
-__global__ void inv_vec(long long n, const double* in, double* out64, float* out32,
-                        __nv_bfloat16* out16 = nullptr) {
+__global__ void inv_vec(long long n, const double* in, double* out64, float* out32) {
   for (long long i = blockIdx.x * (long long)VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT) {
     double v = 1.0 / in[i];
-    if (out16) {
-      const __nv_bfloat16 h = __double2bfloat16(v);
-      out16[i] = h;
-      v = (double)__bfloat162float(h);
-    }
     if (out64) out64[i] = v;
     if (out32) out32[i] = (float)v;
   }
@@ -547,7 +537,6 @@ struct PressureWork {
   float *r32b, *s32b, *Ap32b;
   FusedMaps fmaps;
   bool fusedOk;
-  __nv_bfloat16* invd16;  // BF16 1/diag of the one-pass kernel (ESF_IV16)
   MappedSet mapped;  // FP32 vectors mapped by vec_alloc
 };
 
@@ -683,7 +672,7 @@ static int fused_cz(const GridDev& g) {
     int dev = 0, sms = 152, per = 4;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pcr_iteration_fused<false>, NT, FU_SMEM) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pcr_iteration_fused, NT, FU_SMEM) !=
             cudaSuccess ||
         per < 1)
       per = 4;
@@ -752,7 +741,6 @@ esf_status pressure_work_alloc(PressureWork** out, const GridDev& g, int mixed) 
     }
     esf_status e = vec_alloc(&w->mapped, &w->minv32p, (size_t)w->mpitch * g.Y * g.Z * 4);
     if (e) return e;
-    ESF_CUDA(cudaMalloc(&w->invd16, R * 2));
     ESF_CUDA(cudaMalloc(&w->minv32, g.T * 4));
   }
   ESF_CUDA(cudaMalloc(&w->partial, ESF_MAX_PARTIALS * 8));
@@ -775,7 +763,6 @@ void pressure_work_free(PressureWork* w) {
                    w->Ap32b, w->minv32p})
     vec_free(&w->mapped, v);
   cudaFree(w->minv32);
-  cudaFree(w->invd16);
   cudaFree(w->partial); cudaFree(w->st); cudaFree(w->st32); cudaFree(w->stT);
   if (w->hst) cudaFreeHost(w->hst);
   if (w->gFirst) cudaGraphExecDestroy(w->gFirst);
@@ -804,18 +791,17 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 
 // 3-D FP32 array [d][h][w] (w a multiple of 4), box bw x bh x 1, zero fill
 static esf_status encode3d(CUtensorMap* m, const void* base, long long w, long long h, long long d,
-                           unsigned bw, unsigned bh,
-                           CUtensorMapDataType dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT32, int esize = 4) {
+                           unsigned bw, unsigned bh) {
   PFN_cuTensorMapEncodeTiled_v12000 fn = tensor_map_encoder();
   if (!fn) {
     set_error("cuTensorMapEncodeTiled is not available from the driver");
     return ESF_ERR_CUDA;
   }
   cuuint64_t dims[3] = {(cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)d};
-  cuuint64_t strides[2] = {(cuuint64_t)w * esize, (cuuint64_t)w * h * esize};
+  cuuint64_t strides[2] = {(cuuint64_t)w * 4, (cuuint64_t)w * h * 4};
   cuuint32_t box[3] = {bw, bh, 1};
   cuuint32_t es[3] = {1, 1, 1};
-  CUresult r = fn(m, dt, 3, const_cast<void*>(base), dims, strides, box, es,
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(base), dims, strides, box, es,
                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
@@ -873,13 +859,8 @@ static esf_status prepare_tma(PressureWork* w, const GridDev& g, const double* m
   const bool fits = (long long)gr.x * gr.y * gr.z * FU_SUMS <= ESF_MAX_PARTIALS / 2;
   if (!path || !fits || (pick && strcmp(pick, "tma") == 0)) return ESF_OK;
   if (!w->fusedOk) {
-    static const cudaError_t attr = [] {
-      cudaError_t a = cudaFuncSetAttribute(pcr_iteration_fused<false>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, FU_SMEM);
-      cudaError_t b = cudaFuncSetAttribute(pcr_iteration_fused<true>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, FU_SMEM);
-      return a != cudaSuccess ? a : b;
-    }();
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        pcr_iteration_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, FU_SMEM);
     if (attr != cudaSuccess) {
       set_error("pcr_iteration_fused: %d bytes of shared memory refused: %s", FU_SMEM,
                 cudaGetErrorString(attr));
@@ -896,10 +877,6 @@ static esf_status prepare_tma(PressureWork* w, const GridDev& g, const double* m
       if ((e = encode3d(&m.q[k], qs[k], g.cX, g.cY, g.cZ, TMA_HW, TMA_HH))) return e;
     }
     if ((e = encode3d(&m.iv, w->invd32, g.cX, g.cY, g.cZ, TXW, TY))) return e;
-    // BF16 rows need a multiple of 8 cells for 16-byte strides
-    if (g.cX % 8 == 0 &&
-        (e = encode3d(&m.iv16, w->invd16, g.cX, g.cY, g.cZ, TXW, TY, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2)))
-      return e;
     if ((e = encode3d(&m.x, w->x32, g.cX, g.cY, g.cZ, TXW, TY))) return e;
     if ((e = encode3d(&m.d, w->d32, g.cX, g.cY, g.cZ, TXW, TY))) return e;
     if ((e = encode3d(&m.m, w->minv32p, w->mpitch, g.Y, g.Z, TMA_NW, TMA_NH))) return e;
@@ -917,13 +894,9 @@ struct FusedKernels {
   FusedPtrs p;
   double* partial;
   PcrState* st;
-  bool iv16;
   void iteration(cudaStream_t cs) const {
     const int cz = fused_cz(g);
-    if (iv16)
-      ESF_COUNTED pcr_iteration_fused<true><<<tma_grid(g, cz), NT, FU_SMEM, cs>>>(g, *tm, p, partial, st, cz);
-    else
-      ESF_COUNTED pcr_iteration_fused<false><<<tma_grid(g, cz), NT, FU_SMEM, cs>>>(g, *tm, p, partial, st, cz);
+    ESF_COUNTED pcr_iteration_fused<<<tma_grid(g, cz), NT, FU_SMEM, cs>>>(g, *tm, p, partial, st, cz);
   }
   // graph capture interface of PressureKernels (inner solves only)
   void setup_warm(cudaStream_t) const {}
@@ -932,12 +905,6 @@ struct FusedKernels {
     for (int k = 0; k < n; k++) iteration(cs);
   }
 };
-// ESF_IV16=1: the one-pass kernel reads 1/diag in BF16 (cell rows a
-// multiple of 8 for the BF16 tensor map's 16-byte strides)
-static bool use_iv16(const PressureWork* w, const GridDev& g) {
-  const char* e = getenv("ESF_IV16");
-  return e && atoi(e) != 0 && g.cX % 8 == 0 && w->invd16;
-}
 static FusedKernels fused_kernels(PressureWork* w, const GridDev& g, PcrState* st) {
   FusedKernels k;
   k.g = g;
@@ -949,7 +916,6 @@ static FusedKernels fused_kernels(PressureWork* w, const GridDev& g, PcrState* s
   k.p.d = w->d32;
   k.partial = w->partial;
   k.st = st;
-  k.iv16 = use_iv16(w, g);
   return k;
 }
 
@@ -1098,8 +1064,7 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
     dim3 gr = stencil_grid<double>(g);
     if ((long long)gr.x * gr.y * gr.z > ESF_MAX_PARTIALS) return ESF_ERR_UNSUPPORTED;
   }
-  ESF_COUNTED inv_vec<<<vec_blocks(g.R), VT, 0, st>>>(
-      g.R, diag64, w->invd, w->invd32, precision == ESF_MIXED && use_iv16(w, g) ? w->invd16 : nullptr);
+  ESF_COUNTED inv_vec<<<vec_blocks(g.R), VT, 0, st>>>(g.R, diag64, w->invd, w->invd32);
   ESF_LAUNCH_CHECK();
   // FP64 PCR from the warm start x (the reference's solvePCR): two kernels
   // per iteration replayed as graphs, true-residual check every 5th.
@@ -1156,7 +1121,7 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
   const FusedKernels kf = fused_kernels(w, g, w->st32);
   const void* key[8] = {w->minv32, w->invd32, w->b32, w->x32, tma, &w->fmaps,
                         reinterpret_cast<const void*>(static_cast<uintptr_t>(path + 1)),
-                        reinterpret_cast<const void*>(static_cast<uintptr_t>(fused_cz(g) | (kf.iv16 << 16)))};
+                        reinterpret_cast<const void*>(static_cast<uintptr_t>(fused_cz(g)))};
   if (!w->graphsFor32 || memcmp(key, w->keyB, sizeof key) != 0) {
     esf_status e = fused ? capture(w->capStream, kf, false, false, &w->gChunk32, &w->kChunk32)
                          : capture(w->capStream, k32, false, false, &w->gChunk32, &w->kChunk32);
@@ -1397,8 +1362,7 @@ esf_status pressure_time_kernels(PressureWork* w, const GridDev& g, const double
                                  int precision, int reps, double* update_ms, double* axpy_ms,
                                  cudaStream_t st) {
   (void)x;
-  ESF_COUNTED inv_vec<<<vec_blocks(g.R), VT, 0, st>>>(
-      g.R, diag64, w->invd, w->invd32, precision == ESF_MIXED && use_iv16(w, g) ? w->invd16 : nullptr);
+  ESF_COUNTED inv_vec<<<vec_blocks(g.R), VT, 0, st>>>(g.R, diag64, w->invd, w->invd32);
   if (precision == ESF_MIXED) {
     if (!w->x32) return ESF_ERR_STATE;
     ESF_COUNTED convert_vec<double, float><<<vec_blocks(g.T), VT, 0, st>>>(g.T, minv64, w->minv32);
