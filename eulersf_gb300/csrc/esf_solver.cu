@@ -7,7 +7,8 @@
 //    kernels per iteration (axpy+norm, update+SpMV+dot) plus a residual check
 //    every 5th iteration, with all scalars kept on the device and the
 //    iteration chunks replayed as CUDA graphs;
-//  * FP32 inner solves inside FP64 iterative refinement (ESF_MIXED);
+//  * FP32 inner solves inside FP64 iterative refinement (ESF_MIXED), one
+//    TMA-staged kernel per inner iteration (esf_pcr_fused.cuh);
 //  * the solid system (M + dt^2 K) in 27-neighbour 3x3 block rows.
 #include <stdio.h>
 #include <stdlib.h>
