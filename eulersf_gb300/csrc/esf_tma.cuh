@@ -66,11 +66,8 @@ constexpr int TW_OFF_C = TW_OFF_B + TW_NP * NYN * 4;
 constexpr int TW_OFF_RED = (TW_OFF_C + TW_NP * NYN * 4 + 15) / 16 * 16;
 constexpr int TW_OFF_ACC = TW_OFF_RED + 32 * 8;
 constexpr int TW_SMEM = TW_OFF_ACC + 2 * NT * 4;  // about 45 KB: four blocks per SM
-// bounded waits: up to 2^22 polls, each suspending the thread for at most
-// TMA_WAIT_HINT_NS (the hardware wakes it when the phase completes), so a
-// waiting warp takes no issue slots; a stuck copy is reported after seconds
-constexpr unsigned TMA_WAIT_LIMIT = 1u << 22;
-constexpr unsigned TMA_WAIT_HINT_NS = 1000;
+// bounded waits: ~2^24 polls (seconds) before a block reports a stuck copy
+constexpr unsigned TMA_WAIT_LIMIT = 1u << 24;
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -90,10 +87,10 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
   for (unsigned n = 0; n < TMA_WAIT_LIMIT; n++) {
     unsigned done;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
         " selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)
-        : "r"(a), "r"(parity), "r"(TMA_WAIT_HINT_NS)
+        : "r"(a), "r"(parity)
         : "memory");
     if (done) return true;
   }
