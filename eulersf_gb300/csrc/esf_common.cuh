@@ -172,6 +172,8 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
                           int precision, double innerEps, int maxRefine, int* iters,
                           double* relres, int* refinements, int* converged, cudaStream_t st,
                           int* fp64Iters = nullptr);
+// self-test of the TMA kernels' bounded mbarrier wait (esf_solver.cu)
+esf_status selftest_mbar_wait(int* gaveUp, cudaStream_t st);
 // allocation-free FP64 solve on the module's static scratch (esf_solver.cu)
 esf_status static_scratch_address(void** out);
 esf_status pressure_solve_static(void* scratch, const GridDev& g, const double* minv,

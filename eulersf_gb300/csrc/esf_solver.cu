@@ -14,6 +14,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <chrono>
+#include <mutex>
 #include <cmath>
 #include <type_traits>
 
@@ -1711,6 +1712,30 @@ esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const in
   return status;
 }
 
+// ------------------------------------------------- bounded-wait self-test
+// One thread arms an mbarrier for a 16-byte copy that is never issued and
+// waits on it with mbar_wait, the TMA kernels' bounded wait (TMA_WAIT_LIMIT
+// polls). The phase never completes, so the wait runs out; the thread
+// records that in *gaveUp, invalidates the barrier and the block returns.
+// No copy is in flight, so nothing writes the barrier's shared memory after
+// the block has ended.
+__global__ void k_selftest_mbar_wait(int* gaveUp) {
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_expect_tx(&bar, 16);
+    const bool landed = mbar_wait(&bar, 0);
+    *gaveUp = landed ? 0 : 1;
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&bar)) : "memory");
+  }
+}
+
+esf_status selftest_mbar_wait(int* gaveUp, cudaStream_t st) {
+  ESF_COUNTED k_selftest_mbar_wait<<<1, 32, 0, st>>>(gaveUp);
+  ESF_LAUNCH_CHECK();
+  return ESF_OK;
+}
+
 // ------------------------------------ allocation-free FP64 pressure solve
 // Scratch of esf_pressure_solve_static: one file-scope device array, carved
 // into [PcrState | block partials | invd r d Ap s], sized for grids of at
@@ -1724,8 +1749,69 @@ constexpr size_t kStaticScratchBytes =
 static_assert(sizeof(PcrState) <= kStaticStateBytes, "PcrState outgrew its slot");
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
+// The context the calling thread has current, by its process-unique ID
+// (cuCtxGetId); false when there is none or it has been destroyed.
+static bool current_context_id(unsigned long long* id) {
+  struct Api {
+    PFN_cuCtxGetCurrent_v4000 current = nullptr;
+    PFN_cuCtxGetId_v12000 getId = nullptr;
+  };
+  static const Api api = [] {
+    Api a;
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      a.current = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      a.getId = reinterpret_cast<PFN_cuCtxGetId_v12000>(p);
+    return a;
+  }();
+  CUcontext ctx = nullptr;
+  if (!api.current || !api.getId || api.current(&ctx) != CUDA_SUCCESS || !ctx) return false;
+  return api.getId(ctx, id) == CUDA_SUCCESS;
+}
+
+// Device address of g_static_scratch on the current device. In host code the
+// array's name is only a stand-in, so the address comes from
+// cudaGetSymbolAddress, called with the device current: once per device, and
+// again whenever the device's context has been re-created since (after a
+// cudaDeviceReset the module is loaded anew and the array can move), which
+// the context's ID tells. The lookup allocates nothing; it can load the
+// module's device code.
 esf_status static_scratch_address(void** out) {
-  return cudaGetSymbolAddress(out, g_static_scratch) == cudaSuccess ? ESF_OK : ESF_ERR_CUDA;
+  static std::mutex mu;
+  static unsigned long long ctxOf[ESF_STATIC_SOLVE_MAX_DEVICES];
+  static void* addrOf[ESF_STATIC_SOLVE_MAX_DEVICES];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return ESF_ERR_CUDA;
+  if (dev < 0 || dev >= ESF_STATIC_SOLVE_MAX_DEVICES) {
+    set_error("esf_pressure_solve_static: device %d beyond the %d supported", dev,
+              ESF_STATIC_SOLVE_MAX_DEVICES);
+    return ESF_ERR_UNSUPPORTED;
+  }
+  unsigned long long id = 0;
+  const bool known = current_context_id(&id);
+  std::lock_guard<std::mutex> lock(mu);
+  if (known && addrOf[dev] && ctxOf[dev] == id) {
+    *out = addrOf[dev];
+    return ESF_OK;
+  }
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+  if (e != cudaSuccess || !p) {
+    set_error("esf_pressure_solve_static: cudaGetSymbolAddress failed on device %d: %s", dev,
+              cudaGetErrorString(e));
+    return ESF_ERR_CUDA;
+  }
+  // cache only under the context the lookup ran in; without an ID, look up
+  // again on the next call
+  addrOf[dev] = current_context_id(&id) ? p : nullptr;
+  ctxOf[dev] = id;
+  *out = p;
+  return ESF_OK;
 }
 
 // The reference's FP64 solvePCR with the kernels of the graph path, launched

@@ -128,6 +128,7 @@ struct esf_scene {
   int ns = 0;
   esf::Solid* s[ESF_MAX_SOLIDS] = {};
   bool inited = false;
+  bool failed = false;  // a solve met NaN/Inf; cleared by esf_read_frame
   double fluidDensity = 1.0, defaultDt = 0.01, dt = 0.01, vortEps = 0.0;
   // node fields
   double *vel = nullptr, *vws = nullptr, *vort = nullptr, *intensity = nullptr, *ws = nullptr;
@@ -902,6 +903,10 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     set_error("esf_step: call esf_init first");
     return ESF_ERR_STATE;
   }
+  if (sc->failed) {
+    set_error("esf_step: a solve of an earlier step met NaN/Inf; restore a state with esf_read_frame first");
+    return ESF_ERR_STATE;
+  }
   cudaSetDevice(sc->device);
   const GridDev& G = sc->g;
   cudaStream_t st = sc->stream;
@@ -1002,14 +1007,38 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     TRY(solid_work_alloc(&sc->sw, S + S / 4 + 16, prec == ESF_MIXED));
   }
   esf_status es = ESF_OK;
+  // A solve that met NaN/Inf ends the step there: nothing downstream (the
+  // velocity update, particles, advection) runs on non-finite values. The
+  // report carries what was done; the scene refuses further steps until a
+  // state is restored (esf_read_frame).
+  auto numeric_stop = [&]() -> esf_status {
+    cudaStreamSynchronize(st);
+    sc->failed = true;
+    if (rep) {
+      memset(rep, 0, sizeof *rep);
+      rep->dt = dt;
+      rep->energy = energy;
+      for (int k = 0; k < 3; k++) {
+        rep->iterations[k] = it[k];
+        rep->converged[k] = cv[k];
+        rep->rel_residual[k] = rr[k];
+        rep->refinements[k] = rf[k];
+      }
+      rep->prone_to_contact = prone;
+      rep->fp64_iterations = it64;
+      rep->status = ESF_ERR_NUMERIC;
+    }
+    set_error("esf_step: NaN/Inf met in a solve; the step stopped after it");
+    return ESF_ERR_NUMERIC;
+  };
   ESF_CUDA(cudaEventRecord(sc->ph[3], st));
   if (S > 0) {
     es = solid_solve(sc->sw, S, sc->blocks.as<double>(), sc->nbr.as<int>(), sc->sysDiag.as<double>(),
                      sc->solidF.as<double>(), sc->solidV0.as<double>(), sc->p.implicit_solver_eps,
                      sc->p.cr_max_iterations, prec, sc->p.inner_eps, sc->p.max_refinements, &it[0],
                      &rr[0], &rf[0], &cv[0], st);
-    if (es == ESF_ERR_NUMERIC) sc->status = es;
-    else if (es) return es;
+    if (es == ESF_ERR_NUMERIC) return numeric_stop();
+    if (es) return es;
   }
   ESF_CUDA(cudaEventRecord(sc->ph[4], st));
   ESF_COUNTED k_vstar<<<kblocks(G.T), KT, 0, st>>>(G, sc->sdof, sc->uf, sc->minv, sc->solidV0.as<double>(), sc->vstar);
@@ -1018,8 +1047,8 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
   es = pressure_solve(sc->pw, G, sc->minv, sc->jdiag, sc->b1, sc->lambda, sc->p.div_free_solver_eps,
                       sc->p.cr_max_iterations, prec, sc->p.inner_eps, sc->p.max_refinements, &it[1],
                       &rr[1], &rf[1], &cv[1], st, &it64);
-  if (es == ESF_ERR_NUMERIC) sc->status = es;
-  else if (es) return es;
+  if (es == ESF_ERR_NUMERIC) return numeric_stop();
+  if (es) return es;
   ESF_CUDA(cudaEventRecord(sc->ph[5], st));
   if (S > 0) {
     ESF_COUNTED k_solid_b1<<<kblocks(S), KT, 0, st>>>(G, sc->sNode.as<long long>(), S, sc->lambda, sc->solidB1.as<double>());
@@ -1028,8 +1057,8 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
                      sc->solidB1.as<double>(), sc->solidPC.as<double>(), sc->p.implicit_solver_eps,
                      sc->p.cr_max_iterations, prec, sc->p.inner_eps, sc->p.max_refinements, &it[2],
                      &rr[2], &rf[2], &cv[2], st);
-    if (es == ESF_ERR_NUMERIC) sc->status = es;
-    else if (es) return es;
+    if (es == ESF_ERR_NUMERIC) return numeric_stop();
+    if (es) return es;
   }
   ESF_COUNTED k_velocity_update<<<kblocks(G.T), KT, 0, st>>>(G, sc->sdof, sc->lambda, sc->minv, sc->solidPC.as<double>(),
                                                  sc->vstar, sc->pc, sc->v1, sc->vel);
@@ -1417,11 +1446,6 @@ extern "C" esf_status esf_pressure_solve(const esf_grid* g, const double* minv, 
   return e;
 }
 
-// Per-device address of the static scratch, looked up on the first call on
-// each device.
-static std::mutex g_static_mu;
-static void* g_static_addr[ESF_STATIC_SOLVE_MAX_DEVICES];
-
 extern "C" esf_status esf_pressure_solve_static(const esf_grid* g, const double* minv,
                                                 const double* diag, const double* b, double* x,
                                                 double eps, int maxIt, int* iters, double* relres,
@@ -1436,27 +1460,8 @@ extern "C" esf_status esf_pressure_solve_static(const esf_grid* g, const double*
               cells, ESF_STATIC_SOLVE_MAX_CELLS);
     return ESF_ERR_UNSUPPORTED;
   }
-  int dev = 0;
-  ESF_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= ESF_STATIC_SOLVE_MAX_DEVICES) {
-    set_error("esf_pressure_solve_static: device %d beyond the %d supported", dev,
-              ESF_STATIC_SOLVE_MAX_DEVICES);
-    return ESF_ERR_UNSUPPORTED;
-  }
   void* scratch = nullptr;
-  {
-    std::lock_guard<std::mutex> lock(g_static_mu);
-    if (!g_static_addr[dev]) {
-      void* p = nullptr;
-      if (static_scratch_address(&p) != ESF_OK || !p) {
-        set_error("esf_pressure_solve_static: cudaGetSymbolAddress failed on device %d: %s", dev,
-                  cudaGetErrorString(cudaGetLastError()));
-        return ESF_ERR_CUDA;
-      }
-      g_static_addr[dev] = p;
-    }
-    scratch = g_static_addr[dev];
-  }
+  TRY(static_scratch_address(&scratch));
   GridDev G = grid_dev(g);
   int it = 0, cv = 0;
   double rr = 0;
@@ -1464,6 +1469,45 @@ extern "C" esf_status esf_pressure_solve_static(const esf_grid* g, const double*
                                        (cudaStream_t)stream);
   if (iters) *iters = it;
   if (relres) *relres = rr;
+  return e;
+}
+
+// One block arrives at a grid barrier that expects a second block, which is
+// never launched, and waits with wave_barrier, the wave sweep's bounded wait
+// (WAVE_WAIT_LIMIT polls): the wait runs out, the block sets *err and returns.
+__global__ void k_selftest_wave_barrier(unsigned* count, int* err) { wave_barrier(count, 2, err); }
+
+extern "C" esf_status esf_selftest_bounded_wait(int kind, int* gave_up, double* elapsed_ms) {
+  if ((kind != 0 && kind != 1) || !gave_up) {
+    set_error("esf_selftest_bounded_wait: kind must be 0 or 1 and gave_up non-NULL");
+    return ESF_ERR_INVALID_ARG;
+  }
+  int* d = nullptr;
+  ESF_CUDA(cudaMalloc(&d, 16));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  esf_status e = ESF_OK;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) e = ESF_ERR_CUDA;
+  if (!e && cudaMemset(d, 0, 16) != cudaSuccess) e = ESF_ERR_CUDA;
+  if (!e) {
+    cudaEventRecord(e0, 0);
+    if (kind == 0) {
+      e = selftest_mbar_wait(d, 0);
+    } else {
+      ESF_COUNTED k_selftest_wave_barrier<<<1, 32>>>(reinterpret_cast<unsigned*>(d + 1), d);
+      if (cudaGetLastError() != cudaSuccess) e = ESF_ERR_CUDA;
+    }
+    cudaEventRecord(e1, 0);
+  }
+  int h = -1;
+  if (!e && cudaMemcpy(&h, d, sizeof h, cudaMemcpyDeviceToHost) != cudaSuccess) e = ESF_ERR_CUDA;
+  float ms = 0;
+  if (!e) cudaEventElapsedTime(&ms, e0, e1);
+  if (e == ESF_ERR_CUDA) set_error("esf_selftest_bounded_wait: %s", cudaGetErrorString(cudaGetLastError()));
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(d);
+  *gave_up = h;
+  if (elapsed_ms) *elapsed_ms = ms;
   return e;
 }
 
@@ -1513,6 +1557,12 @@ extern "C" esf_status esf_write_frame(esf_scene* s, const char* path, int frame,
   if (full) {
     TRY(esf_get_field(s, ESF_F_VELOCITY, 0, buf.data(), G.T * 24));
     TRY(write_field_gz(base + ".velocity", res, G.dh, G.o, buf.data(), G.T * 3));
+    // extension: the pressure warm start, which the reference keeps in a
+    // function-local static and never writes; a cell field (cell centres)
+    const int cres[3] = {G.cX, G.cY, G.cZ};
+    const double corig[3] = {G.o[0] + 0.5 * G.dh, G.o[1] + 0.5 * G.dh, G.o[2] + 0.5 * G.dh};
+    TRY(esf_get_field(s, ESF_F_PRESSURE, 0, buf.data(), G.R * 8));
+    TRY(write_field_gz(base + ".lambda1", cres, G.dh, corig, buf.data(), G.R));
   }
   TRY(esf_get_field(s, ESF_F_INTENSITY, 0, buf.data(), G.T * 8));
   TRY(write_field_gz(base + ".intensity", res, G.dh, G.o, buf.data(), G.T));
@@ -1523,8 +1573,10 @@ extern "C" esf_status esf_write_frame(esf_scene* s, const char* path, int frame,
 // DEFOR_SOLID_3D::readFrame (DEFOR_SOLID_3D.cpp:1299-1361): the fields above,
 // then per solid X from u, the mesh from its OBJ, the boxes from the mesh's
 // vertex bounds, computeSolidMass(true) and initMaterialParticles; then
-// gatherSolidMasses and recoverVelocityField. Like the reference, the
-// pressure warm start and dt are not part of a frame.
+// gatherSolidMasses and recoverVelocityField. dt is not part of a frame (it
+// is recomputed from the CFL condition each step); the pressure warm start is
+// read from the ".lambda1" extension file where present. A successful read
+// also lifts the stop left by a step whose solve met NaN/Inf.
 extern "C" esf_status esf_read_frame(esf_scene* s, const char* path, int frame, int debug) {
   if (!s || !path) {
     set_error("esf_read_frame: invalid argument");
@@ -1590,11 +1642,27 @@ extern "C" esf_status esf_read_frame(esf_scene* s, const char* path, int frame, 
     TRY(read_field_gz(base + ".velocity", res, G.T * 3, buf.data()));
     TRY(esf_set_field(s, ESF_F_VELOCITY, 0, buf.data(), G.T * 24));
   }
+  // the pressure warm start, where the frame has it (our extension); a frame
+  // written by the reference has none, and the warm start is kept, as the
+  // reference keeps its static one, unless a failed solve left it non-finite
+  {
+    const int cres[3] = {G.cX, G.cY, G.cZ};
+    const std::string lf = base + ".lambda1";
+    FILE* probe = full ? fopen(lf.c_str(), "rb") : nullptr;
+    if (probe) {
+      fclose(probe);
+      TRY(read_field_gz(lf, cres, G.R, buf.data()));
+      TRY(esf_set_field(s, ESF_F_PRESSURE, 0, buf.data(), G.R * 8));
+    } else if (s->failed) {
+      ESF_CUDA(cudaMemsetAsync(s->lambda, 0, G.R * 8, st));
+    }
+  }
   TRY(read_field_gz(base + ".intensity", res, G.T, buf.data()));
   TRY(esf_set_field(s, ESF_F_INTENSITY, 0, buf.data(), G.T * 8));
   TRY(gather_solid_masses(s));
   TRY(recover_velocity(s));
   ESF_CUDA(cudaStreamSynchronize(st));
+  s->failed = false;
   return ESF_OK;
 }
 

@@ -66,8 +66,11 @@ constexpr int TW_OFF_C = TW_OFF_B + TW_NP * NYN * 4;
 constexpr int TW_OFF_RED = (TW_OFF_C + TW_NP * NYN * 4 + 15) / 16 * 16;
 constexpr int TW_OFF_ACC = TW_OFF_RED + 32 * 8;
 constexpr int TW_SMEM = TW_OFF_ACC + 2 * NT * 4;  // about 45 KB: four blocks per SM
-// bounded waits: ~2^24 polls (seconds) before a block reports a stuck copy
-constexpr unsigned TMA_WAIT_LIMIT = 1u << 24;
+// bounded waits: 2^18 polls before a block reports a stuck copy. An
+// unsuccessful mbarrier.try_wait suspends the thread for its own time limit
+// first (measured on GB300: ~3.8 us a poll), so the wait gives up after about
+// one second, far beyond any copy that lands.
+constexpr unsigned TMA_WAIT_LIMIT = 1u << 18;
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
   return (unsigned)__cvta_generic_to_shared(p);

@@ -239,29 +239,41 @@ esf_status esf_pressure_solve(const esf_grid* grid, const double* mass_inv_node,
                               double eps, int max_iterations, int precision,
                               int* iterations, double* rel_residual, void* stream);
 
-/* Allocation-free variant of esf_pressure_solve at ESF_FP64; no reference
- * counterpart (solvePCR allocates its vectors per call,
- * CONJUGATE_RESIDUAL.inl:109-125). For callers that must not allocate or
- * free device memory during a solve: a host whose HBM is reserved up front
+/* Allocation-free variant of esf_pressure_solve at ESF_FP64. It has no
+ * counterpart in the reference. It is for callers that must not allocate or
+ * free device memory while they solve: a host whose HBM is reserved up front
  * by its own pool (a framework's caching allocator, a serving runtime), where
- * a cudaMalloc can fail or fragment, and callers overlapping other streams,
- * which cudaFree's implicit device-wide synchronisation would stall.
+ * a cudaMalloc can fail or fragment that pool, and callers that keep other
+ * streams busy, which the device-wide synchronisation of cudaFree would stall.
  * Same kernels, order and results as esf_pressure_solve(..., ESF_FP64, ...).
- * Its scratch is a file-scope static device array (10.1 MiB per device,
- * part of the loaded module) for grids of at most ESF_STATIC_SOLVE_MAX_CELLS
- * cells; larger grids return ESF_ERR_UNSUPPORTED with a message. Nothing is
- * allocated, freed or created (no stream, event or graph). The scratch
- * address is looked up with cudaGetSymbolAddress on the first call on each
- * device (this can load the module): make that first call outside any stream
- * capture. One scratch per device: calls that overlap on the same device,
- * from two host threads or two streams, race on it and must be serialised by
- * the caller. Returns when the solve has finished on `stream`. */
+ * Its scratch is a file-scope static device array (10.1 MiB per device, part
+ * of the loaded module, held by every GPU that loads the library until the
+ * process exits) for grids of at most ESF_STATIC_SOLVE_MAX_CELLS cells;
+ * larger grids return ESF_ERR_UNSUPPORTED with a message. Nothing is
+ * allocated, freed or created (no stream, event or graph). The first call on
+ * each device, and the first after that device's context has been re-created
+ * (cudaDeviceReset), looks up the array's device address with
+ * cudaGetSymbolAddress, which can load the module's device code: that first
+ * call should come before any stream capture. One scratch per device: calls
+ * that overlap on the same device, from two host threads or two streams, race
+ * on it and must be serialised by the caller; each call clears what it needs
+ * zeroed. Returns when the solve has finished on `stream`. */
 #define ESF_STATIC_SOLVE_MAX_CELLS (64 * 64 * 64)
 #define ESF_STATIC_SOLVE_MAX_DEVICES 64
 esf_status esf_pressure_solve_static(const esf_grid* grid, const double* mass_inv_node,
                                      const double* diag, const double* b, double* x,
                                      double eps, int max_iterations, int* iterations,
                                      double* rel_residual, void* stream);
+
+/* Self-test of the kernels' bounded waits; no reference counterpart (the
+ * reference has no device code). Runs a one-block kernel that waits, with the
+ * same wait the step's kernels use, on something that never happens:
+ * kind 0, an mbarrier armed for a TMA copy that is never issued (the wait of
+ * the TMA pressure kernels); kind 1, a grid barrier that the other blocks
+ * never reach (the wait of the wave sweeps). *gave_up = 1 when the wait ran
+ * out and the kernel returned on its own, as it should; *elapsed_ms (may be
+ * NULL) is the kernel's device time. The context stays usable afterwards. */
+esf_status esf_selftest_bounded_wait(int kind, int* gave_up, double* elapsed_ms);
 
 /* ---- serving: many scenes on one GPU -------------------------------------
  * No reference counterpart: the reference runs one scene per process (its

@@ -69,6 +69,23 @@ def pressure_apply(g, mass_inv_node, x):
     return out
 
 
+def pressure_residual(I):
+    """||J M^-1 J^T lambda1 - b1|| / ||b1|| of an integrator's last pressure
+    solve (getMatVecMult, COUPLED_INTEGRATOR_3D.cpp:638-660, applied by the
+    oracle on the CPU): an independent check of a solve's answer. I is any
+    CoupledIntegrator3D (the CUDA library's or the oracle's)."""
+    dof = I.get("gridIdxToSolutionIdx")
+    mv = I.get("nzMassVecInv").reshape(-1, 3)
+    assert np.array_equal(mv[:, 0], mv[:, 1]) and np.array_equal(mv[:, 0], mv[:, 2])
+    minv = np.zeros(len(dof))
+    minv[dof >= 0] = mv[dof[dof >= 0], 0]
+    from eulersf_gb300 import abi
+    g = abi.Grid(I.xRes(), I.yRes(), I.zRes(), I.dh(), (C.c_double * 3)(*I.origin()))
+    b = I.get("b1")
+    r = pressure_apply(g, minv, I.get("lambda1")) - b
+    return float(np.linalg.norm(r) / np.linalg.norm(b))
+
+
 def pressure_solve(g, mass_inv_node, diag, b, x0, eps, max_it):
     x = np.array(x0, dtype=np.float64, copy=True)
     it, rr = C.c_int(), C.c_double()

@@ -108,3 +108,69 @@ def compare_to_golden(get, z, step, tol, fields=None, skip=()):
         if not e <= tol:
             fails.append(f"{pre}{g}: rel err {e:.3e} > {tol:.1e}")
     return fails
+
+
+# ------------------------------------------- benchmark-sized (compact) fixtures
+BIG_SCENES = ["config1_64", "config2_128"]
+# fixture name -> integrator field name
+BIG_NAME = {"velocity": "velocity", "lambda1": "lambda1", "intensity": "intensity",
+            "nodeSolidVolumeFraction": "nodeSolidVolumeFraction", "solid0.u": "solid.u",
+            "solid0.velocity": "solid.velocity", "solid0.mass": "solid.mass",
+            "solid0.meshVertices": "solid.meshVertices"}
+
+
+def load_big(name):
+    """A compact fixture of tests/golden/make_golden.py --big: (desc, z, log, meta)."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    meta = json.loads(str(z["scene"]))
+    log = json.loads(str(z["log"]))
+    solids = [SolidDesc(center=tuple(s["center"]), radius=s["radius"], density=s["density"],
+                        E=s["E"], nu=s["nu"], velocity=tuple(s["velocity"])) for s in meta["solids"]]
+    desc = SceneDesc(N=meta["N"], mass_sample_dh=meta["mass_sample_dh"],
+                     vorticity_eps=meta["vorticity_eps"], buoyancy=meta["buoyancy"],
+                     noise_seed=meta["noise_seed"], solids=solids)
+    return desc, z, log, meta
+
+
+def compare_big(get, z, step, tol):
+    """Compare an integrator's state after `step` with a compact fixture.
+    Integer maps/flags bit-exact; each floating-point field's max |.| and
+    L2 norm within `tol` relative; at the stored steps, the sampled nodes and
+    cells and the solid nodes within `tol` of the field's max |.| (the
+    max-norm relative error of the full fields, restricted to those points).
+    Returns (failures, {field: worst relative error})."""
+    fails, worst = [], {}
+    pre = f"s{step}."
+    exact = ["gridIdxToSolidIdx", "solid0.valid", "solid0.boxes"]
+    if step == 0:
+        exact.append("gridIdxToSolutionIdx")
+    for f in exact:
+        mine = np.asarray(get(NAME[f])).reshape(-1)
+        ref = z[pre + f].reshape(-1)
+        if mine.shape != ref.shape or not np.array_equal(mine, ref.astype(mine.dtype)):
+            bad = np.count_nonzero(mine != ref) if mine.shape == ref.shape else "shape"
+            fails.append(f"{pre}{f}: not bit-exact ({bad})")
+    sdof = z[pre + "gridIdxToSolidIdx"].reshape(-1)
+    nodes, cells = z["sample.nodes"], z["sample.cells"]
+    for f, name in BIG_NAME.items():
+        if pre + f + ".stats" not in z.files:
+            continue
+        a = np.asarray(get(name), dtype=np.float64)
+        ref_max, _, ref_sq = z[pre + f + ".stats"]
+        mine_max, mine_sq = float(np.abs(a).max()), float((a.reshape(-1) ** 2).sum())
+        scale = ref_max if ref_max > 0 else 1.0
+        errs = [abs(mine_max - ref_max) / scale,
+                abs(np.sqrt(mine_sq) - np.sqrt(ref_sq)) / (np.sqrt(ref_sq) or 1.0)]
+        # node fields: one row per grid node; lambda1: one value per cell
+        comp = a.reshape(-1) if f in ("lambda1", "solid0.meshVertices") else a.reshape(len(sdof), -1)
+        if pre + f + ".sample" in z.files:
+            pts = cells if f == "lambda1" else nodes
+            errs.append(float(np.abs(comp[pts].reshape(-1) - z[pre + f + ".sample"].reshape(-1)).max()) / scale)
+        if pre + f + ".solid" in z.files:
+            errs.append(float(np.abs(comp[sdof >= 0].reshape(-1) - z[pre + f + ".solid"].reshape(-1)).max()) / scale)
+        if pre + f in z.files:
+            errs.append(float(np.abs(a.reshape(-1) - z[pre + f].reshape(-1)).max()) / scale)
+        worst[f] = max(errs)
+        if not worst[f] <= tol:
+            fails.append(f"{pre}{f}: rel err {worst[f]:.3e} > {tol:.1e}")
+    return fails, worst

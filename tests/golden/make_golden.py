@@ -7,6 +7,17 @@ the unmodified EULERSF sources) on small synthetic scenes.
 Each scene is written as <name>.npz holding the initial state (s0.*) and the
 state after every step (s<k>.*) for the fields listed below, plus the step
 log (iterations per solve, dt, energy) as JSON text.
+
+The benchmark-sized scenes (64^3 for 20 steps, 128^3 for a 2-step prefix)
+run the reference's OpenMP build (``make -C oracle omp``) and are stored in a
+compact form (``compact()``): the DOF maps and cell flags of every step in
+full, per-step statistics of the floating-point fields, and at a few steps
+the grid fields at a fixed seeded sample of nodes and cells and the solid's
+fields at every solid node:
+
+    python tests/golden/make_golden.py --big config1_64 config2_128 [--keep DIR]
+
+``--keep DIR`` keeps the harness's raw dumps there and reuses a completed run.
 """
 from __future__ import annotations
 
@@ -25,6 +36,7 @@ sys.path.insert(0, ROOT)
 from eulersf_gb300.scene import SceneDesc, SolidDesc, write_scene  # noqa: E402
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+HARNESS_OMP = os.path.join(ROOT, "oracle", "_ref", "ref_harness_omp")
 
 
 def scenes():
@@ -102,10 +114,122 @@ def run(name, desc, frames, out_dir):
         shutil.rmtree(tmp, ignore_errors=True)
 
 
+def big_scenes():
+    """The rubber-ball scene at the benchmark's 64^3 and 128^3 sizes (the
+    fluid-noise seed is 0 for both; the mass sample spacing is dh/8, so the
+    reference's integer sample count is exactly 8 per axis).
+    name -> (SceneDesc, steps, steps whose fields are stored, nodes sampled)."""
+    return {
+        "config1_64": (SceneDesc(N=64, mass_sample_dh=(1 / 64) / 8, noise_seed=0), 20,
+                       (1, 5, 10, 15, 20), 1 << 14),
+        "config2_128": (SceneDesc(N=128, mass_sample_dh=(1 / 128) / 8, noise_seed=0), 2, (1, 2), 1 << 15),
+    }
+
+
+# fields of the compact fixtures: integer maps/flags kept whole at every step;
+# floating-point fields as whole-field statistics at every step and, at the
+# stored steps, at a fixed seeded sample of nodes/cells (grid fields) or at
+# every solid node (the solid's fields, which live on and near the solid)
+BIG_EXACT = ["gridIdxToSolidIdx", "solid0.valid", "solid0.boxes"]
+BIG_FLOAT = ["velocity", "lambda1", "solid0.u", "solid0.velocity", "solid0.mass", "intensity",
+             "nodeSolidVolumeFraction", "solid0.meshVertices"]
+NODE_FIELDS = ["velocity", "intensity", "nodeSolidVolumeFraction"]
+CELL_FIELDS = ["lambda1"]
+SOLID_FIELDS = ["solid0.u", "solid0.velocity", "solid0.mass"]
+
+
+def field_stats(a):
+    """max |a|, sum a, sum a^2 in FP64."""
+    a = np.asarray(a, dtype=np.float64).reshape(-1)
+    return np.array([np.abs(a).max() if a.size else 0.0, a.sum(), (a * a).sum()])
+
+
+def sample_indices(n, count, seed):
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(n, size=min(count, n), replace=False)).astype(np.int64)
+
+
+def compact(dump, desc, steps, stored, sample):
+    """The compact fixture of a benchmark-sized run (see the module docstring)."""
+    arrays = {}
+    X = desc.res
+    nodes = sample_indices(X ** 3, sample, 1234)
+    cells = sample_indices(desc.N ** 3, sample, 4321)
+    arrays["sample.nodes"], arrays["sample.cells"] = nodes, cells
+    for k in range(0, steps + 1):
+        pre = f"s{k}."
+        load = lambda f: np.load(os.path.join(dump, f"{pre}{f}.npy"))
+        for f in BIG_EXACT + (["gridIdxToSolutionIdx"] if k == 0 else []):
+            arrays[pre + f] = load(f)
+        sdof = load("gridIdxToSolidIdx")
+        for f in BIG_FLOAT:
+            if not os.path.exists(os.path.join(dump, f"{pre}{f}.npy")):
+                continue
+            a = load(f)
+            arrays[pre + f + ".stats"] = field_stats(a)
+            if k not in stored:
+                continue
+            if f in NODE_FIELDS:
+                arrays[pre + f + ".sample"] = a.reshape(X ** 3, -1)[nodes]
+            elif f in CELL_FIELDS:
+                arrays[pre + f + ".sample"] = a.reshape(-1)[cells]
+            elif f in SOLID_FIELDS:
+                arrays[pre + f + ".solid"] = a.reshape(X ** 3, -1)[sdof >= 0]
+            else:
+                arrays[pre + f] = a
+    return arrays
+
+
+def run_big(name, desc, steps, stored, sample, out_dir, keep=None):
+    tmp = os.path.join(keep, name) if keep else tempfile.mkdtemp(prefix="esf_golden_")
+    try:
+        dump = os.path.join(tmp, "dump")
+        log_path = os.path.join(dump, "log.jsonl")
+        done = os.path.exists(log_path) and sum(1 for _ in open(log_path)) >= steps + 1
+        if not done:
+            cfg = write_scene(desc, os.path.join(tmp, "scene"))
+            subprocess.run([HARNESS_OMP, cfg, dump, str(steps), "--noise",
+                            os.path.join(tmp, "scene", "noise.f64"), "--full-every", "1000000"],
+                           check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        log = [json.loads(l) for l in open(log_path)][1:]
+        if len(log) != steps:
+            raise RuntimeError(f"{name}: {len(log)} steps in {steps} frames (substeps)")
+        arrays = compact(dump, desc, steps, stored, sample)
+        seconds = [l.pop("seconds", None) for l in log]
+        arrays["log"] = np.array(json.dumps(log))
+        solids = [dict(sd.__dict__) for sd in desc.solids]
+        arrays["scene"] = np.array(json.dumps({
+            "N": desc.N, "mass_sample_dh": desc.mass_sample_dh, "vorticity_eps": desc.vorticity_eps,
+            "buoyancy": desc.buoyancy, "noise_seed": desc.noise_seed, "frames": steps,
+            "flow_rate": desc.flow_rate, "solids": solids, "stored_steps": list(stored),
+            "sample": sample, "reference_seconds_per_step": seconds,
+            "reference_threads": os.cpu_count()}))
+        np.savez_compressed(os.path.join(out_dir, name + ".npz"), **arrays)
+    finally:
+        if not keep:
+            shutil.rmtree(tmp, ignore_errors=True)
+
+
 def main():
+    args = sys.argv[1:]
+    if args and args[0] == "--big":
+        keep = None
+        if "--keep" in args:
+            i = args.index("--keep")
+            keep = args[i + 1]
+            del args[i:i + 2]
+        if not os.path.exists(HARNESS_OMP):
+            sys.exit(f"{HARNESS_OMP} missing: build it with make -C oracle omp")
+        only = args[1:]
+        for name, (desc, steps, full, sample) in big_scenes().items():
+            if only and name not in only:
+                continue
+            run_big(name, desc, steps, full, sample, HERE, keep)
+            print(name, os.path.getsize(os.path.join(HERE, name + ".npz")), "bytes")
+        return
     if not os.path.exists(HARNESS):
         sys.exit(f"{HARNESS} missing: build it with make -C oracle")
-    only = sys.argv[1:]  # optional scene names
+    only = args  # optional scene names
     for name, (desc, frames) in scenes().items():
         if only and name not in only:
             continue

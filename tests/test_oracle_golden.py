@@ -51,3 +51,51 @@ def test_mt19937_stream():
         assert p[i, 0] == x * desc.dh + r[3 * i + 2]
         assert p[i, 1] == y * desc.dh + r[3 * i + 1]
         assert p[i, 2] == zz * desc.dh + r[3 * i]
+
+
+@pytest.mark.parametrize("name", ["ball16", "wall20"])
+def test_pressure_residual_helper_on_reference_solutions(name):
+    """oracle.pressure_residual (the independent residual check used by the
+    smoke step and the benchmark) gives the reference's own pressure solutions
+    a relative residual below its 1e-8 tolerance, step by step."""
+    desc, z, log = load_golden(name)
+
+    class Dump:
+        def __init__(self, k):
+            self.k = k
+
+        def get(self, f):
+            key = f"s0.{f}" if f == "gridIdxToSolutionIdx" else f"s{self.k}.{f}"
+            return z[key]
+
+        def xRes(self):
+            return desc.res
+        yRes = zRes = xRes
+
+        def dh(self):
+            return desc.dh
+
+        def origin(self):
+            return (0.0, 0.0, 0.0)
+
+    for k in range(1, len(log) + 1):
+        res = oracle.pressure_residual(Dump(k))
+        assert res < 1.01e-8, (k, res)
+
+
+def test_oracle_matches_reference_at_64():
+    """The oracle against the reference's OpenMP build on the 64^3 benchmark
+    scene (compact fixture), first step: maps and flags bit-exact, identical
+    iteration counts and dt, fields within 1e-7."""
+    from common import compare_big, load_big
+    desc, z, log, _ = load_big("config1_64")
+    I = oracle.scene(desc)
+    fails, _ = compare_big(I.get, z, 0, tol=0.0)
+    assert not fails, fails
+    r = I.stepImplicit()
+    ref = log[0]
+    assert r["iterations"] == [ref["solid_iters"][0], ref["pressure_iters"][0], ref["solid_iters"][1]]
+    assert r["dt"] == ref["dt"]
+    assert abs(r["energy"] - ref["energy"]) <= 1e-9 * abs(ref["energy"])
+    fails, _ = compare_big(I.get, z, 1, tol=1e-7)
+    assert not fails, fails

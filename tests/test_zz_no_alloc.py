@@ -1,9 +1,16 @@
 """esf_pressure_solve_static, the allocation-free FP64 pressure solve, against
-esf_pressure_solve at ESF_FP64 on two different systems solved one after the
-other (and the first again): same iterations, same bits, the same device
-memory free before and after. Collected last so that it runs both alone and
-after every other test in the process."""
+esf_pressure_solve at ESF_FP64: two different systems solved one after the
+other (and the first again) give the same iterations and the same bits, the
+largest grid the static scratch takes (64^3 cells) included; a child process
+with a counting shim in front of the CUDA runtime shows that the calls make
+no allocation, free or stream/event/graph creation at all. Collected last so
+that it runs both alone and after every other test in the process."""
 import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import textwrap
 
 import numpy as np
 import pytest
@@ -11,6 +18,8 @@ import pytest
 import oracle
 
 pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
 
 
 def _dev(a):
@@ -44,16 +53,16 @@ def _system(X, seed):
     return g, minv, _jacobi_diag(X, minv), b, x0
 
 
-def _solve(lib, fn, system):
+def _solve(lib, fn, system, max_it=20000):
     import torch
     g, minv, diag, b, x0 = system
     dm, dd, db, dx = _dev(minv), _dev(diag), _dev(b), _dev(x0)
     it, rr = C.c_int(), C.c_double()
     if fn == "static":
         s = lib.esf_pressure_solve_static(C.byref(g), _ptr(dm), _ptr(dd), _ptr(db), _ptr(dx), 1e-8,
-                                          20000, C.byref(it), C.byref(rr), None)
+                                          max_it, C.byref(it), C.byref(rr), None)
     else:
-        s = lib.esf_pressure_solve(C.byref(g), _ptr(dm), _ptr(dd), _ptr(db), _ptr(dx), 1e-8, 20000,
+        s = lib.esf_pressure_solve(C.byref(g), _ptr(dm), _ptr(dd), _ptr(db), _ptr(dx), 1e-8, max_it,
                                    0, C.byref(it), C.byref(rr), None)
     torch.cuda.synchronize()
     return s, it.value, rr.value, dx.cpu().numpy()
@@ -67,6 +76,7 @@ def test_static_solve_equals_allocating_solve(gpu_lib):
     free0 = torch.cuda.mem_get_info()[0]
     got = [_solve(gpu_lib, "static", systems[1]), _solve(gpu_lib, "static", systems[0])]
     free1 = torch.cuda.mem_get_info()[0]
+    # a secondary check only (device-wide; the counting test below is the proof)
     assert free1 == free0, (free0, free1)
     ref = [_solve(gpu_lib, "alloc", s) for s in systems]
     for (s, it, rr, x), (s0, it0, rr0, x0) in zip([first, got[0]], ref):
@@ -75,6 +85,18 @@ def test_static_solve_equals_allocating_solve(gpu_lib):
         assert np.array_equal(x, x0)
     # the repeat of system 0 starts from clean scratch: identical to the first call
     assert got[1][1] == first[1] and np.array_equal(got[1][3], first[3])
+
+
+def test_static_solve_at_the_size_limit(gpu_lib):
+    """64^3 cells fill all five vectors and the partial sums of the scratch:
+    the same bits as the allocating solve, twice in a row."""
+    system = _system(65, 13)
+    ref = _solve(gpu_lib, "alloc", system, max_it=3000)
+    for _ in range(2):
+        s, it, rr, x = _solve(gpu_lib, "static", system, max_it=3000)
+        assert s == 0 and ref[0] == 0
+        assert it == ref[1] and rr == ref[2], (it, ref[1], rr, ref[2])
+        assert np.array_equal(x, ref[3])
 
 
 def test_static_solve_rejects_oversize_grid(gpu_lib):
@@ -86,3 +108,54 @@ def test_static_solve_rejects_oversize_grid(gpu_lib):
                                           10, C.byref(it), C.byref(rr), None)
     assert s == 8  # ESF_ERR_UNSUPPORTED
     assert b"static scratch holds at most" in gpu_lib.esf_last_error()
+
+
+_CHILD = textwrap.dedent("""
+    import ctypes as C, json, sys
+    sys.path[:0] = [{root!r}, {tests!r}, {oracle!r}]
+    import torch
+    import eulersf_gb300 as E
+    from test_zz_no_alloc import _system, _dev, _ptr
+    counter = C.CDLL({shim!r})
+    counter.esf_test_alloc_calls.restype = C.c_ulonglong
+    lib = E.load()
+    g, minv, diag, b, x0 = _system(33, 21)
+    dm, dd, db = _dev(minv), _dev(diag), _dev(b)
+    xs = [_dev(x0) for _ in range(4)]
+    torch.cuda.synchronize()
+    it, rr = C.c_int(), C.c_double()
+    def static(x):
+        return lib.esf_pressure_solve_static(C.byref(g), _ptr(dm), _ptr(dd), _ptr(db), _ptr(x),
+                                             1e-8, 20000, C.byref(it), C.byref(rr), None)
+    out = {{"first": static(xs[0])}}  # looks up the scratch address
+    c0 = counter.esf_test_alloc_calls()
+    out["static"] = [static(xs[1]), static(xs[2])]
+    c1 = counter.esf_test_alloc_calls()
+    out["alloc"] = lib.esf_pressure_solve(C.byref(g), _ptr(dm), _ptr(dd), _ptr(db), _ptr(xs[3]),
+                                          1e-8, 20000, 0, C.byref(it), C.byref(rr), None)
+    c2 = counter.esf_test_alloc_calls()
+    out["static_calls"], out["alloc_calls"] = c1 - c0, c2 - c1
+    torch.cuda.synchronize()
+    out["same"] = bool(torch.equal(xs[1], xs[3]) and torch.equal(xs[2], xs[3]))
+    print(json.dumps(out))
+""")
+
+
+def test_static_solve_makes_no_allocation_calls(gpu_lib, tmp_path):
+    """Two static solves in a child process whose CUDA runtime calls pass
+    through a counting shim: none allocates, frees or creates anything, while
+    the allocating solve on the same system is seen doing so (the shim works)."""
+    shim = str(tmp_path / "alloc_counter.so")
+    r = subprocess.run(["gcc", "-shared", "-fPIC", "-O2", "-o", shim,
+                        os.path.join(HERE, "alloc_counter.c"), "-ldl"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    code = _CHILD.format(root=ROOT, tests=HERE, oracle=os.path.join(ROOT, "oracle"), shim=shim)
+    env = dict(os.environ, LD_PRELOAD=shim)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    assert out["first"] == 0 and out["static"] == [0, 0] and out["alloc"] == 0, out
+    assert out["alloc_calls"] > 0, out
+    assert out["static_calls"] == 0, out
+    assert out["same"], out
