@@ -13,6 +13,14 @@ the 129 MB L2, so no flush is needed between steps.
 
 N > 1 runs N independent replicas (one scene per GPU): the step does not
 shard. Prints one JSON line (rank 0).
+
+Beside the mixed-precision headline, a single-GPU run also steps the plain
+FP64 GPU path over the first steps of the same scene (--fp64-steps, default
+3: steps 1..3, after an untimed step 0 that both paths take) and reports
+the ratio of the two paths' steps/s on those steps, each path's pressure
+iterations, and the L-inf differences of velocity and pressure between them
+after each compared step; and it re-checks the final mixed pressure solve's
+relative residual with the CPU oracle's operator (outside the timed region).
 """
 from __future__ import annotations
 
@@ -32,10 +40,14 @@ sys.path.insert(0, ROOT)
 METRIC = "coupled steps/s and CG iters/s at 256^3 (mixed vs FP64 GPU)"
 UNIT = "steps/s"
 # Pressure PCR iterations per step of the reference's FP64 algorithm on this
-# workload (steps 0-7), from the FP64 GPU path, whose counts match the
-# reference's to within one 5-iteration check interval:
-# profiles/mixed_vs_fp64_256.md. Later steps use the mean of steps 5-7.
-FP64_PRESSURE_ITERS_256 = [19060, 14655, 9545, 8925, 6770, 5385, 5740, 5360]
+# workload, steps 0-29, counted by the FP64 GPU path (its counts match the
+# reference's build to within one 5-iteration check interval at 64^3 over 20
+# steps): profiles/mixed_vs_fp64_256.md. Later steps use the mean of steps
+# 27-29. A single-GPU run re-counts its first steps live (fp64_gpu) and
+# reports whether they agree with this table.
+FP64_PRESSURE_ITERS_256 = [19060, 14655, 9545, 8925, 6770, 5385, 5740, 5360, 5795, 6785,
+                           6615, 5390, 6790, 7325, 5665, 6930, 8310, 6650, 12150, 14465,
+                           14565, 11800, 10665, 20430, 13165, 10400, 9745, 10470, 10325, 14700]
 
 
 def fp64_iters(step):
@@ -60,6 +72,16 @@ def config_dict(desc, precision, n_gpus):
                         f"fluid 1000 / solid 1100, dt=1/240, tol 1e-8, seed {desc.noise_seed}",
             "grid_cells": desc.N ** 3, "precision": precision, "parallelism": f"replicas x{n_gpus}",
             "l2": "inputs larger than L2 (no flush)"}
+
+
+def _linf(a, b):
+    """max |a - b| / max |b| (b the FP64 field)."""
+    import numpy as np
+    a = np.asarray(a, dtype=np.float64).reshape(-1)
+    b = np.asarray(b, dtype=np.float64).reshape(-1)
+    s = float(np.abs(b).max()) if b.size else 0.0
+    d = float(np.abs(a - b).max()) if b.size else 0.0
+    return d / s if s > 0 else d
 
 
 def read_peaks():
@@ -207,6 +229,7 @@ def reference_arm(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": config_dict(desc, "fp64 (reference algorithm)", args.gpus),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "extrapolated": True, "sampled_iterations_per_step": sample_iters,
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -226,8 +249,15 @@ def ours(args):
     desc = workload(args.size)
     stream = torch.cuda.current_stream()
     I = E.make_scene(desc, precision=prec, stream=stream.cuda_stream)
-    for _ in range(args.warmup):
-        I.stepImplicit()
+    # the FP64 comparison covers steps 1..F, which the warm-up takes (step 0
+    # carries the first step's one-time set-up on both paths)
+    compare = (world == 1 and prec == abi.ESF_MIXED and not args.no_fp64)
+    F = max(0, min(args.fp64_steps, args.warmup - 1)) if compare else 0
+    warm_reports, snaps = [], {}
+    for k in range(args.warmup):
+        warm_reports.append(I.stepImplicit())
+        if 1 <= k <= F:
+            snaps[k] = (I.get("velocity"), I.get("lambda1"))
     # ---- timed region. Every step goes through the public C ABI: the step's
     # input field (intensity, the smoke source) is copied in from pinned host
     # memory, esf_step runs, and its result (the velocity field) is copied
@@ -276,6 +306,19 @@ def ours(args):
            "what": "the timed steps themselves, each with the intensity field copied in and the "
                    "velocity field copied out through pinned host buffers (esf_set_field, esf_step, "
                    "esf_get_field)"}
+    # ---- independent check of the last mixed pressure solve: its relative
+    # residual with the CPU oracle's operator (rank 0, N=1; outside the timing)
+    final_check = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        tr = time.perf_counter()
+        res = oracle.pressure_residual(I)
+        final_check = {"relative_residual": res, "step": args.warmup + args.steps - 1,
+                       "gpu_reported": max(reports[-1]["rel_residual"]),
+                       "seconds": time.perf_counter() - tr,
+                       "what": "||J M^-1 J^T lambda1 - b1|| / ||b1|| of the last timed step's pressure "
+                               "solve, evaluated by the oracle on the host"}
     # ---- dominant kernel of the pressure PCR: the one-pass FP32 iteration
     # (mixed, rows a multiple of 4 floats) or the update + stencil + dot kernel
     upd, axpy = C.c_double(), C.c_double()
@@ -302,6 +345,7 @@ def ours(args):
     else:
         kname = ("pressure_update_tma" if (w == 4 and desc.N % 4 == 0) else
                  f"pressure_stencil<{'float' if w == 4 else 'double'}, update>")
+    dram_gbs = traffic / (upd.value * 1e-3) / 1e9 if (traffic and achieved) else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                 "peak_kind": peak_kind, "kernel": kname,
@@ -309,7 +353,50 @@ def ours(args):
                 "algorithmic_bytes_per_launch": algo,
                 "words_per_row": {"algorithmic": words, "moved": moved},
                 "moved_bytes_per_launch": moved * w * R,
-                "frac_of_moved": (moved_gbs / peak) if moved_gbs else None}
+                "frac_of_moved": (moved_gbs / peak) if moved_gbs else None,
+                "dram_achieved_gbs": dram_gbs,
+                "dram_frac": (dram_gbs / peak) if dram_gbs else None,
+                "note": "achieved/frac count the per-iteration model's words (a whole iteration but "
+                        "its residual check: 17 words a row); the one-pass kernel folds the Jacobi "
+                        "scaling into its vectors and moves 12 (frac_of_moved); dram_* divide the "
+                        "ncu-measured DRAM bytes of one launch (traffic, with L2 compression) by "
+                        "the same duration"}
+    # ---- the plain FP64 GPU path on the same scene, steps 1..F
+    fp64 = None
+    if F > 0:
+        I.close()  # the mixed scene's memory is not needed any more
+        I = None
+        D = E.make_scene(desc, precision=abi.ESF_FP64, stream=stream.cuda_stream)
+        rows = []
+        for k in range(F + 1):
+            r = D.stepImplicit()
+            if k == 0:
+                continue
+            vm, lm = snaps[k]
+            rows.append({"step": k, "fp64_ms": r["device_ms"], "mixed_ms": warm_reports[k]["device_ms"],
+                         "fp64_pressure_iters": r["iterations"][1],
+                         "mixed_pressure_iters": warm_reports[k]["iterations"][1],
+                         "fp64_rel_residual": max(r["rel_residual"]),
+                         "mixed_rel_residual": max(warm_reports[k]["rel_residual"]),
+                         "l_inf_velocity": _linf(vm, D.get("velocity")),
+                         "l_inf_pressure": _linf(lm, D.get("lambda1"))})
+        D.close()
+        t64 = sum(r["fp64_ms"] for r in rows) * 1e-3
+        tmx = sum(r["mixed_ms"] for r in rows) * 1e-3
+        table = [fp64_iters(r["step"]) for r in rows]
+        fp64 = {"steps": [r["step"] for r in rows],
+                "fp64_gpu_steps_per_s": len(rows) / t64, "mixed_steps_per_s_same_steps": len(rows) / tmx,
+                "mixed_over_fp64": t64 / tmx,
+                "fp64_pressure_iters_each_step": [r["fp64_pressure_iters"] for r in rows],
+                "fp64_iters_match_table": [r["fp64_pressure_iters"] for r in rows] == table,
+                "mixed_pressure_iters_each_step": [r["mixed_pressure_iters"] for r in rows],
+                "l_inf_velocity_each_step": [r["l_inf_velocity"] for r in rows],
+                "l_inf_pressure_each_step": [r["l_inf_pressure"] for r in rows],
+                "rel_residual_max": {"fp64": max(r["fp64_rel_residual"] for r in rows),
+                                     "mixed": max(r["mixed_rel_residual"] for r in rows)},
+                "what": "both paths from the same initial state, steps 1..F (step 0 untimed on both: "
+                        "first-step set-up); device time of each step (CUDA events in esf_step); "
+                        "L-inf = max |mixed - fp64| / max |fp64| of the field after the step"}
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -318,11 +405,16 @@ def ours(args):
         per_iter = tc / max(it, 1)
         t_step = per_iter * fp64_iters_window(args.warmup, args.steps)
         cpu = {"value": 1.0 / t_step, "unit": UNIT, "cores": threads, "kind": "port",
+               "extrapolated": True, "sampled_iterations": it, "sample_seconds": tc, "seconds_per_iteration": per_iter,
+               "fp64_iters_per_step": fp64_iters_window(args.warmup, args.steps),
                "sample": f"{it} FP64 pressure-PCR iterations at {desc.N}^3 on the oracle port "
                          f"({tc:.1f} s, {threads} threads); steps/s = 1 / (time per iteration x "
                          f"{fp64_iters_window(args.warmup, args.steps):.0f}, the reference algorithm's "
                          f"pressure iterations per step over the same steps "
-                         f"{args.warmup}..{args.warmup + args.steps - 1}); non-solver work not counted"}
+                         f"{args.warmup}..{args.warmup + args.steps - 1}, counted by the FP64 GPU path); "
+                         f"non-solver work not counted"}
+        if final_check is not None:
+            cpu["residual_check"] = final_check
     if rank == 0:
         last = reports[-1]
         line = {
@@ -337,10 +429,16 @@ def ours(args):
             "refinements_last_step": last["refinements"],
             "rel_residual_max": max(max(r["rel_residual"]) for r in reports),
             "phase_ms_last_step": last["phase_ms"], "roofline": roofline, "cpu_baseline": cpu,
+            "fp64_gpu": fp64,
+            "mixed_over_fp64": fp64["mixed_over_fp64"] if fp64 else None,
+            "fp64_gpu_steps_per_s": fp64["fp64_gpu_steps_per_s"] if fp64 else None,
+            "l_inf_velocity": max(fp64["l_inf_velocity_each_step"]) if fp64 else None,
+            "l_inf_pressure": max(fp64["l_inf_pressure_each_step"]) if fp64 else None,
             "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
         }
         print(json.dumps(line), flush=True)
-    I.close()
+    if I is not None:
+        I.close()
     if pg is not None:
         pg.destroy_process_group()
     return 0
@@ -356,6 +454,9 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-iters", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--fp64-steps", type=int, default=3,
+                    help="FP64 GPU comparison over steps 1..F (bounded by --warmup - 1)")
+    ap.add_argument("--no-fp64", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
