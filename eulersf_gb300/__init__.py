@@ -23,10 +23,10 @@ EXPORTS = [
     "esf_abi_version", "esf_last_error", "esf_params_default", "esf_parse_config", "esf_create",
     "esf_destroy", "esf_add_solid", "esf_set_fluid", "esf_init", "esf_set_max_dt", "esf_step",
     "esf_dt", "esf_field_info", "esf_get_field", "esf_set_field", "esf_pressure_apply",
-    "esf_pressure_solve", "esf_pressure_solve_static", "esf_write_frame", "esf_read_frame", "esf_kernel_launches",
+    "esf_pressure_solve", "esf_pressure_solve_batch", "esf_pressure_solve_static", "esf_write_frame", "esf_read_frame", "esf_kernel_launches",
     "esf_time_pressure_kernels", "esf_scene_footprint", "esf_server_create", "esf_server_submit",
     "esf_server_poll", "esf_server_wait", "esf_server_get_field", "esf_server_release",
-    "esf_server_destroy", "esf_selftest_bounded_wait",
+    "esf_server_destroy", "esf_server_batch_stats", "esf_selftest_bounded_wait",
 ]
 
 
@@ -50,6 +50,9 @@ def load(build_if_missing: bool = False) -> C.CDLL:
     lib.esf_pressure_apply.argtypes = [C.POINTER(abi.Grid), vp, vp, vp, vp]
     lib.esf_pressure_solve.argtypes = [C.POINTER(abi.Grid), vp, vp, vp, vp, C.c_double, C.c_int,
                                        C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), vp]
+    lib.esf_pressure_solve_batch.argtypes = [C.c_int, C.POINTER(abi.Grid), C.POINTER(vp), C.POINTER(vp),
+                                             C.POINTER(vp), C.POINTER(vp), C.c_double, C.c_int, C.c_int,
+                                             C.POINTER(C.c_int), C.POINTER(C.c_double), vp]
     lib.esf_pressure_solve_static.argtypes = [C.POINTER(abi.Grid), vp, vp, vp, vp, C.c_double,
                                               C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                               vp]

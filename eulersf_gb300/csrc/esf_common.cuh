@@ -172,6 +172,15 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
                           int precision, double innerEps, int maxRefine, int* iters,
                           double* relres, int* refinements, int* converged, cudaStream_t st,
                           int* fp64Iters = nullptr);
+// continuous batching of the mixed inner solves of several scenes (serving,
+// batched solves): scenes whose pressure work is attached to a batcher hand
+// their inner solves over to its thread and streams (esf_solver.cu)
+struct InnerBatcher;
+esf_status batcher_create(int device, InnerBatcher** out);
+void batcher_destroy(InnerBatcher* b);
+void batcher_stats(InnerBatcher* b, long long* launches, long long* taskLaunches, long long* maxTasks,
+                   long long* solves);
+esf_status pressure_work_set_batcher(PressureWork* w, InnerBatcher* b);
 // self-test of the TMA kernels' bounded mbarrier wait (esf_solver.cu)
 esf_status selftest_mbar_wait(int* gaveUp, cudaStream_t st);
 // allocation-free FP64 solve on the module's static scratch (esf_solver.cu)

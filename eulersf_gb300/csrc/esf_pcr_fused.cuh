@@ -96,10 +96,13 @@ __device__ __forceinline__ void finish_fused(PcrState* st, double dl, double mu,
   }
 }
 
-__global__ void __launch_bounds__(NT, 4) pcr_iteration_fused(GridDev g, const __grid_constant__ FusedMaps tm,
-                                                             FusedPtrs p, double* partial, PcrState* st,
-                                                             int cz) {
-  extern __shared__ __align__(128) unsigned char smem[];
+// One block's share of a pass: the 64 x 8-cell column (bx, by) over the cell
+// layers bz*cz .. bz*cz+cz-1 of the scene (g, tm, p, partial, st), whose
+// pass has nb blocks; bid is this block's place among them (the order in
+// which the last block folds the partial sums).
+__device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm, const FusedPtrs& p,
+                                           double* partial, PcrState* st, int cz, int bx, int by,
+                                           int bz, int nb, int bid, unsigned char* smem) {
   unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem + FU_OFF_BAR);
   float* sP = reinterpret_cast<float*>(smem + FU_OFF_P);
   float* sQ = reinterpret_cast<float*>(smem + FU_OFF_SQ);
@@ -110,13 +113,13 @@ __global__ void __launch_bounds__(NT, 4) pcr_iteration_fused(GridDev g, const __
   __shared__ bool amLast;
   if (st->done) return;
   if (st->iter >= st->maxIt) {
-    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0) st->done = 1;
+    if (bid == 0 && threadIdx.x == 0) st->done = 1;
     return;
   }
   const int pin = st->pp & 1, pout = pin ^ 1;
   const float alpha = (float)st->alpha, beta = (float)st->beta;
   const int tid = threadIdx.x;
-  const int x0 = blockIdx.x * TXW, y0 = blockIdx.y * TY, z0 = blockIdx.z * cz;
+  const int x0 = bx * TXW, y0 = by * TY, z0 = bz * cz;
   const int z1 = min(z0 + cz, g.cZ);
   const int nsteps = z1 - z0 + 2;  // cell layers z0-1 .. z1
 
@@ -325,8 +328,6 @@ __global__ void __launch_bounds__(NT, 4) pcr_iteration_fused(GridDev g, const __
     return;
   }
   // the four sums: block partials, folded in block order by the last block
-  const int nb = gridDim.x * gridDim.y * gridDim.z;
-  const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
   const double pDl = block_sum<NT>((double)sDl, sred);
   const double pMu = block_sum<NT>((double)sMu, sred);
   const double pNu = block_sum<NT>((double)sNu, sred);
@@ -353,4 +354,62 @@ __global__ void __launch_bounds__(NT, 4) pcr_iteration_fused(GridDev g, const __
     st->ticket[1] = 0;
     finish_fused(st, tDl, tMu, tNu, tOm);
   }
+}
+
+__global__ void __launch_bounds__(NT, 4) pcr_iteration_fused(GridDev g, const __grid_constant__ FusedMaps tm,
+                                                             FusedPtrs p, double* partial, PcrState* st,
+                                                             int cz) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  fused_pass(g, tm, p, partial, st, cz, blockIdx.x, blockIdx.y, blockIdx.z,
+             gridDim.x * gridDim.y * gridDim.z,
+             blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z), smem);
+}
+
+// ---- several scenes' inner solves in one launch (continuous batching).
+// A task is one scene's inner solve: its grid, tensor maps, vectors, partial
+// sums and state, and its pass's shape (cz layers per block, gx x gy x gz
+// blocks). Tasks live in device memory (tensor maps there must be 64-byte
+// aligned; the host writes them before the launches that read them).
+struct FusedTask {
+  FusedMaps tm;
+  GridDev g;
+  FusedPtrs p;
+  double* partial;
+  PcrState* st;
+  int cz, gx, gy, gz;
+};
+static_assert(alignof(FusedTask) >= 64 && sizeof(FusedTask) % 64 == 0, "tensor maps need 64-byte alignment");
+// The launch's list: entry k is (task slot, first block of that task in the
+// launch); blocks [first_k, first_{k+1}) run task k's pass, so each task's
+// blocks see the same (bx, by, bz), block count and block order as a launch
+// of that scene alone, and their sums fold to the same bits.
+constexpr int FU_MAX_BATCH = 256;
+struct FusedBatch {
+  int n;
+  int slot[FU_MAX_BATCH];
+  int first[FU_MAX_BATCH + 1];
+};
+
+__global__ void __launch_bounds__(NT, 4) pcr_iteration_fused_batch(const FusedTask* tasks,
+                                                                   const __grid_constant__ FusedBatch b) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int blk = blockIdx.x;
+  int lo = 0, hi = b.n - 1;  // the last k with first[k] <= blk
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (b.first[mid] <= blk) lo = mid;
+    else hi = mid - 1;
+  }
+  const FusedTask& t = tasks[b.slot[lo]];
+  const int local = blk - b.first[lo];
+  const int nb = t.gx * t.gy * t.gz;
+  if (local >= nb) return;
+  const int bx = local % t.gx, by = (local / t.gx) % t.gy, bz = local / (t.gx * t.gy);
+  fused_pass(t.g, t.tm, t.p, t.partial, t.st, t.cz, bx, by, bz, nb, local, smem);
+}
+
+// The states of a batch's tasks, in list order, for one copy to the host.
+__global__ void gather_task_states(const FusedTask* tasks, const __grid_constant__ FusedBatch b,
+                                   PcrState* out) {
+  for (int k = threadIdx.x; k < b.n; k += blockDim.x) out[k] = *tasks[b.slot[k]].st;
 }

@@ -3,7 +3,8 @@
 // device footprint fits the remaining memory budget and a slot is free
 // (first fit in arrival order); each admitted scene runs on its own CUDA
 // stream, driven by its own host thread, so scenes that arrive while others
-// are on the GPU overlap with them on the device. Results stay readable until
+// are on the GPU overlap with them on the device; the inner solves of active
+// scenes of one grid shape share launches (continuous batching, esf_solver.cu). Results stay readable until
 // the client releases the request, which also returns its memory to the
 // budget. The reference has no counterpart: it runs one scene per process
 // (its function-local statics pin one grid size per process).
@@ -25,6 +26,12 @@
 
 namespace esf {
 void set_error(const char* fmt, ...);
+struct InnerBatcher;
+esf_status batcher_create(int device, InnerBatcher** out);
+void batcher_destroy(InnerBatcher* b);
+void batcher_stats(InnerBatcher* b, long long* launches, long long* taskLaunches, long long* maxTasks,
+                   long long* solves);
+esf_status scene_set_batcher(esf_scene* s, InnerBatcher* b);
 }
 
 namespace {
@@ -79,6 +86,7 @@ void add_noise(std::vector<double>& v, const std::vector<double>& solidMass, int
 
 struct esf_server {
   int device = 0;
+  esf::InnerBatcher* batcher = nullptr;  // shared by every scene's inner solves
   size_t budget = 0, inUse = 0;
   int maxActive = 8, active = 0;
   uint64_t next = 1;
@@ -106,6 +114,7 @@ struct esf_server {
     cudaSetDevice(device);
     esf_status e = esf_create(&r->grid, &r->params, nullptr, &r->scene);
     if (e) return e;
+    if (batcher && (e = esf::scene_set_batcher(r->scene, batcher))) return e;
     for (auto& s : r->solids)
       if ((e = esf_add_solid(r->scene, &s->d))) return e;
     if ((e = esf_set_fluid(r->scene, r->density, r->viscosity))) return e;
@@ -216,6 +225,13 @@ extern "C" esf_status esf_server_create(const esf_server_config* cfg, esf_server
   cudaMemGetInfo(&freeB, &totalB);
   s->budget = (cfg && cfg->hbm_budget_bytes) ? cfg->hbm_budget_bytes : (size_t)(0.85 * (double)freeB);
   s->maxActive = (cfg && cfg->max_active > 0) ? cfg->max_active : 8;
+  if (!(cfg && cfg->no_batching)) {
+    esf_status e = esf::batcher_create(s->device, &s->batcher);
+    if (e) {
+      delete s;
+      return e;
+    }
+  }
   for (int i = 0; i < s->maxActive; i++) s->workers.emplace_back([s] { s->worker(); });
   *out = s;
   return ESF_OK;
@@ -352,6 +368,16 @@ extern "C" esf_status esf_server_destroy(esf_server* s) {
   cudaSetDevice(s->device);
   for (auto& kv : s->reqs)
     if (kv.second->scene) esf_destroy(kv.second->scene);
+  esf::batcher_destroy(s->batcher);
   delete s;
+  return ESF_OK;
+}
+
+extern "C" esf_status esf_server_batch_stats(esf_server* s, esf_batch_stats* out) {
+  if (!s || !out) return ESF_ERR_INVALID_ARG;
+  memset(out, 0, sizeof *out);
+  if (s->batcher)
+    esf::batcher_stats(s->batcher, &out->launches, &out->task_launches, &out->max_tasks,
+                       &out->inner_solves);
   return ESF_OK;
 }

@@ -15,6 +15,12 @@
 #include <string.h>
 #include <chrono>
 #include <mutex>
+#include <algorithm>
+#include <array>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <thread>
 #include <cmath>
 #include <type_traits>
 
@@ -510,6 +516,7 @@ struct MappedSet {
   int n;
 };
 
+struct InnerBatcher;
 struct PressureWork {
   long long R, T;
   // FP64 path (also the outer loop of the mixed path)
@@ -540,6 +547,9 @@ struct PressureWork {
   FusedMaps fmaps;
   bool fusedOk;
   MappedSet mapped;  // FP32 vectors mapped by vec_alloc
+  // inner solves handed to a batcher shared with other scenes or systems
+  InnerBatcher* batcher;
+  cudaEvent_t batchReady, batchDone;
 };
 
 // ---- FP32 vectors of the inner solves in compressible memory. They are
@@ -774,6 +784,9 @@ void pressure_work_free(PressureWork* w) {
   if (w->capStream) cudaStreamDestroy(w->capStream);
   for (int i = 0; i < 4; i++)
     if (w->ev[i]) cudaEventDestroy(w->ev[i]);
+  if (w->batcher) pressure_work_set_batcher(w, nullptr);
+  if (w->batchReady) cudaEventDestroy(w->batchReady);
+  if (w->batchDone) cudaEventDestroy(w->batchDone);
   delete w;
 }
 
@@ -1056,6 +1069,9 @@ static esf_status init_state(PcrState* d, double eps, int maxIt, cudaStream_t st
   return ESF_OK;
 }
 
+static esf_status batched_inner_solve(PressureWork* w, const GridDev& g, cudaStream_t st, PcrState* out);
+static bool batching_pays(PressureWork* w);
+
 esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv64,
                           const double* diag64, const double* b, double* x, double eps, int maxIt,
                           int precision, double innerEps, int maxRefine, int* iters,
@@ -1211,8 +1227,10 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
         fprintf(stderr, "[esf] refine %d at %.2f ms: iters %d rel %.3e\n", ref, ms, total, rel);
       }
       PcrState hi;
-      esf_status e = run_graph_solve(w->hst, w->ev, w->st32, nullptr, w->gChunk32, 0, w->kChunk32,
-                                     maxIt, st, &hi);
+      esf_status e = (fused && batching_pays(w))
+                         ? batched_inner_solve(w, g, st, &hi)
+                         : run_graph_solve(w->hst, w->ev, w->st32, nullptr, w->gChunk32, 0, w->kChunk32,
+                                           maxIt, st, &hi);
       if (e) return e;
       total = hi.iter;
       if (hi.status) {
@@ -1710,6 +1728,338 @@ esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const in
   if (relres) *relres = rel;
   if (converged) *converged = conv;
   return status;
+}
+
+// ------------------------------------------- continuous batching (serving)
+// The inner FP32 solves of the mixed pressure solves of several scenes (the
+// scenes a server is stepping, or the systems of one batched solve),
+// advanced in shared launches: one host thread launches chunks of
+// pcr_iteration_fused_batch, each chunk five iterations of every task in the
+// batch, then gathers the tasks' states into pinned memory. A scene's thread
+// hands its inner solve over (after its set-up pass, behind an event on the
+// scene's stream) and blocks; the task joins at the next chunk and leaves
+// once its state reads done, when the scene's stream is made to wait for
+// everything queued on the batch's stream so far. Tasks that finish inside a
+// chunk exit the chunk's later launches at once (their state says done): the
+// per-scene convergence mask.
+// A launch lasts as long as its slowest task, so only scenes of one grid
+// shape share launches: each shape has its own lane (stream, tasks, chunks in
+// flight), and lanes of different shapes run side by side on the device.
+// Up to three chunks are in flight per lane.
+struct InnerBatcher {
+  static constexpr int kSlots = FU_MAX_BATCH, kInflight = 3, kRing = 4, kChunk = 5;
+  struct Job {
+    FusedTask task;
+    cudaEvent_t ready = nullptr, done = nullptr;
+    bool finished = false;
+    PcrState out;
+    int slot = -1;
+    unsigned long long seq = 0;  // unique per job: a finished job's memory can be reused
+  };
+  struct Entry {
+    Job* job;
+    unsigned long long seq;
+    int slot;
+  };
+  struct Chunk {
+    int ring;
+    unsigned long long order;  // launch order across lanes
+    std::vector<Entry> jobs;   // the chunk's tasks in list order
+  };
+  struct Lane {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[kRing] = {};
+    PcrState* dStates = nullptr;  // [kRing][kSlots]
+    PcrState* hStates = nullptr;  // pinned copies
+    std::vector<Job*> active;
+    std::deque<Chunk> inflight;
+    long long chunks = 0;
+  };
+  using Shape = std::array<int, 4>;  // cells per axis and the pass's layers per block
+  int device = 0;
+  FusedTask* dTasks = nullptr;   // device task slots (64-byte aligned)
+  FusedTask* hTasks = nullptr;   // pinned staging of the slots
+  // a slot is free for a new task when no task holds it and no chunk in
+  // flight lists it (lanes run on different streams: a chunk still queued on
+  // one lane reads its slots' descriptors when it runs)
+  bool slotUsed[kSlots] = {};
+  int slotRefs[kSlots] = {};
+  std::map<Shape, Lane> lanes;
+  std::map<std::array<int, 3>, int> attached;  // works attached, by grid shape (cells per axis)
+  std::mutex m;
+  std::condition_variable cv, doneCv;
+  std::deque<Job*> pending;
+  bool stop = false;
+  std::thread thr;
+  long long launches = 0, taskLaunches = 0, maxTasks = 0, solves = 0;
+  unsigned long long nextSeq = 1, nextOrder = 0;
+
+  static Shape shape_of(const FusedTask& t) { return {t.g.cX, t.g.cY, t.g.cZ, t.cz}; }
+
+  esf_status init(int dev) {
+    device = dev;
+    cudaSetDevice(dev);
+    ESF_CUDA(cudaMalloc(&dTasks, sizeof(FusedTask) * kSlots));
+    ESF_CUDA(cudaMallocHost(&hTasks, sizeof(FusedTask) * kSlots));
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        pcr_iteration_fused_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, FU_SMEM);
+    if (attr != cudaSuccess) {
+      set_error("pcr_iteration_fused_batch: %d bytes of shared memory refused: %s", FU_SMEM,
+                cudaGetErrorString(attr));
+      return ESF_ERR_CUDA;
+    }
+    thr = std::thread([this] { loop(); });
+    return ESF_OK;
+  }
+  esf_status lane_init(Lane& L) {
+    ESF_CUDA(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
+    for (int i = 0; i < kRing; i++) ESF_CUDA(cudaEventCreateWithFlags(&L.ev[i], cudaEventDisableTiming));
+    ESF_CUDA(cudaMalloc(&L.dStates, sizeof(PcrState) * kSlots * kRing));
+    ESF_CUDA(cudaMallocHost(&L.hStates, sizeof(PcrState) * kSlots * kRing));
+    return ESF_OK;
+  }
+  void shutdown() {
+    {
+      std::lock_guard<std::mutex> g(m);
+      stop = true;
+    }
+    cv.notify_all();
+    if (thr.joinable()) thr.join();
+    cudaSetDevice(device);
+    for (auto& kv : lanes) {
+      Lane& L = kv.second;
+      if (L.stream) cudaStreamSynchronize(L.stream);
+      for (int i = 0; i < kRing; i++)
+        if (L.ev[i]) cudaEventDestroy(L.ev[i]);
+      cudaFree(L.dStates);
+      if (L.hStates) cudaFreeHost(L.hStates);
+      if (L.stream) cudaStreamDestroy(L.stream);
+    }
+    cudaFree(dTasks);
+    if (hTasks) cudaFreeHost(hTasks);
+  }
+  // called by a scene's thread; blocks until the task is done
+  esf_status solve(Job* j) {
+    {
+      std::lock_guard<std::mutex> g(m);
+      if (stop) {
+        set_error("inner-solve batcher: stopped");
+        return ESF_ERR_STATE;
+      }
+      j->seq = nextSeq++;
+      pending.push_back(j);
+    }
+    cv.notify_all();
+    std::unique_lock<std::mutex> g(m);
+    doneCv.wait(g, [&] { return j->finished; });
+    return j->out.status == ESF_ERR_CUDA && !j->out.iter ? ESF_ERR_CUDA : ESF_OK;
+  }
+  // a lane's oldest chunk in flight: read its states, finish the tasks that are done
+  void settle(Lane& L) {
+    Chunk c = std::move(L.inflight.front());
+    L.inflight.pop_front();
+    cudaEventSynchronize(L.ev[c.ring]);
+    bool any = false;
+    std::lock_guard<std::mutex> g(m);
+    for (size_t i = 0; i < c.jobs.size(); i++) {
+      slotRefs[c.jobs[i].slot]--;
+      const PcrState& h = L.hStates[c.ring * kSlots + i];
+      if (!h.done) continue;
+      // only jobs still active are alive; a finished one is not touched
+      auto it = std::find(L.active.begin(), L.active.end(), c.jobs[i].job);
+      if (it == L.active.end() || (*it)->seq != c.jobs[i].seq) continue;
+      Job* j = *it;
+      L.active.erase(it);
+      // after every chunk queued so far, some of which may still hold the task
+      cudaEventRecord(j->done, L.stream);
+      slotUsed[j->slot] = false;
+      j->out = h;
+      j->finished = true;
+      solves++;
+      any = true;
+    }
+    if (any) doneCv.notify_all();
+  }
+  // one chunk of a lane's active tasks
+  void launch(Lane& L) {
+    std::vector<Entry> ids;
+    FusedBatch b;
+    int blocks = 0;
+    {
+      std::lock_guard<std::mutex> g(m);
+      b.n = (int)L.active.size();
+      for (int k = 0; k < b.n; k++) {
+        const FusedTask& t = L.active[k]->task;
+        b.slot[k] = L.active[k]->slot;
+        b.first[k] = blocks;
+        blocks += t.gx * t.gy * t.gz;
+        ids.push_back(Entry{L.active[k], L.active[k]->seq, L.active[k]->slot});
+        slotRefs[L.active[k]->slot]++;
+      }
+    }
+    b.first[b.n] = blocks;
+    const int ring = (int)(L.chunks % kRing);
+    for (int k = 0; k < kChunk; k++) {
+      ESF_COUNTED pcr_iteration_fused_batch<<<blocks, NT, FU_SMEM, L.stream>>>(dTasks, b);
+    }
+    ESF_COUNTED gather_task_states<<<1, 64, 0, L.stream>>>(dTasks, b, L.dStates + ring * kSlots);
+    cudaMemcpyAsync(L.hStates + ring * kSlots, L.dStates + ring * kSlots, sizeof(PcrState) * b.n,
+                    cudaMemcpyDeviceToHost, L.stream);
+    cudaEventRecord(L.ev[ring], L.stream);
+    L.chunks++;
+    launches += kChunk;
+    taskLaunches += (long long)kChunk * b.n;
+    if (b.n > maxTasks) maxTasks = b.n;
+    L.inflight.push_back(Chunk{ring, nextOrder++, std::move(ids)});
+  }
+  void loop() {
+    cudaSetDevice(device);
+    for (;;) {
+      std::vector<Job*> joining;
+      {
+        std::unique_lock<std::mutex> g(m);
+        bool busy = false;
+        for (auto& kv : lanes) busy = busy || !kv.second.active.empty() || !kv.second.inflight.empty();
+        if (!busy) cv.wait(g, [&] { return stop || !pending.empty(); });
+        if (stop && pending.empty() && !busy) return;
+        while (!pending.empty()) {
+          int s = 0;
+          while (s < kSlots && (slotUsed[s] || slotRefs[s] > 0)) s++;
+          if (s == kSlots) break;  // wait for chunks in flight to release slots
+          Job* j = pending.front();
+          pending.pop_front();
+          slotUsed[s] = true;
+          j->slot = s;
+          joining.push_back(j);
+        }
+      }
+      for (Job* j : joining) {
+        Lane& L = lanes[shape_of(j->task)];
+        if (!L.stream && lane_init(L) != ESF_OK) {
+          std::lock_guard<std::mutex> g(m);
+          memset(&j->out, 0, sizeof j->out);
+          j->out.status = ESF_ERR_CUDA;
+          j->out.done = 1;
+          j->finished = true;
+          slotUsed[j->slot] = false;
+          doneCv.notify_all();
+          continue;
+        }
+        hTasks[j->slot] = j->task;
+        cudaMemcpyAsync(dTasks + j->slot, hTasks + j->slot, sizeof(FusedTask), cudaMemcpyHostToDevice,
+                        L.stream);
+        cudaStreamWaitEvent(L.stream, j->ready, 0);
+        std::lock_guard<std::mutex> g(m);
+        L.active.push_back(j);
+      }
+      // a chunk on every lane that has tasks and room; settle what is ready
+      bool launched = false;
+      for (auto& kv : lanes) {
+        Lane& L = kv.second;
+        while (!L.inflight.empty() && cudaEventQuery(L.ev[L.inflight.front().ring]) == cudaSuccess)
+          settle(L);
+        bool has;
+        {
+          std::lock_guard<std::mutex> g(m);
+          has = !L.active.empty();
+        }
+        if (has && (int)L.inflight.size() < kInflight) {
+          launch(L);
+          launched = true;
+        }
+      }
+      if (!launched) {
+        // every lane is full or idle: wait for the oldest chunk in flight
+        Lane* oldest = nullptr;
+        for (auto& kv : lanes)
+          if (!kv.second.inflight.empty() &&
+              (!oldest || kv.second.inflight.front().order < oldest->inflight.front().order))
+            oldest = &kv.second;
+        if (oldest) settle(*oldest);
+      }
+    }
+  }
+};
+
+esf_status batcher_create(int device, InnerBatcher** out) {
+  InnerBatcher* b = new InnerBatcher();
+  esf_status e = b->init(device);
+  if (e) {
+    b->shutdown();
+    delete b;
+    return e;
+  }
+  *out = b;
+  return ESF_OK;
+}
+void batcher_destroy(InnerBatcher* b) {
+  if (!b) return;
+  b->shutdown();
+  delete b;
+}
+void batcher_stats(InnerBatcher* b, long long* launches, long long* taskLaunches, long long* maxTasks,
+                   long long* solves) {
+  std::lock_guard<std::mutex> g(b->m);
+  *launches = b->launches;
+  *taskLaunches = b->taskLaunches;
+  *maxTasks = b->maxTasks;
+  *solves = b->solves;
+}
+esf_status pressure_work_set_batcher(PressureWork* w, InnerBatcher* b) {
+  if (!w) return ESF_ERR_STATE;
+  if (b && !w->batchReady) {
+    ESF_CUDA(cudaEventCreateWithFlags(&w->batchReady, cudaEventDisableTiming));
+    ESF_CUDA(cudaEventCreateWithFlags(&w->batchDone, cudaEventDisableTiming));
+  }
+  const std::array<int, 3> shape = {w->g.cX, w->g.cY, w->g.cZ};
+  if (w->batcher) {
+    std::lock_guard<std::mutex> g(w->batcher->m);
+    w->batcher->attached[shape]--;
+  }
+  w->batcher = b;
+  if (b) {
+    std::lock_guard<std::mutex> g(b->m);
+    b->attached[shape]++;
+  }
+  return ESF_OK;
+}
+// Whether a scene's inner solves go through its batcher: only while another
+// work of the same grid shape is attached (a launch lasts as long as its
+// slowest task, and a task alone in its lane gains nothing over the scene's
+// own captured graphs).
+static bool batching_pays(PressureWork* w) {
+  if (!w->batcher) return false;
+  std::lock_guard<std::mutex> g(w->batcher->m);
+  auto it = w->batcher->attached.find({w->g.cX, w->g.cY, w->g.cZ});
+  return it != w->batcher->attached.end() && it->second >= 2;
+}
+
+// One inner solve of a scene through the batcher: the set-up pass has been
+// queued on the scene's stream; the task joins the batch behind it, and the
+// scene's stream resumes behind the batch stream's work once it is done.
+static esf_status batched_inner_solve(PressureWork* w, const GridDev& g, cudaStream_t st, PcrState* out) {
+  InnerBatcher::Job j;
+  const FusedKernels kf = fused_kernels(w, g, w->st32);
+  j.task.tm = w->fmaps;
+  j.task.g = g;
+  j.task.p = kf.p;
+  j.task.partial = w->partial;
+  j.task.st = w->st32;
+  j.task.cz = fused_cz(g);
+  const dim3 gr = tma_grid(g, j.task.cz);
+  j.task.gx = (int)gr.x;
+  j.task.gy = (int)gr.y;
+  j.task.gz = (int)gr.z;
+  j.ready = w->batchReady;
+  j.done = w->batchDone;
+  ESF_CUDA(cudaEventRecord(j.ready, st));
+  {
+    esf_status e = w->batcher->solve(&j);
+    if (e) return e;
+  }
+  ESF_CUDA(cudaStreamWaitEvent(st, j.done, 0));
+  *out = j.out;
+  return ESF_OK;
 }
 
 // ------------------------------------------------- bounded-wait self-test

@@ -13,6 +13,7 @@
 #include <cub/device/device_scan.cuh>
 #include <chrono>
 #include <mutex>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -1443,6 +1444,84 @@ extern "C" esf_status esf_pressure_solve(const esf_grid* g, const double* minv, 
   pressure_work_free(w);
   if (iters) *iters = it;
   if (relres) *relres = rr;
+  return e;
+}
+
+namespace esf {
+// Serving: hand this scene's mixed inner solves to a batcher shared with
+// other scenes (nullptr: solve them on the scene's own stream).
+esf_status scene_set_batcher(esf_scene* s, InnerBatcher* b) {
+  if (!s || !s->pw) return ESF_ERR_STATE;
+  return pressure_work_set_batcher(s->pw, b);
+}
+}  // namespace esf
+
+extern "C" esf_status esf_pressure_solve_batch(int n, const esf_grid* grids, const double* const* minv,
+                                               const double* const* diag, const double* const* b,
+                                               double* const* x, double eps, int maxIt, int precision,
+                                               int* iters, double* relres, void* stream) {
+  if (n < 1 || !grids || !minv || !diag || !b || !x || maxIt < 0 ||
+      (precision != ESF_FP64 && precision != ESF_MIXED)) {
+    set_error("esf_pressure_solve_batch: invalid argument");
+    return ESF_ERR_INVALID_ARG;
+  }
+  for (int i = 0; i < n; i++)
+    if (!minv[i] || !diag[i] || !b[i] || !x[i] || grids[i].xRes < 3 || grids[i].yRes < 3 ||
+        grids[i].zRes < 3) {
+      set_error("esf_pressure_solve_batch: invalid system %d", i);
+      return ESF_ERR_INVALID_ARG;
+    }
+  int dev = 0;
+  ESF_CUDA(cudaGetDevice(&dev));
+  InnerBatcher* batcher = nullptr;
+  if (precision == ESF_MIXED) TRY(batcher_create(dev, &batcher));
+  cudaEvent_t start = nullptr;
+  ESF_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+  ESF_CUDA(cudaEventRecord(start, (cudaStream_t)stream));
+  std::vector<esf_status> st(n, ESF_OK);
+  std::vector<int> it(n, 0);
+  std::vector<double> rr(n, 0.0);
+  // every system's work is attached before any solve starts, so systems of
+  // one grid shape find each other in the batcher from their first inner solve
+  std::vector<PressureWork*> works(n, nullptr);
+  std::vector<cudaStream_t> streams(n, nullptr);
+  esf_status e = ESF_OK;
+  for (int i = 0; i < n && !e; i++) {
+    if (cudaStreamCreateWithFlags(&streams[i], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamWaitEvent(streams[i], start, 0) != cudaSuccess) {
+      set_error("esf_pressure_solve_batch: %s", cudaGetErrorString(cudaGetLastError()));
+      e = ESF_ERR_CUDA;
+      break;
+    }
+    e = pressure_work_alloc(&works[i], grid_dev(&grids[i]), precision == ESF_MIXED);
+    if (!e && batcher) e = pressure_work_set_batcher(works[i], batcher);
+  }
+  if (!e) {
+    // one host thread per system drives its FP64 refinement loop on its own
+    // stream; the inner iterations of systems of one grid shape share the
+    // batcher's launches
+    std::vector<std::thread> threads;
+    for (int i = 0; i < n; i++)
+      threads.emplace_back([&, i] {
+        cudaSetDevice(dev);
+        int rf = 0, cv = 0;
+        st[i] = pressure_solve(works[i], grid_dev(&grids[i]), minv[i], diag[i], b[i], x[i], eps, maxIt,
+                               precision, 1e-4, 50, &it[i], &rr[i], &rf, &cv, streams[i]);
+        cudaStreamSynchronize(streams[i]);
+      });
+    for (auto& t : threads) t.join();
+  }
+  for (int i = 0; i < n; i++) {
+    pressure_work_free(works[i]);
+    if (streams[i]) cudaStreamDestroy(streams[i]);
+  }
+  batcher_destroy(batcher);
+  cudaEventDestroy(start);
+  for (int i = 0; i < n; i++) {
+    if (iters) iters[i] = it[i];
+    if (relres) relres[i] = rr[i];
+    if (st[i] && !e) e = st[i];
+  }
   return e;
 }
 

@@ -20,7 +20,12 @@ ESF_REQ_QUEUED, ESF_REQ_RUNNING, ESF_REQ_DONE, ESF_REQ_FAILED = 0, 1, 2, 3
 
 
 class ServerConfig(C.Structure):
-    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_active", C.c_int)]
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_active", C.c_int), ("no_batching", C.c_int)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("launches", C.c_longlong), ("task_launches", C.c_longlong),
+                ("max_tasks", C.c_longlong), ("inner_solves", C.c_longlong)]
 
 
 class Request(C.Structure):
@@ -54,6 +59,7 @@ def declare(lib: C.CDLL) -> None:
     lib.esf_server_get_field.argtypes = [vp, u64, C.c_int, C.c_int, vp, C.c_size_t]
     lib.esf_server_release.argtypes = [vp, u64]
     lib.esf_server_destroy.argtypes = [vp]
+    lib.esf_server_batch_stats.argtypes = [vp, C.POINTER(BatchStats)]
 
 
 def request_for(desc, steps: int, precision: int = abi.ESF_MIXED):
@@ -84,10 +90,10 @@ def request_for(desc, steps: int, precision: int = abi.ESF_MIXED):
 
 
 class Server:
-    def __init__(self, hbm_budget_bytes: int = 0, max_active: int = 0, lib=None):
+    def __init__(self, hbm_budget_bytes: int = 0, max_active: int = 0, lib=None, batching: bool = True):
         from . import load
         self._lib = lib or load()
-        cfg = ServerConfig(hbm_budget_bytes, max_active)
+        cfg = ServerConfig(hbm_budget_bytes, max_active, 0 if batching else 1)
         h = C.c_void_p()
         st = self._lib.esf_server_create(C.byref(cfg), C.byref(h))
         if st != 0:
@@ -135,6 +141,16 @@ class Server:
         st = self._lib.esf_server_release(self._h, ticket)
         if st != 0:
             raise abi.EsfError(st, "esf_server_release", self._err())
+
+    def batch_stats(self) -> dict:
+        """Counters of the continuous batching of inner solves (esf_server_batch_stats)."""
+        b = BatchStats()
+        st = self._lib.esf_server_batch_stats(self._h, C.byref(b))
+        if st != 0:
+            raise abi.EsfError(st, "esf_server_batch_stats", self._err())
+        return {"launches": b.launches, "task_launches": b.task_launches, "max_tasks": b.max_tasks,
+                "inner_solves": b.inner_solves,
+                "mean_tasks": (b.task_launches / b.launches) if b.launches else 0.0}
 
     def close(self):
         if getattr(self, "_h", None):

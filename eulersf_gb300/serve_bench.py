@@ -9,9 +9,12 @@ mixed precision to the 1e-8 FP64 residual.
 
     python -m eulersf_gb300.serve_bench [--requests 60] [--rate 40] [--steps 10]
                                         [--seed 11] [--max-active 8] [--no-sequential]
+                                        [--no-batching]
 
 Prints one JSON line: scene-steps/s served and sequential, the ratio, and
-the p50/p99 request latency (submit to last step).
+the p50/p99 request latency (submit to last step). The served run batches
+the inner solves of active scenes of one grid shape (continuous batching,
+unless --no-batching); the sequential run steps one scene at a time.
 """
 from __future__ import annotations
 
@@ -39,12 +42,12 @@ def make_requests(n, seed, sizes):
     return out
 
 
-def serve(descs, steps, rate, seed, max_active):
+def serve(descs, steps, rate, seed, max_active, batching=True):
     from .serve import Server
     rng = np.random.default_rng(seed + 1)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, len(descs))) if rate > 0 else np.zeros(len(descs))
     stats = []
-    with Server(max_active=max_active) as srv:
+    with Server(max_active=max_active, batching=batching) as srv:
         t0 = time.perf_counter()
         tickets = []
         for d, at in zip(descs, arrivals):
@@ -59,7 +62,8 @@ def serve(descs, steps, rate, seed, max_active):
             stats.append(st)
             srv.release(t)
         wall = time.perf_counter() - t0
-    return wall, stats
+        batch = srv.batch_stats()
+    return wall, stats, batch
 
 
 def main(argv=None):
@@ -71,9 +75,11 @@ def main(argv=None):
     ap.add_argument("--sizes", default="48,64,96,128,160")
     ap.add_argument("--max-active", type=int, default=8)
     ap.add_argument("--no-sequential", action="store_true")
+    ap.add_argument("--no-batching", action="store_true",
+                    help="each scene's inner solves on its own stream (no shared launches)")
     a = ap.parse_args(argv)
     descs = make_requests(a.requests, a.seed, [int(x) for x in a.sizes.split(",")])
-    wall, stats = serve(descs, a.steps, a.rate, a.seed, a.max_active)
+    wall, stats, batch = serve(descs, a.steps, a.rate, a.seed, a.max_active, not a.no_batching)
     lat = np.array([s["latency_ms"] for s in stats])
     steps_all = a.steps * len(descs)
     line = {"metric": "served scene-steps/s (Poisson arrivals)", "requests": len(descs),
@@ -81,9 +87,10 @@ def main(argv=None):
             "sizes": a.sizes, "served_steps_per_s": steps_all / wall, "served_wall_s": wall,
             "latency_p50_ms": float(np.percentile(lat, 50)), "latency_p99_ms": float(np.percentile(lat, 99)),
             "queued_p50_ms": float(np.percentile([s["queued_ms"] for s in stats], 50)),
-            "max_rel_residual": max(max(s["last"]["rel_residual"]) for s in stats)}
+            "max_rel_residual": max(max(s["last"]["rel_residual"]) for s in stats),
+            "batching": not a.no_batching, "batch_stats": batch}
     if not a.no_sequential:
-        swall, sstats = serve(descs, a.steps, 0.0, a.seed, 1)
+        swall, sstats, _ = serve(descs, a.steps, 0.0, a.seed, 1, False)
         line["sequential_steps_per_s"] = steps_all / swall
         line["sequential_wall_s"] = swall
         line["served_over_sequential"] = line["served_steps_per_s"] / line["sequential_steps_per_s"]

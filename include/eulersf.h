@@ -239,6 +239,21 @@ esf_status esf_pressure_solve(const esf_grid* grid, const double* mass_inv_node,
                               double eps, int max_iterations, int precision,
                               int* iterations, double* rel_residual, void* stream);
 
+/* Batched solver seam: n independent pressure systems solved together, each
+ * with its own grid, m^-1, diagonal, right-hand side and warm start (arrays of
+ * n device pointers; iterations and rel_residual NULL or arrays of n). No
+ * reference counterpart: the reference solves one system per process
+ * (solvePCR). At ESF_MIXED the FP32 inner iterations of systems of the same
+ * grid shape advance in shared launches (continuous batching, as the server
+ * does); each system's FP64 refinement runs on its own stream, driven by its
+ * own host thread. Every system gets the same answer, iterations and bits as
+ * esf_pressure_solve alone. Work waits for what is queued on `stream` before
+ * the call; the call returns when every solve has finished. */
+esf_status esf_pressure_solve_batch(int n, const esf_grid* grids, const double* const* mass_inv_node,
+                                    const double* const* diag, const double* const* b,
+                                    double* const* x, double eps, int max_iterations, int precision,
+                                    int* iterations, double* rel_residual, void* stream);
+
 /* Allocation-free variant of esf_pressure_solve at ESF_FP64. It has no
  * counterpart in the reference. It is for callers that must not allocate or
  * free device memory while they solve: a host whose HBM is reserved up front
@@ -289,6 +304,7 @@ typedef struct esf_server esf_server;
 typedef struct esf_server_config {
   size_t hbm_budget_bytes; /* admission budget; 0: 85% of the device's free memory */
   int max_active;          /* scenes stepping at once; 0: 8 */
+  int no_batching;         /* 1: each scene runs its inner solves alone on its own stream */
 } esf_server_config;
 typedef struct esf_request {
   esf_grid grid;
@@ -329,6 +345,21 @@ esf_status esf_server_wait(esf_server* server, uint64_t ticket, esf_request_stat
 esf_status esf_server_get_field(esf_server* server, uint64_t ticket, esf_field field, int solid,
                                 void* host, size_t bytes);
 esf_status esf_server_release(esf_server* server, uint64_t ticket);
+/* Continuous batching of the inner solves: the mixed-precision pressure
+ * solves of the scenes the server is stepping hand their FP32 inner
+ * iterations to one batcher. Scenes of the same grid shape advance their
+ * pending inner solves in the same launches (chunks of five iterations of
+ * each task), joining and leaving between chunks; each shape has its own
+ * lane, and lanes run side by side. A scene whose shape no other active scene
+ * shares keeps solving on its own stream. Counters since the server was
+ * created. */
+typedef struct esf_batch_stats {
+  long long launches;        /* launches of the batched iteration kernel */
+  long long task_launches;   /* sum over those launches of the tasks they carried */
+  long long max_tasks;       /* most tasks in one launch */
+  long long inner_solves;    /* inner solves finished through the batcher */
+} esf_batch_stats;
+esf_status esf_server_batch_stats(esf_server* server, esf_batch_stats* stats);
 /* lets running requests finish their steps, drops queued ones */
 esf_status esf_server_destroy(esf_server* server);
 

@@ -1,7 +1,8 @@
 """The multi-scene server (esf_server_*): each request's result is the same,
-bit for bit, whether it runs alone or concurrently with others; admission
-holds a request back until the memory budget has room; a request larger
-than the budget is refused."""
+bit for bit, whether it runs alone or concurrently with others, with its
+inner solves batched with the other scenes' of its grid shape (continuous
+batching) or run on its own stream; admission holds a request back until the
+memory budget has room; a request larger than the budget is refused."""
 import ctypes as C
 
 import numpy as np
@@ -32,6 +33,9 @@ def test_concurrent_requests_equal_solo_runs(gpu_lib):
             got.append((srv.get(t, "velocity", d.res ** 3 * 3), srv.get(t, "lambda1", d.N ** 3),
                          st["last"]["iterations"]))
             srv.release(t)
+        stats = srv.batch_stats()
+    # the two 16^3 scenes' inner solves went through the batcher
+    assert stats["inner_solves"] > 0 and stats["launches"] > 0, stats
     for d, (vel, lam, its) in zip(descs, got):
         G = E.make_scene(d, precision=abi.ESF_MIXED)
         for _ in range(steps):
@@ -60,3 +64,26 @@ def test_admission_waits_for_budget_and_refuses_oversize(gpu_lib):
         with pytest.raises(abi.EsfError) as e:
             srv.submit(SceneDesc(N=64), 1)
         assert e.value.status == 4  # ESF_ERR_OOM
+
+
+def test_batched_and_unbatched_serving_agree(gpu_lib):
+    """The same requests through a server without batching (each scene's
+    inner solves on its own stream): the same bits as batched."""
+    from eulersf_gb300.serve import Server
+    descs, steps = _descs(), 2
+    out = {}
+    for batching in (True, False):
+        with Server(max_active=3, batching=batching) as srv:
+            tickets = [srv.submit(d, steps, abi.ESF_MIXED) for d in descs]
+            res = []
+            for d, t in zip(descs, tickets):
+                st = srv.wait(t)
+                assert st["state"] == 2, st
+                res.append((srv.get(t, "velocity", d.res ** 3 * 3), st["last"]["iterations"]))
+                srv.release(t)
+            if not batching:
+                assert srv.batch_stats()["launches"] == 0
+        out[batching] = res
+    for (va, ia), (vb, ib) in zip(out[True], out[False]):
+        assert ia == ib
+        assert np.array_equal(va, vb)

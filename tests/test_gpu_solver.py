@@ -192,3 +192,38 @@ def test_one_pass_iteration_matches_two_kernel_split(shape, gpu_lib, monkeypatch
     assert abs(it1 - it2) <= 0.1 * it2 + 10, (it1, it2)
     assert rel_err(out["fused"][1], out["tma"][1]) <= 1e-3
 
+
+
+def test_batched_solve_equals_single_solves(gpu_lib):
+    """esf_pressure_solve_batch on systems of two grid shapes (24^3 and 32^3
+    cells, mixed precision; systems of one shape share launches): each
+    answer, iteration count and residual is the same as esf_pressure_solve's
+    on that system alone, bit for bit."""
+    import torch
+    systems = []
+    for X, seed in ((25, 1), (33, 2), (25, 3), (33, 4), (25, 5)):
+        rng = np.random.default_rng(seed)
+        g = oracle.grid(X, 1.0 / (X - 1))
+        minv = rng.uniform(50.0, 300.0, X ** 3)
+        b = oracle.pressure_apply(g, minv, rng.standard_normal((X - 1) ** 3))
+        systems.append((g, minv, _jacobi_diag(X, X, X, minv), b, 0.1 * rng.standard_normal(len(b))))
+    n = len(systems)
+    dm = [_dev(s[1]) for s in systems]
+    dd = [_dev(s[2]) for s in systems]
+    db = [_dev(s[3]) for s in systems]
+    dx = [_dev(s[4]) for s in systems]
+    grids = (type(systems[0][0]) * n)(*[s[0] for s in systems])
+    arr = lambda ts: (C.c_void_p * n)(*[t.data_ptr() for t in ts])
+    its, rr = (C.c_int * n)(), (C.c_double * n)()
+    st = gpu_lib.esf_pressure_solve_batch(n, grids, arr(dm), arr(dd), arr(db), arr(dx), 1e-8, 20000, 1,
+                                          its, rr, None)
+    torch.cuda.synchronize()
+    assert st == 0, gpu_lib.esf_last_error()
+    for i, (g, minv, diag, b, x0) in enumerate(systems):
+        sx = _dev(x0)
+        it, r1 = C.c_int(), C.c_double()
+        assert gpu_lib.esf_pressure_solve(C.byref(g), _ptr(dm[i]), _ptr(dd[i]), _ptr(db[i]), _ptr(sx), 1e-8,
+                                          20000, 1, C.byref(it), C.byref(r1), None) == 0
+        torch.cuda.synchronize()
+        assert its[i] == it.value and rr[i] == r1.value and rr[i] < 1e-8
+        assert torch.equal(dx[i], sx), i
