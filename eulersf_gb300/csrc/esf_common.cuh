@@ -178,8 +178,7 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
 struct InnerBatcher;
 esf_status batcher_create(int device, InnerBatcher** out);
 void batcher_destroy(InnerBatcher* b);
-void batcher_stats(InnerBatcher* b, long long* launches, long long* taskLaunches, long long* maxTasks,
-                   long long* solves);
+void batcher_stats(InnerBatcher* b, esf_batch_stats* out);
 esf_status pressure_work_set_batcher(PressureWork* w, InnerBatcher* b);
 // self-test of the TMA kernels' bounded mbarrier wait (esf_solver.cu)
 esf_status selftest_mbar_wait(int* gaveUp, cudaStream_t st);

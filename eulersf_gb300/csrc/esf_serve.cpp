@@ -29,8 +29,7 @@ void set_error(const char* fmt, ...);
 struct InnerBatcher;
 esf_status batcher_create(int device, InnerBatcher** out);
 void batcher_destroy(InnerBatcher* b);
-void batcher_stats(InnerBatcher* b, long long* launches, long long* taskLaunches, long long* maxTasks,
-                   long long* solves);
+void batcher_stats(InnerBatcher* b, esf_batch_stats* out);
 esf_status scene_set_batcher(esf_scene* s, InnerBatcher* b);
 }
 
@@ -376,8 +375,6 @@ extern "C" esf_status esf_server_destroy(esf_server* s) {
 extern "C" esf_status esf_server_batch_stats(esf_server* s, esf_batch_stats* out) {
   if (!s || !out) return ESF_ERR_INVALID_ARG;
   memset(out, 0, sizeof *out);
-  if (s->batcher)
-    esf::batcher_stats(s->batcher, &out->launches, &out->task_launches, &out->max_tasks,
-                       &out->inner_solves);
+  if (s->batcher) esf::batcher_stats(s->batcher, out);
   return ESF_OK;
 }

@@ -1765,10 +1765,13 @@ struct InnerBatcher {
     int ring;
     unsigned long long order;  // launch order across lanes
     std::vector<Entry> jobs;   // the chunk's tasks in list order
+    bool timed;                // its launches are bracketed by the lane's timing events
+    long long rows;            // pressure rows of its tasks
   };
   struct Lane {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[kRing] = {};
+    cudaEvent_t t0 = nullptr, t1 = nullptr;  // device time of every 8th chunk's launches
     PcrState* dStates = nullptr;  // [kRing][kSlots]
     PcrState* hStates = nullptr;  // pinned copies
     std::vector<Job*> active;
@@ -1792,6 +1795,8 @@ struct InnerBatcher {
   bool stop = false;
   std::thread thr;
   long long launches = 0, taskLaunches = 0, maxTasks = 0, solves = 0;
+  long long timedLaunches = 0, timedRows = 0;
+  double timedMs = 0;
   unsigned long long nextSeq = 1, nextOrder = 0;
 
   static Shape shape_of(const FusedTask& t) { return {t.g.cX, t.g.cY, t.g.cZ, t.cz}; }
@@ -1814,6 +1819,8 @@ struct InnerBatcher {
   esf_status lane_init(Lane& L) {
     ESF_CUDA(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
     for (int i = 0; i < kRing; i++) ESF_CUDA(cudaEventCreateWithFlags(&L.ev[i], cudaEventDisableTiming));
+    ESF_CUDA(cudaEventCreate(&L.t0));
+    ESF_CUDA(cudaEventCreate(&L.t1));
     ESF_CUDA(cudaMalloc(&L.dStates, sizeof(PcrState) * kSlots * kRing));
     ESF_CUDA(cudaMallocHost(&L.hStates, sizeof(PcrState) * kSlots * kRing));
     return ESF_OK;
@@ -1831,6 +1838,8 @@ struct InnerBatcher {
       if (L.stream) cudaStreamSynchronize(L.stream);
       for (int i = 0; i < kRing; i++)
         if (L.ev[i]) cudaEventDestroy(L.ev[i]);
+      if (L.t0) cudaEventDestroy(L.t0);
+      if (L.t1) cudaEventDestroy(L.t1);
       cudaFree(L.dStates);
       if (L.hStates) cudaFreeHost(L.hStates);
       if (L.stream) cudaStreamDestroy(L.stream);
@@ -1861,6 +1870,14 @@ struct InnerBatcher {
     cudaEventSynchronize(L.ev[c.ring]);
     bool any = false;
     std::lock_guard<std::mutex> g(m);
+    if (c.timed) {
+      float ms = 0;
+      if (cudaEventElapsedTime(&ms, L.t0, L.t1) == cudaSuccess) {
+        timedMs += ms;
+        timedLaunches += kChunk;
+        timedRows += (long long)kChunk * c.rows;
+      }
+    }
     for (size_t i = 0; i < c.jobs.size(); i++) {
       slotRefs[c.jobs[i].slot]--;
       const PcrState& h = L.hStates[c.ring * kSlots + i];
@@ -1885,6 +1902,7 @@ struct InnerBatcher {
     std::vector<Entry> ids;
     FusedBatch b;
     int blocks = 0;
+    long long rows = 0;
     {
       std::lock_guard<std::mutex> g(m);
       b.n = (int)L.active.size();
@@ -1893,15 +1911,22 @@ struct InnerBatcher {
         b.slot[k] = L.active[k]->slot;
         b.first[k] = blocks;
         blocks += t.gx * t.gy * t.gz;
+        rows += t.g.R;
         ids.push_back(Entry{L.active[k], L.active[k]->seq, L.active[k]->slot});
         slotRefs[L.active[k]->slot]++;
       }
     }
     b.first[b.n] = blocks;
     const int ring = (int)(L.chunks % kRing);
+    // the timing events are reused: only a chunk whose predecessor with
+    // timing has been settled is timed (one timed chunk in flight per lane)
+    bool timed = (L.chunks % 8) == 0;
+    for (const Chunk& c : L.inflight) timed = timed && !c.timed;
+    if (timed) cudaEventRecord(L.t0, L.stream);
     for (int k = 0; k < kChunk; k++) {
       ESF_COUNTED pcr_iteration_fused_batch<<<blocks, NT, FU_SMEM, L.stream>>>(dTasks, b);
     }
+    if (timed) cudaEventRecord(L.t1, L.stream);
     ESF_COUNTED gather_task_states<<<1, 64, 0, L.stream>>>(dTasks, b, L.dStates + ring * kSlots);
     cudaMemcpyAsync(L.hStates + ring * kSlots, L.dStates + ring * kSlots, sizeof(PcrState) * b.n,
                     cudaMemcpyDeviceToHost, L.stream);
@@ -1910,7 +1935,7 @@ struct InnerBatcher {
     launches += kChunk;
     taskLaunches += (long long)kChunk * b.n;
     if (b.n > maxTasks) maxTasks = b.n;
-    L.inflight.push_back(Chunk{ring, nextOrder++, std::move(ids)});
+    L.inflight.push_back(Chunk{ring, nextOrder++, std::move(ids), timed, rows});
   }
   void loop() {
     cudaSetDevice(device);
@@ -1997,13 +2022,15 @@ void batcher_destroy(InnerBatcher* b) {
   b->shutdown();
   delete b;
 }
-void batcher_stats(InnerBatcher* b, long long* launches, long long* taskLaunches, long long* maxTasks,
-                   long long* solves) {
+void batcher_stats(InnerBatcher* b, esf_batch_stats* out) {
   std::lock_guard<std::mutex> g(b->m);
-  *launches = b->launches;
-  *taskLaunches = b->taskLaunches;
-  *maxTasks = b->maxTasks;
-  *solves = b->solves;
+  out->launches = b->launches;
+  out->task_launches = b->taskLaunches;
+  out->max_tasks = b->maxTasks;
+  out->inner_solves = b->solves;
+  out->timed_launches = b->timedLaunches;
+  out->timed_rows = b->timedRows;
+  out->timed_ms = b->timedMs;
 }
 esf_status pressure_work_set_batcher(PressureWork* w, InnerBatcher* b) {
   if (!w) return ESF_ERR_STATE;

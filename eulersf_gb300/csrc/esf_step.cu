@@ -1459,7 +1459,8 @@ esf_status scene_set_batcher(esf_scene* s, InnerBatcher* b) {
 extern "C" esf_status esf_pressure_solve_batch(int n, const esf_grid* grids, const double* const* minv,
                                                const double* const* diag, const double* const* b,
                                                double* const* x, double eps, int maxIt, int precision,
-                                               int* iters, double* relres, void* stream) {
+                                               int* iters, double* relres, esf_batch_stats* stats,
+                                               void* stream) {
   if (n < 1 || !grids || !minv || !diag || !b || !x || maxIt < 0 ||
       (precision != ESF_FP64 && precision != ESF_MIXED)) {
     set_error("esf_pressure_solve_batch: invalid argument");
@@ -1514,6 +1515,10 @@ extern "C" esf_status esf_pressure_solve_batch(int n, const esf_grid* grids, con
   for (int i = 0; i < n; i++) {
     pressure_work_free(works[i]);
     if (streams[i]) cudaStreamDestroy(streams[i]);
+  }
+  if (stats) {
+    memset(stats, 0, sizeof *stats);
+    if (batcher) batcher_stats(batcher, stats);
   }
   batcher_destroy(batcher);
   cudaEventDestroy(start);

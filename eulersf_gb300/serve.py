@@ -25,7 +25,18 @@ class ServerConfig(C.Structure):
 
 class BatchStats(C.Structure):
     _fields_ = [("launches", C.c_longlong), ("task_launches", C.c_longlong),
-                ("max_tasks", C.c_longlong), ("inner_solves", C.c_longlong)]
+                ("max_tasks", C.c_longlong), ("inner_solves", C.c_longlong),
+                ("timed_launches", C.c_longlong), ("timed_rows", C.c_longlong),
+                ("timed_ms", C.c_double)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["mean_tasks"] = (self.task_launches / self.launches) if self.launches else 0.0
+        # device time of one batched launch, and the one-pass iteration's 48
+        # bytes a row it stands for, over the timed launches
+        d["launch_ms"] = (self.timed_ms / self.timed_launches) if self.timed_launches else None
+        d["launch_gbs"] = (48.0 * self.timed_rows / (self.timed_ms * 1e-3) / 1e9) if self.timed_ms else None
+        return d
 
 
 class Request(C.Structure):
@@ -148,9 +159,7 @@ class Server:
         st = self._lib.esf_server_batch_stats(self._h, C.byref(b))
         if st != 0:
             raise abi.EsfError(st, "esf_server_batch_stats", self._err())
-        return {"launches": b.launches, "task_launches": b.task_launches, "max_tasks": b.max_tasks,
-                "inner_solves": b.inner_solves,
-                "mean_tasks": (b.task_launches / b.launches) if b.launches else 0.0}
+        return b.as_dict()
 
     def close(self):
         if getattr(self, "_h", None):

@@ -87,6 +87,8 @@ def run_batch(size=32, batch=256, iters=300, repeat=2):
     arr = lambda ts: (C.c_void_p * batch)(*[t.data_ptr() for t in ts])
     its = (C.c_int * batch)()
     rr = (C.c_double * batch)()
+    from .serve import BatchStats
+    stats = BatchStats()
 
     def solve(n):
         for x in dx:
@@ -94,7 +96,7 @@ def run_batch(size=32, batch=256, iters=300, repeat=2):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         s = lib.esf_pressure_solve_batch(batch, grids, arr(dm), arr(dd), arr(db), arr(dx), 1e-30, n,
-                                         abi.ESF_MIXED, its, rr, None)
+                                         abi.ESF_MIXED, its, rr, C.byref(stats), None)
         t = time.perf_counter() - t0
         if s != 0:
             raise abi.EsfError(s, "esf_pressure_solve_batch", (lib.esf_last_error() or b"").decode())
@@ -109,6 +111,7 @@ def run_batch(size=32, batch=256, iters=300, repeat=2):
     n, t = best
     n4, t4 = solve(4 * iters)
     marginal = (n4 - n) / (t4 - t) if t4 > t else None
+    kernel = stats.as_dict()
     R = desc.N ** 3
     peak = None
     p = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "MEASURED_PEAKS.json")
@@ -123,9 +126,13 @@ def run_batch(size=32, batch=256, iters=300, repeat=2):
             "frac_of_hbm": (gbs / peak) if peak else None,
             "marginal_iters_per_s": marginal, "marginal_gbs": mgbs,
             "marginal_frac_of_hbm": (mgbs / peak) if (peak and mgbs) else None,
+            "launch_ms": kernel["launch_ms"], "launch_gbs": kernel["launch_gbs"],
+            "launch_frac_of_hbm": (kernel["launch_gbs"] / peak) if (peak and kernel["launch_gbs"]) else None,
+            "tasks_per_launch": kernel["mean_tasks"],
             "what": "wall clock around one esf_pressure_solve_batch call (host threads, work arrays, "
                     "refinements and set-up passes included); bandwidth = iterations x 48 bytes x rows / "
-                    "wall; marginal_* from a 4x longer call (per-call set-up left out)"}
+                    "wall; marginal_* from a 4x longer call (per-call set-up left out); launch_* from "
+                    "CUDA events around every 8th chunk of batched launches (48 bytes x rows / device time)"}
 
 
 def main(argv=None):

@@ -247,12 +247,15 @@ esf_status esf_pressure_solve(const esf_grid* grid, const double* mass_inv_node,
  * grid shape advance in shared launches (continuous batching, as the server
  * does); each system's FP64 refinement runs on its own stream, driven by its
  * own host thread. Every system gets the same answer, iterations and bits as
- * esf_pressure_solve alone. Work waits for what is queued on `stream` before
- * the call; the call returns when every solve has finished. */
+ * esf_pressure_solve alone. `stats` (may be NULL) receives the batcher's
+ * counters (esf_batch_stats, below). Work waits for what is queued on
+ * `stream` before the call; the call returns when every solve has finished. */
+struct esf_batch_stats;
 esf_status esf_pressure_solve_batch(int n, const esf_grid* grids, const double* const* mass_inv_node,
                                     const double* const* diag, const double* const* b,
                                     double* const* x, double eps, int max_iterations, int precision,
-                                    int* iterations, double* rel_residual, void* stream);
+                                    int* iterations, double* rel_residual,
+                                    struct esf_batch_stats* stats, void* stream);
 
 /* Allocation-free variant of esf_pressure_solve at ESF_FP64. It has no
  * counterpart in the reference. It is for callers that must not allocate or
@@ -353,12 +356,16 @@ esf_status esf_server_release(esf_server* server, uint64_t ticket);
  * lane, and lanes run side by side. A scene whose shape no other active scene
  * shares keeps solving on its own stream. Counters since the server was
  * created. */
-typedef struct esf_batch_stats {
+struct esf_batch_stats {
   long long launches;        /* launches of the batched iteration kernel */
   long long task_launches;   /* sum over those launches of the tasks they carried */
   long long max_tasks;       /* most tasks in one launch */
   long long inner_solves;    /* inner solves finished through the batcher */
-} esf_batch_stats;
+  long long timed_launches;  /* launches timed with CUDA events (every 8th chunk of a lane) */
+  long long timed_rows;      /* pressure rows those launches advanced by one iteration */
+  double timed_ms;           /* their device time */
+};
+typedef struct esf_batch_stats esf_batch_stats;
 esf_status esf_server_batch_stats(esf_server* server, esf_batch_stats* stats);
 /* lets running requests finish their steps, drops queued ones */
 esf_status esf_server_destroy(esf_server* server);

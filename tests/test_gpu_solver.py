@@ -215,10 +215,14 @@ def test_batched_solve_equals_single_solves(gpu_lib):
     grids = (type(systems[0][0]) * n)(*[s[0] for s in systems])
     arr = lambda ts: (C.c_void_p * n)(*[t.data_ptr() for t in ts])
     its, rr = (C.c_int * n)(), (C.c_double * n)()
+    from eulersf_gb300.serve import BatchStats
+    stats = BatchStats()
     st = gpu_lib.esf_pressure_solve_batch(n, grids, arr(dm), arr(dd), arr(db), arr(dx), 1e-8, 20000, 1,
-                                          its, rr, None)
+                                          its, rr, C.byref(stats), None)
     torch.cuda.synchronize()
     assert st == 0, gpu_lib.esf_last_error()
+    # both shapes have several systems: their inner solves shared launches
+    assert stats.inner_solves > 0 and stats.max_tasks >= 2, stats.as_dict()
     for i, (g, minv, diag, b, x0) in enumerate(systems):
         sx = _dev(x0)
         it, r1 = C.c_int(), C.c_double()
