@@ -52,7 +52,7 @@ def load(build_if_missing: bool = False) -> C.CDLL:
                                        C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), vp]
     lib.esf_pressure_solve_batch.argtypes = [C.c_int, C.POINTER(abi.Grid), C.POINTER(vp), C.POINTER(vp),
                                              C.POINTER(vp), C.POINTER(vp), C.c_double, C.c_int, C.c_int,
-                                             C.POINTER(C.c_int), C.POINTER(C.c_double), vp, vp]
+                                             C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), vp, vp]
     lib.esf_pressure_solve_static.argtypes = [C.POINTER(abi.Grid), vp, vp, vp, vp, C.c_double,
                                               C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                               vp]

@@ -176,7 +176,7 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
 // batched solves): scenes whose pressure work is attached to a batcher hand
 // their inner solves over to its thread and streams (esf_solver.cu)
 struct InnerBatcher;
-esf_status batcher_create(int device, InnerBatcher** out);
+esf_status batcher_create(int device, InnerBatcher** out, bool autotune);
 void batcher_destroy(InnerBatcher* b);
 void batcher_stats(InnerBatcher* b, esf_batch_stats* out);
 esf_status pressure_work_set_batcher(PressureWork* w, InnerBatcher* b);

@@ -27,7 +27,7 @@
 namespace esf {
 void set_error(const char* fmt, ...);
 struct InnerBatcher;
-esf_status batcher_create(int device, InnerBatcher** out);
+esf_status batcher_create(int device, InnerBatcher** out, bool autotune);
 void batcher_destroy(InnerBatcher* b);
 void batcher_stats(InnerBatcher* b, esf_batch_stats* out);
 esf_status scene_set_batcher(esf_scene* s, InnerBatcher* b);
@@ -225,7 +225,7 @@ extern "C" esf_status esf_server_create(const esf_server_config* cfg, esf_server
   s->budget = (cfg && cfg->hbm_budget_bytes) ? cfg->hbm_budget_bytes : (size_t)(0.85 * (double)freeB);
   s->maxActive = (cfg && cfg->max_active > 0) ? cfg->max_active : 8;
   if (!(cfg && cfg->no_batching)) {
-    esf_status e = esf::batcher_create(s->device, &s->batcher);
+    esf_status e = esf::batcher_create(s->device, &s->batcher, cfg && cfg->autotune);
     if (e) {
       delete s;
       return e;

@@ -1746,6 +1746,16 @@ esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const in
 // shape share launches: each shape has its own lane (stream, tasks, chunks in
 // flight), and lanes of different shapes run side by side on the device.
 // Up to three chunks are in flight per lane.
+// Tile autotuner (opt-in): the depth cz of a block's z-march is the one knob
+// of the one-pass kernel's tile. The single-scene heuristic (fused_cz) fills
+// the GPU with one scene's blocks; a lane of many small tasks fills it with
+// fewer, deeper blocks. With autotuning on, a lane whose task count has
+// changed by more than 2x since it was last tuned times two chunks at each
+// candidate depth (4, 8, 16, 32, 64 and the whole column, within the partial-
+// sum capacity) with CUDA events, then keeps the fastest. Depth changes wait
+// until the lane has no chunk in flight. Another depth changes the order of
+// the partial sums, so a tuned lane's answers agree with the untuned ones to
+// rounding, not bit for bit.
 struct InnerBatcher {
   static constexpr int kSlots = FU_MAX_BATCH, kInflight = 3, kRing = 4, kChunk = 5;
   struct Job {
@@ -1765,13 +1775,18 @@ struct InnerBatcher {
     int ring;
     unsigned long long order;  // launch order across lanes
     std::vector<Entry> jobs;   // the chunk's tasks in list order
-    bool timed;                // its launches are bracketed by the lane's timing events
     long long rows;            // pressure rows of its tasks
+    int cand;                  // autotuner candidate it measures, or -1
   };
   struct Lane {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[kRing] = {};
-    cudaEvent_t t0 = nullptr, t1 = nullptr;  // device time of every 8th chunk's launches
+    cudaEvent_t t0[kRing] = {}, t1[kRing] = {};  // device time of each chunk's launches
+    // autotuner: the lane's depth (0: each task's own), candidates, and the
+    // task count it was tuned for
+    int cz = 0, tunedTasks = 0, cand = -1, candChunks = 0;
+    std::vector<int> cands;
+    std::vector<double> candMs;
     PcrState* dStates = nullptr;  // [kRing][kSlots]
     PcrState* hStates = nullptr;  // pinned copies
     std::vector<Job*> active;
@@ -1797,6 +1812,7 @@ struct InnerBatcher {
   long long launches = 0, taskLaunches = 0, maxTasks = 0, solves = 0;
   long long timedLaunches = 0, timedRows = 0;
   double timedMs = 0;
+  bool autotune = false;
   unsigned long long nextSeq = 1, nextOrder = 0;
 
   static Shape shape_of(const FusedTask& t) { return {t.g.cX, t.g.cY, t.g.cZ, t.cz}; }
@@ -1819,8 +1835,10 @@ struct InnerBatcher {
   esf_status lane_init(Lane& L) {
     ESF_CUDA(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
     for (int i = 0; i < kRing; i++) ESF_CUDA(cudaEventCreateWithFlags(&L.ev[i], cudaEventDisableTiming));
-    ESF_CUDA(cudaEventCreate(&L.t0));
-    ESF_CUDA(cudaEventCreate(&L.t1));
+    for (int i = 0; i < kRing; i++) {
+      ESF_CUDA(cudaEventCreate(&L.t0[i]));
+      ESF_CUDA(cudaEventCreate(&L.t1[i]));
+    }
     ESF_CUDA(cudaMalloc(&L.dStates, sizeof(PcrState) * kSlots * kRing));
     ESF_CUDA(cudaMallocHost(&L.hStates, sizeof(PcrState) * kSlots * kRing));
     return ESF_OK;
@@ -1838,8 +1856,10 @@ struct InnerBatcher {
       if (L.stream) cudaStreamSynchronize(L.stream);
       for (int i = 0; i < kRing; i++)
         if (L.ev[i]) cudaEventDestroy(L.ev[i]);
-      if (L.t0) cudaEventDestroy(L.t0);
-      if (L.t1) cudaEventDestroy(L.t1);
+      for (int i = 0; i < kRing; i++) {
+        if (L.t0[i]) cudaEventDestroy(L.t0[i]);
+        if (L.t1[i]) cudaEventDestroy(L.t1[i]);
+      }
       cudaFree(L.dStates);
       if (L.hStates) cudaFreeHost(L.hStates);
       if (L.stream) cudaStreamDestroy(L.stream);
@@ -1870,12 +1890,16 @@ struct InnerBatcher {
     cudaEventSynchronize(L.ev[c.ring]);
     bool any = false;
     std::lock_guard<std::mutex> g(m);
-    if (c.timed) {
+    {
       float ms = 0;
-      if (cudaEventElapsedTime(&ms, L.t0, L.t1) == cudaSuccess) {
+      if (cudaEventElapsedTime(&ms, L.t0[c.ring], L.t1[c.ring]) == cudaSuccess) {
         timedMs += ms;
         timedLaunches += kChunk;
         timedRows += (long long)kChunk * c.rows;
+        if (c.cand >= 0 && c.cand == L.cand && c.rows > 0) {
+          L.candMs[c.cand] += ms / (double)c.rows;  // per row: task counts can change meanwhile
+          L.candChunks++;
+        }
       }
     }
     for (size_t i = 0; i < c.jobs.size(); i++) {
@@ -1896,6 +1920,79 @@ struct InnerBatcher {
       any = true;
     }
     if (any) doneCv.notify_all();
+  }
+  // a task's pass at depth cz (0: its own heuristic depth)
+  static void set_depth(FusedTask& t, int cz) {
+    if (cz <= 0) cz = fused_cz(t.g);
+    t.cz = cz;
+    const dim3 gr = tma_grid(t.g, cz);
+    t.gx = (int)gr.x;
+    t.gy = (int)gr.y;
+    t.gz = (int)gr.z;
+  }
+  // every active task of the lane at depth cz; only with no chunk in flight
+  void apply_depth(Lane& L, int cz) {
+    L.cz = cz;
+    std::lock_guard<std::mutex> g(m);
+    for (Job* j : L.active) {
+      set_depth(j->task, cz);
+      hTasks[j->slot] = j->task;
+      cudaMemcpyAsync(dTasks + j->slot, hTasks + j->slot, sizeof(FusedTask), cudaMemcpyHostToDevice,
+                      L.stream);
+    }
+  }
+  // The autotuner's step before a lane's next chunk; false while it waits
+  // for the lane's chunks in flight to drain before a depth change.
+  bool tune(Lane& L) {
+    if (!autotune) return true;
+    int n;
+    GridDev g;
+    {
+      std::lock_guard<std::mutex> lk(m);
+      n = (int)L.active.size();
+      if (!n) return true;
+      g = L.active[0]->task.g;
+    }
+    if (L.cand < 0) {
+      if (L.tunedTasks && n <= 2 * L.tunedTasks && 2 * n >= L.tunedTasks) return true;
+      // start: candidate depths within the partial-sum capacity
+      L.cands.clear();
+      const long long cols = (long long)((g.cX + TXW - 1) / TXW) * ((g.cY + TY - 1) / TY);
+      for (int cz : {4, 8, 16, 32, 64, g.cZ}) {
+        if (cz > g.cZ || (!L.cands.empty() && cz <= L.cands.back())) continue;
+        if (cols * ((g.cZ + cz - 1) / cz) * FU_SUMS > ESF_MAX_PARTIALS / 2) continue;
+        L.cands.push_back(cz);
+      }
+      if (L.cands.empty()) {
+        L.tunedTasks = n;
+        return true;
+      }
+      L.candMs.assign(L.cands.size(), 0.0);
+      L.cand = 0;
+      L.candChunks = 0;
+      L.tunedTasks = n;
+    }
+    const bool measured = L.candChunks >= 2;
+    const int want = measured ? -1 : L.cands[L.cand];
+    if (!measured && L.cz == want) return true;
+    if (!L.inflight.empty()) return false;  // drain before changing the depth
+    if (!measured) {
+      apply_depth(L, want);
+      return true;
+    }
+    // this candidate is measured: the next one, or the fastest when done
+    if (L.cand + 1 < (int)L.cands.size()) {
+      L.cand++;
+      L.candChunks = 0;
+      apply_depth(L, L.cands[L.cand]);
+      return true;
+    }
+    int best = 0;
+    for (int i = 1; i < (int)L.cands.size(); i++)
+      if (L.candMs[i] < L.candMs[best]) best = i;
+    L.cand = -1;
+    apply_depth(L, L.cands[best]);
+    return true;
   }
   // one chunk of a lane's active tasks
   void launch(Lane& L) {
@@ -1918,15 +2015,11 @@ struct InnerBatcher {
     }
     b.first[b.n] = blocks;
     const int ring = (int)(L.chunks % kRing);
-    // the timing events are reused: only a chunk whose predecessor with
-    // timing has been settled is timed (one timed chunk in flight per lane)
-    bool timed = (L.chunks % 8) == 0;
-    for (const Chunk& c : L.inflight) timed = timed && !c.timed;
-    if (timed) cudaEventRecord(L.t0, L.stream);
+    cudaEventRecord(L.t0[ring], L.stream);
     for (int k = 0; k < kChunk; k++) {
       ESF_COUNTED pcr_iteration_fused_batch<<<blocks, NT, FU_SMEM, L.stream>>>(dTasks, b);
     }
-    if (timed) cudaEventRecord(L.t1, L.stream);
+    cudaEventRecord(L.t1[ring], L.stream);
     ESF_COUNTED gather_task_states<<<1, 64, 0, L.stream>>>(dTasks, b, L.dStates + ring * kSlots);
     cudaMemcpyAsync(L.hStates + ring * kSlots, L.dStates + ring * kSlots, sizeof(PcrState) * b.n,
                     cudaMemcpyDeviceToHost, L.stream);
@@ -1935,7 +2028,7 @@ struct InnerBatcher {
     launches += kChunk;
     taskLaunches += (long long)kChunk * b.n;
     if (b.n > maxTasks) maxTasks = b.n;
-    L.inflight.push_back(Chunk{ring, nextOrder++, std::move(ids), timed, rows});
+    L.inflight.push_back(Chunk{ring, nextOrder++, std::move(ids), rows, L.cand});
   }
   void loop() {
     cudaSetDevice(device);
@@ -1970,6 +2063,7 @@ struct InnerBatcher {
           doneCv.notify_all();
           continue;
         }
+        if (L.cz) set_depth(j->task, L.cz);
         hTasks[j->slot] = j->task;
         cudaMemcpyAsync(dTasks + j->slot, hTasks + j->slot, sizeof(FusedTask), cudaMemcpyHostToDevice,
                         L.stream);
@@ -1988,7 +2082,7 @@ struct InnerBatcher {
           std::lock_guard<std::mutex> g(m);
           has = !L.active.empty();
         }
-        if (has && (int)L.inflight.size() < kInflight) {
+        if (has && (int)L.inflight.size() < kInflight && tune(L)) {
           launch(L);
           launched = true;
         }
@@ -2006,8 +2100,9 @@ struct InnerBatcher {
   }
 };
 
-esf_status batcher_create(int device, InnerBatcher** out) {
+esf_status batcher_create(int device, InnerBatcher** out, bool autotune) {
   InnerBatcher* b = new InnerBatcher();
+  b->autotune = autotune;
   esf_status e = b->init(device);
   if (e) {
     b->shutdown();

@@ -1459,8 +1459,8 @@ esf_status scene_set_batcher(esf_scene* s, InnerBatcher* b) {
 extern "C" esf_status esf_pressure_solve_batch(int n, const esf_grid* grids, const double* const* minv,
                                                const double* const* diag, const double* const* b,
                                                double* const* x, double eps, int maxIt, int precision,
-                                               int* iters, double* relres, esf_batch_stats* stats,
-                                               void* stream) {
+                                               int autotune, int* iters, double* relres,
+                                               esf_batch_stats* stats, void* stream) {
   if (n < 1 || !grids || !minv || !diag || !b || !x || maxIt < 0 ||
       (precision != ESF_FP64 && precision != ESF_MIXED)) {
     set_error("esf_pressure_solve_batch: invalid argument");
@@ -1475,7 +1475,7 @@ extern "C" esf_status esf_pressure_solve_batch(int n, const esf_grid* grids, con
   int dev = 0;
   ESF_CUDA(cudaGetDevice(&dev));
   InnerBatcher* batcher = nullptr;
-  if (precision == ESF_MIXED) TRY(batcher_create(dev, &batcher));
+  if (precision == ESF_MIXED) TRY(batcher_create(dev, &batcher, autotune != 0));
   cudaEvent_t start = nullptr;
   ESF_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
   ESF_CUDA(cudaEventRecord(start, (cudaStream_t)stream));

@@ -20,7 +20,8 @@ ESF_REQ_QUEUED, ESF_REQ_RUNNING, ESF_REQ_DONE, ESF_REQ_FAILED = 0, 1, 2, 3
 
 
 class ServerConfig(C.Structure):
-    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_active", C.c_int), ("no_batching", C.c_int)]
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_active", C.c_int), ("no_batching", C.c_int),
+                ("autotune", C.c_int)]
 
 
 class BatchStats(C.Structure):
@@ -101,10 +102,11 @@ def request_for(desc, steps: int, precision: int = abi.ESF_MIXED):
 
 
 class Server:
-    def __init__(self, hbm_budget_bytes: int = 0, max_active: int = 0, lib=None, batching: bool = True):
+    def __init__(self, hbm_budget_bytes: int = 0, max_active: int = 0, lib=None, batching: bool = True,
+                 autotune: bool = False):
         from . import load
         self._lib = lib or load()
-        cfg = ServerConfig(hbm_budget_bytes, max_active, 0 if batching else 1)
+        cfg = ServerConfig(hbm_budget_bytes, max_active, 0 if batching else 1, 1 if autotune else 0)
         h = C.c_void_p()
         st = self._lib.esf_server_create(C.byref(cfg), C.byref(h))
         if st != 0:

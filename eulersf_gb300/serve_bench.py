@@ -42,12 +42,12 @@ def make_requests(n, seed, sizes):
     return out
 
 
-def serve(descs, steps, rate, seed, max_active, batching=True):
+def serve(descs, steps, rate, seed, max_active, batching=True, autotune=False):
     from .serve import Server
     rng = np.random.default_rng(seed + 1)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, len(descs))) if rate > 0 else np.zeros(len(descs))
     stats = []
-    with Server(max_active=max_active, batching=batching) as srv:
+    with Server(max_active=max_active, batching=batching, autotune=autotune) as srv:
         t0 = time.perf_counter()
         tickets = []
         for d, at in zip(descs, arrivals):
@@ -75,11 +75,12 @@ def main(argv=None):
     ap.add_argument("--sizes", default="48,64,96,128,160")
     ap.add_argument("--max-active", type=int, default=8)
     ap.add_argument("--no-sequential", action="store_true")
+    ap.add_argument("--autotune", action="store_true", help="tune each batch lane's tile depth by timing")
     ap.add_argument("--no-batching", action="store_true",
                     help="each scene's inner solves on its own stream (no shared launches)")
     a = ap.parse_args(argv)
     descs = make_requests(a.requests, a.seed, [int(x) for x in a.sizes.split(",")])
-    wall, stats, batch = serve(descs, a.steps, a.rate, a.seed, a.max_active, not a.no_batching)
+    wall, stats, batch = serve(descs, a.steps, a.rate, a.seed, a.max_active, not a.no_batching, a.autotune)
     lat = np.array([s["latency_ms"] for s in stats])
     steps_all = a.steps * len(descs)
     line = {"metric": "served scene-steps/s (Poisson arrivals)", "requests": len(descs),
@@ -88,7 +89,7 @@ def main(argv=None):
             "latency_p50_ms": float(np.percentile(lat, 50)), "latency_p99_ms": float(np.percentile(lat, 99)),
             "queued_p50_ms": float(np.percentile([s["queued_ms"] for s in stats], 50)),
             "max_rel_residual": max(max(s["last"]["rel_residual"]) for s in stats),
-            "batching": not a.no_batching, "batch_stats": batch}
+            "batching": not a.no_batching, "autotune": a.autotune, "batch_stats": batch}
     if not a.no_sequential:
         swall, sstats, _ = serve(descs, a.steps, 0.0, a.seed, 1, False)
         line["sequential_steps_per_s"] = steps_all / swall

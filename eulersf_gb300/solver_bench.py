@@ -6,7 +6,7 @@ scene's size, device-resident inputs, timed with CUDA events on the stream
 the solve runs on.
 
     python -m eulersf_gb300.solver_bench [--size 256] [--precision mixed|fp64]
-                                         [--iters 300] [--repeat 3] [--batch B]
+                                         [--iters 300] [--repeat 3] [--batch B [--autotune]]
 
 The tolerance is set to 1e-30 so every solve runs exactly --iters
 iterations (mixed: FP32 inner iterations summed over the refinements).
@@ -68,7 +68,7 @@ def run(size=256, precision="mixed", iters=300, repeat=3, seed=0):
             "us_per_iter": 1e6 / max(rates)}
 
 
-def run_batch(size=32, batch=256, iters=300, repeat=2):
+def run_batch(size=32, batch=256, iters=300, repeat=2, autotune=False):
     import os
     import time
 
@@ -96,7 +96,7 @@ def run_batch(size=32, batch=256, iters=300, repeat=2):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         s = lib.esf_pressure_solve_batch(batch, grids, arr(dm), arr(dd), arr(db), arr(dx), 1e-30, n,
-                                         abi.ESF_MIXED, its, rr, C.byref(stats), None)
+                                         abi.ESF_MIXED, int(autotune), its, rr, C.byref(stats), None)
         t = time.perf_counter() - t0
         if s != 0:
             raise abi.EsfError(s, "esf_pressure_solve_batch", (lib.esf_last_error() or b"").decode())
@@ -121,6 +121,7 @@ def run_batch(size=32, batch=256, iters=300, repeat=2):
     gbs = n * 48.0 * R / t / 1e9
     mgbs = marginal * 48.0 * R / 1e9 if marginal else None
     return {"metric": "batched pressure PCR iterations/s", "size": size, "batch": batch, "rows_each": R,
+            "autotune": autotune,
             "precision": "mixed", "iters_per_solve": iters, "iters_total": n, "wall_s": t,
             "iters_per_s": n / t, "effective_gbs": gbs, "hbm_peak_gbs": peak,
             "frac_of_hbm": (gbs / peak) if peak else None,
@@ -142,9 +143,10 @@ def main(argv=None):
     ap.add_argument("--iters", type=int, default=300)
     ap.add_argument("--repeat", type=int, default=3)
     ap.add_argument("--batch", type=int, default=1)
+    ap.add_argument("--autotune", action="store_true", help="batched: tune the tile depth by timing")
     a = ap.parse_args(argv)
     if a.batch > 1:
-        print(json.dumps(run_batch(a.size, a.batch, a.iters, a.repeat)), flush=True)
+        print(json.dumps(run_batch(a.size, a.batch, a.iters, a.repeat, a.autotune)), flush=True)
     else:
         print(json.dumps(run(a.size, a.precision, a.iters, a.repeat)), flush=True)
     return 0

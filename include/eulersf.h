@@ -247,14 +247,16 @@ esf_status esf_pressure_solve(const esf_grid* grid, const double* mass_inv_node,
  * grid shape advance in shared launches (continuous batching, as the server
  * does); each system's FP64 refinement runs on its own stream, driven by its
  * own host thread. Every system gets the same answer, iterations and bits as
- * esf_pressure_solve alone. `stats` (may be NULL) receives the batcher's
+ * esf_pressure_solve alone, unless `autotune` is set: the batcher then picks
+ * each shape's tile depth by timing (esf_server_config.autotune), and the
+ * answers agree to rounding instead. `stats` (may be NULL) receives the batcher's
  * counters (esf_batch_stats, below). Work waits for what is queued on
  * `stream` before the call; the call returns when every solve has finished. */
 struct esf_batch_stats;
 esf_status esf_pressure_solve_batch(int n, const esf_grid* grids, const double* const* mass_inv_node,
                                     const double* const* diag, const double* const* b,
                                     double* const* x, double eps, int max_iterations, int precision,
-                                    int* iterations, double* rel_residual,
+                                    int autotune, int* iterations, double* rel_residual,
                                     struct esf_batch_stats* stats, void* stream);
 
 /* Allocation-free variant of esf_pressure_solve at ESF_FP64. It has no
@@ -308,6 +310,8 @@ typedef struct esf_server_config {
   size_t hbm_budget_bytes; /* admission budget; 0: 85% of the device's free memory */
   int max_active;          /* scenes stepping at once; 0: 8 */
   int no_batching;         /* 1: each scene runs its inner solves alone on its own stream */
+  int autotune;            /* 1: the batcher tunes each lane's tile depth by timing (answers then
+                              agree with untuned runs to rounding, not bit for bit) */
 } esf_server_config;
 typedef struct esf_request {
   esf_grid grid;

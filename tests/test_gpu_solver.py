@@ -217,7 +217,7 @@ def test_batched_solve_equals_single_solves(gpu_lib):
     its, rr = (C.c_int * n)(), (C.c_double * n)()
     from eulersf_gb300.serve import BatchStats
     stats = BatchStats()
-    st = gpu_lib.esf_pressure_solve_batch(n, grids, arr(dm), arr(dd), arr(db), arr(dx), 1e-8, 20000, 1,
+    st = gpu_lib.esf_pressure_solve_batch(n, grids, arr(dm), arr(dd), arr(db), arr(dx), 1e-8, 20000, 1, 0,
                                           its, rr, C.byref(stats), None)
     torch.cuda.synchronize()
     assert st == 0, gpu_lib.esf_last_error()
@@ -231,3 +231,42 @@ def test_batched_solve_equals_single_solves(gpu_lib):
         torch.cuda.synchronize()
         assert its[i] == it.value and rr[i] == r1.value and rr[i] < 1e-8
         assert torch.equal(dx[i], sx), i
+
+
+def test_autotuned_batched_solve_converges_to_the_same_answers(gpu_lib):
+    """With the tile autotuner on, a batch of twelve 24^3 systems: the tuner
+    times other tile depths on the lane (their partial sums fold in another
+    order), so each answer meets the 1e-8 residual (checked with the oracle's
+    operator) and agrees with the single solve to the system's conditioning
+    times the tolerance."""
+    import torch
+    from eulersf_gb300.serve import BatchStats
+    X, n = 25, 12
+    systems = []
+    for seed in range(n):
+        rng = np.random.default_rng(100 + seed)
+        g = oracle.grid(X, 1.0 / (X - 1))
+        minv = rng.uniform(50.0, 300.0, X ** 3)
+        b = oracle.pressure_apply(g, minv, rng.standard_normal((X - 1) ** 3))
+        systems.append((g, minv, _jacobi_diag(X, X, X, minv), b))
+    dm = [_dev(s[1]) for s in systems]
+    dd = [_dev(s[2]) for s in systems]
+    db = [_dev(s[3]) for s in systems]
+    dx = [_dev(np.zeros(len(s[3]))) for s in systems]
+    grids = (type(systems[0][0]) * n)(*[s[0] for s in systems])
+    arr = lambda ts: (C.c_void_p * n)(*[t.data_ptr() for t in ts])
+    its, rr, stats = (C.c_int * n)(), (C.c_double * n)(), BatchStats()
+    st = gpu_lib.esf_pressure_solve_batch(n, grids, arr(dm), arr(dd), arr(db), arr(dx), 1e-8, 20000, 1, 1,
+                                          its, rr, C.byref(stats), None)
+    torch.cuda.synchronize()
+    assert st == 0, gpu_lib.esf_last_error()
+    assert stats.max_tasks >= 2, stats.as_dict()
+    for i, (g, minv, diag, b) in enumerate(systems):
+        x = dx[i].cpu().numpy()
+        res = np.linalg.norm(oracle.pressure_apply(g, minv, x) - b) / np.linalg.norm(b)
+        assert rr[i] < 1e-8 and res < 1.01e-8, (i, rr[i], res)
+        sx = _dev(np.zeros(len(b)))
+        it, r1 = C.c_int(), C.c_double()
+        assert gpu_lib.esf_pressure_solve(C.byref(g), _ptr(dm[i]), _ptr(dd[i]), _ptr(db[i]), _ptr(sx), 1e-8,
+                                          20000, 1, C.byref(it), C.byref(r1), None) == 0
+        assert rel_err(x, sx.cpu().numpy()) <= 1e-3, i
