@@ -10,7 +10,13 @@
 // (APPLICATION::step :174-204), and writes every intermediate field as .npy.
 //
 // usage: ref_harness <cfg> <outdir> <frames> [--noise <file.npy-raw f64 X^3*3>]
-//                    [--dump-every k] [--no-dump] [--time]
+//                    [--dump-every k] [--no-dump] [--full-every k] [--frame-restart dir]
+//
+// --frame-restart dir: after the last step, COUPLED_INTEGRATOR_3D::writeFrame
+// (frame 0, debug) writes the state into dir; a second integrator built the
+// same way reads it back (readFrame), writes it again as frame 1, and takes
+// one step; its state after the read and after that step is dumped with the
+// prefixes "r0." and "r1.", and the step's log line goes to log_restart.jsonl.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -26,6 +32,7 @@
 #include <vector>
 #include <sys/stat.h>
 #include <sys/time.h>
+#include <unistd.h>
 #include <Eigen/Dense>
 #include <Eigen/Sparse>
 #include <Eigen/Geometry>
@@ -218,38 +225,15 @@ static void dump_state(Dumper& d, COUPLED_INTEGRATOR_3D* I, bool full) {
   }
 }
 
-int main(int argc, char** argv) {
-  if (argc < 4) {
-    fprintf(stderr,
-            "usage: %s <cfg> <outdir> <frames> [--noise file] [--dump-every k]"
-            " [--no-dump] [--full-every k]\n",
-            argv[0]);
-    return 2;
-  }
-  std::string cfg = argv[1];
-  std::string outdir = argv[2];
-  int frames = atoi(argv[3]);
-  std::string noiseFile;
-  int dumpEvery = 1, fullEvery = 1;
-  bool noDump = false;
-  for (int a = 4; a < argc; a++) {
-    std::string s = argv[a];
-    if (s == "--noise" && a + 1 < argc) noiseFile = argv[++a];
-    else if (s == "--dump-every" && a + 1 < argc) dumpEvery = atoi(argv[++a]);
-    else if (s == "--full-every" && a + 1 < argc) fullEvery = atoi(argv[++a]);
-    else if (s == "--no-dump") noDump = true;
-  }
-  mkdir(outdir.c_str(), 0755);
-  Eigen::initParallel();
-  if (!SIMPLE_PARSER::parse(cfg)) return 3;
-
+// APPLICATION::init (projects/rubberBall/main.cpp:63-97) and addSolids
+// (:99-160), headless: a new integrator with the cfg's solids, initialised.
+static COUPLED_INTEGRATOR_3D* build_integrator() {
   // APPLICATION::init (projects/rubberBall/main.cpp:63-97), headless.
   int xRes = SIMPLE_PARSER::getInt("xRes", 100);
   int yRes = SIMPLE_PARSER::getInt("yRes", 100);
   int zRes = SIMPLE_PARSER::getInt("zRes", 100);
   Real dh = SIMPLE_PARSER::getFloat("dh", 0.01);
   VEC3F origin = SIMPLE_PARSER::getVEC3F("origin", VEC3F(0, 0, 0));
-  double t0 = now_s();
   COUPLED_INTEGRATOR_3D* integrator =
       new COUPLED_INTEGRATOR_3D(xRes, yRes, zRes, dh, origin);
 
@@ -298,6 +282,40 @@ int main(int argc, char** argv) {
   integrator->setFluidDensity(SIMPLE_PARSER::getFloat("fluid density", 1));
   integrator->setFluidViscocity(SIMPLE_PARSER::getFloat("fluid viscocity", 0));
   integrator->init();
+  return integrator;
+}
+
+int main(int argc, char** argv) {
+  if (argc < 4) {
+    fprintf(stderr,
+            "usage: %s <cfg> <outdir> <frames> [--noise file] [--dump-every k]"
+            " [--no-dump] [--full-every k]\n",
+            argv[0]);
+    return 2;
+  }
+  std::string cfg = argv[1];
+  std::string outdir = argv[2];
+  int frames = atoi(argv[3]);
+  std::string noiseFile;
+  int dumpEvery = 1, fullEvery = 1;
+  bool noDump = false;
+  std::string restartDir;
+  for (int a = 4; a < argc; a++) {
+    std::string s = argv[a];
+    if (s == "--noise" && a + 1 < argc) noiseFile = argv[++a];
+    else if (s == "--dump-every" && a + 1 < argc) dumpEvery = atoi(argv[++a]);
+    else if (s == "--full-every" && a + 1 < argc) fullEvery = atoi(argv[++a]);
+    else if (s == "--no-dump") noDump = true;
+    else if (s == "--frame-restart" && a + 1 < argc) restartDir = argv[++a];
+  }
+  mkdir(outdir.c_str(), 0755);
+  Eigen::initParallel();
+  if (!SIMPLE_PARSER::parse(cfg)) return 3;
+
+  double t0 = now_s();
+  COUPLED_INTEGRATOR_3D* integrator = build_integrator();
+  const int xRes = integrator->xRes(), yRes = integrator->yRes(), zRes = integrator->zRes();
+  const Real dh = integrator->dh();
 
   Real carpetThickness = SIMPLE_PARSER::getFloat("smoke carpet thickness", 0.06);
   int carpetLayers = carpetThickness / dh;
@@ -368,6 +386,38 @@ int main(int argc, char** argv) {
     }
   }
   fclose(log);
+  if (!restartDir.empty()) {
+    // COUPLED_INTEGRATOR_3D::writeFrame/readFrame take their directory from
+    // the "data path" key (empty here), so the files go to the working directory
+    char cwd[4096];
+    if (!getcwd(cwd, sizeof cwd)) return 5;
+    mkdir(restartDir.c_str(), 0755);
+    if (chdir(restartDir.c_str()) != 0) return 5;
+    integrator->writeFrame(0, true);
+    COUPLED_INTEGRATOR_3D* again = build_integrator();
+    again->readFrame(0, true);
+    again->writeFrame(1, true);
+    if (chdir(cwd) != 0) return 5;
+    Dumper dr;
+    dr.dir = outdir;
+    dr.prefix = "r0.";
+    dump_state(dr, again, false);
+    again->setMaxDt(frameTimeStep);
+    size_t n1 = again->_solver.numberOfIterations().size();
+    size_t n2 = again->_divFreeSolver.numberOfIterations().size();
+    Real energy = again->stepImplicit();
+    FILE* rl = fopen((outdir + "/log_restart.jsonl").c_str(), "w");
+    std::vector<int>& it1 = again->_solver.numberOfIterations();
+    std::vector<int>& it2 = again->_divFreeSolver.numberOfIterations();
+    fprintf(rl, "{\"step\": 1, \"dt\": %.17g, \"energy\": %.17g, \"solid_iters\": [", again->dt(), energy);
+    for (size_t k = n1; k < it1.size(); k++) fprintf(rl, "%s%d", k > n1 ? ", " : "", it1[k]);
+    fprintf(rl, "], \"pressure_iters\": [");
+    for (size_t k = n2; k < it2.size(); k++) fprintf(rl, "%s%d", k > n2 ? ", " : "", it2[k]);
+    fprintf(rl, "]}\n");
+    fclose(rl);
+    dr.prefix = "r1.";
+    dump_state(dr, again, false);
+  }
   delete integrator;
   return 0;
 }

@@ -17,6 +17,10 @@ fields at every solid node:
 
     python tests/golden/make_golden.py --big config1_64 config2_128 [--keep DIR]
 
+and the reference's own frame files with a restart from them (``run_frame``):
+
+    python tests/golden/make_golden.py --frame
+
 ``--keep DIR`` keeps the harness's raw dumps there and reuses a completed run.
 """
 from __future__ import annotations
@@ -105,6 +109,54 @@ def run(name, desc, frames, out_dir):
             p = os.path.join(dump, f"s0.solid{i}.rotation.npy")
             if os.path.exists(p):  # the reference's own rotation matrix
                 sd["rotation_matrix"] = [float(x) for x in np.load(p).reshape(-1)]
+        arrays["scene"] = np.array(json.dumps({
+            "N": desc.N, "mass_sample_dh": desc.mass_sample_dh, "vorticity_eps": desc.vorticity_eps,
+            "buoyancy": desc.buoyancy, "noise_seed": desc.noise_seed, "frames": frames,
+            "flow_rate": desc.flow_rate, "solids": solids}))
+        np.savez_compressed(os.path.join(out_dir, name + ".npz"), **arrays)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+
+
+# Frame files: the reference writes its state after the last step
+# (writeFrame, frame 0, debug), a second integrator reads them back (readFrame)
+# and writes them again as frame 1, and takes one step. The fixture holds the
+# frame files as written (gz bytes, OBJ text), the warm start the step used
+# (the last solve's lambda1, a function-local static the frame does not
+# carry) and the state after the read (r0.*) and after the step (r1.*).
+FRAME_SCENE = ("frame16", SceneDesc(N=16, mass_sample_dh=(1 / 16) / 4, noise_seed=6), 2)
+RESTART_FIELDS = ["gridIdxToSolidIdx", "velocity", "intensity", "lambda1", "solid0.valid", "solid0.boxes",
+                  "solid0.mass", "solid0.phi", "solid0.u", "solid0.velocity", "solid0.meshVertices",
+                  "solid0.particles", "nodeSolidVolumeFraction"]
+
+
+def run_frame(out_dir):
+    name, desc, frames = FRAME_SCENE
+    tmp = tempfile.mkdtemp(prefix="esf_golden_")
+    try:
+        cfg = write_scene(desc, os.path.join(tmp, "scene"))
+        dump, fdir = os.path.join(tmp, "dump"), os.path.join(tmp, "frames")
+        subprocess.run([HARNESS, cfg, dump, str(frames), "--noise", os.path.join(tmp, "scene", "noise.f64"),
+                        "--no-dump", "--frame-restart", fdir], check=True,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        arrays = {}
+        for f in sorted(os.listdir(fdir)):
+            if f.endswith(".pbrt"):
+                continue  # render export, not state
+            with open(os.path.join(fdir, f), "rb") as fh:
+                arrays["file." + f] = np.frombuffer(fh.read(), dtype=np.uint8)
+        for pre in ("r0.", "r1."):
+            for f in RESTART_FIELDS:
+                p = os.path.join(dump, f"{pre}{f}.npy")
+                if os.path.exists(p):
+                    arrays[pre + f] = np.load(p)
+        log = [json.loads(l) for l in open(os.path.join(dump, "log.jsonl"))][1:]
+        for l in log:
+            l.pop("seconds", None)
+        arrays["log"] = np.array(json.dumps(log))
+        arrays["log_restart"] = np.array(json.dumps(
+            [json.loads(l) for l in open(os.path.join(dump, "log_restart.jsonl"))]))
+        solids = [dict(sd.__dict__) for sd in desc.solids]
         arrays["scene"] = np.array(json.dumps({
             "N": desc.N, "mass_sample_dh": desc.mass_sample_dh, "vorticity_eps": desc.vorticity_eps,
             "buoyancy": desc.buoyancy, "noise_seed": desc.noise_seed, "frames": frames,
@@ -233,6 +285,10 @@ def main():
         return
     if not os.path.exists(HARNESS):
         sys.exit(f"{HARNESS} missing: build it with make -C oracle")
+    if args == ["--frame"]:
+        run_frame(HERE)
+        print(FRAME_SCENE[0], os.path.getsize(os.path.join(HERE, FRAME_SCENE[0] + ".npz")), "bytes")
+        return
     only = args  # optional scene names
     for name, (desc, frames) in scenes().items():
         if only and name not in only:

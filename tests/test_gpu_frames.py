@@ -3,8 +3,12 @@ COUPLED_INTEGRATOR_3D::writeFrame/readFrame): the written gz fields are the
 scene's fields bit for bit in the FIELD_3D layout the reference reads
 (the same layout tests/golden's .mass inputs use), the OBJ holds the current
 mesh to 6 significant digits, the every-10th-frame rule is kept, and a fresh
-scene that reads a frame holds the same fields and keeps stepping."""
+scene that reads a frame holds the same fields and keeps stepping. Against
+the reference's own frame files (tests/golden/frame16.npz): reading them
+restores the reference's read state and steps like the reference's restart,
+and writing after the read gives the reference's bytes."""
 import ctypes as C
+import json
 import os
 
 import numpy as np
@@ -80,3 +84,85 @@ def test_read_frame_restores_fields_and_steps(tmp_path, gpu_lib):
     assert "needs" in E.last_error() or "holds" in E.last_error()
     for s in (A, B, C_):
         s.close()
+
+
+def _reference_frames(tmp_path):
+    """The reference's own frame files (tests/golden/frame16.npz, written by
+    COUPLED_INTEGRATOR_3D::writeFrame) into tmp_path; returns the fixture."""
+    from common import load_golden
+    desc, z, log = load_golden("frame16")
+    for k in z.files:
+        if k.startswith("file."):
+            with open(os.path.join(tmp_path, k[5:]), "wb") as f:
+                f.write(z[k].tobytes())
+    return desc, z
+
+
+def test_reads_reference_frame_and_steps_like_the_reference(tmp_path, gpu_lib):
+    """esf_read_frame on the files the reference wrote restores the state the
+    reference's readFrame restores (maps and flags bit-exact, fields to 1e-6),
+    and one step from there matches the reference's step from its read (the
+    warm start, which no frame carries, set to the reference's)."""
+    import eulersf_gb300 as E
+    desc, z = _reference_frames(tmp_path)
+    G = E.make_scene(desc)
+    G.readFrame(0, debug=True, data_path=str(tmp_path) + "/")
+    fails = _compare(G.get, z, "r0.")
+    assert not fails, fails
+    G.set("lambda1", z["r0.lambda1"])
+    r = G.stepImplicit()
+    ref = json.loads(str(z["log_restart"]))[0]
+    assert r["status"] == 0 and all(r["converged"]), r
+    want = [ref["solid_iters"][0], ref["pressure_iters"][0], ref["solid_iters"][1]]
+    assert all(abs(a - b) <= 5 for a, b in zip(r["iterations"], want)), (r["iterations"], want)
+    assert r["dt"] == ref["dt"]
+    assert abs(r["energy"] - ref["energy"]) <= 1e-8 * abs(ref["energy"])
+    fails = _compare(G.get, z, "r1.")
+    assert not fails, fails
+    G.close()
+
+
+def _compare(get, z, pre, tol=1e-6):
+    from common import EXACT, NAME, rel_err
+    fails = []
+    for k in z.files:
+        if not k.startswith(pre):
+            continue
+        f = k[len(pre):]
+        mine, ref = np.asarray(get(NAME[f])), z[k]
+        if f in EXACT:
+            if not np.array_equal(mine.reshape(-1), ref.reshape(-1).astype(mine.dtype)):
+                fails.append(f"{k}: not bit-exact")
+        else:
+            a, b = mine.reshape(-1), ref.reshape(-1)
+            if f == "solid0.particles":
+                a, b = mine.reshape(-1, 10)[:, :9], ref.reshape(-1, 10)[:, :9]
+            if a.size != b.size or not rel_err(a, b) <= tol:
+                fails.append(f"{k}: rel err {rel_err(a, b) if a.size == b.size else 'size'}")
+    return fails
+
+
+def test_written_frame_is_the_reference_frame(tmp_path, gpu_lib):
+    """After reading the reference's frame 0, esf_write_frame writes frame 1
+    with the same content as the reference's writeFrame after its read: the
+    gz fields decompress to the same bytes (header and data), and the OBJ is
+    the same text."""
+    import gzip
+    import eulersf_gb300 as E
+    desc, z = _reference_frames(tmp_path)
+    out = tmp_path / "ours"
+    out.mkdir()
+    G = E.make_scene(desc)
+    G.readFrame(0, debug=True, data_path=str(tmp_path) + "/")
+    G.writeFrame(1, debug=True, data_path=str(out) + "/")
+    names = [k[5:] for k in z.files if k.startswith("file.frame.0001.")]
+    assert names
+    for n in names:
+        ref = z["file." + n].tobytes()
+        with open(out / n, "rb") as f:
+            mine = f.read()
+        if n.endswith(".obj"):
+            assert mine == ref, n
+        else:
+            assert gzip.decompress(mine) == gzip.decompress(ref), n
+    G.close()

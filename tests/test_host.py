@@ -197,3 +197,20 @@ def test_reference_arm_two_ranks_prints_one_line(tmp_path):
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+
+
+def test_reads_the_reference_frame_layout(tmp_path):
+    """scene.read_field_gz (the FIELD_3D gz layout of esf_io.cpp) reads a frame
+    file the reference's writeFrame wrote: three int32 resolutions, dh and
+    origin as float64, then the data; the velocity it holds is the state the
+    reference's readFrame restored, away from the solid's nodes (which
+    recoverVelocityField overwrites on reading)."""
+    from common import load_golden
+    desc, z, _ = load_golden("frame16")
+    p = tmp_path / "frame.0000.velocity"
+    p.write_bytes(z["file.frame.0000.velocity"].tobytes())
+    res, dh, origin, data = scene.read_field_gz(str(p))
+    assert tuple(res) == (desc.res,) * 3 and dh == desc.dh and list(origin) == [0.0, 0.0, 0.0]
+    v = data.reshape(-1, 3)
+    fluid = z["r0.gridIdxToSolidIdx"] < 0
+    assert np.array_equal(v[fluid], z["r0.velocity"].reshape(-1, 3)[fluid])
