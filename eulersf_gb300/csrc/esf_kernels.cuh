@@ -67,35 +67,45 @@ struct SolidDev {
 };
 
 // --------------------------------------------------------- 3x3 helpers
-struct M3 {
-  double m[3][3];
+// Templated on the arithmetic type: double everywhere on the reference's
+// path; float for the stress evaluation of the mixed-precision path
+// (k_element_stiffness_f32). The double instantiations are the reference's
+// operation order.
+template <class T>
+struct M3T {
+  T m[3][3];
 };
-__device__ __forceinline__ M3 m3_id() {
-  M3 r;
+using M3 = M3T<double>;
+template <class T = double>
+__device__ __forceinline__ M3T<T> m3_id() {
+  M3T<T> r;
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
-    for (int j = 0; j < 3; j++) r.m[i][j] = (i == j) ? 1.0 : 0.0;
+    for (int j = 0; j < 3; j++) r.m[i][j] = (i == j) ? T(1) : T(0);
   return r;
 }
-__device__ __forceinline__ M3 m3_mul(const M3& a, const M3& b) {
-  M3 r;
+template <class T>
+__device__ __forceinline__ M3T<T> m3_mul(const M3T<T>& a, const M3T<T>& b) {
+  M3T<T> r;
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++) r.m[i][j] = (a.m[i][0] * b.m[0][j] + a.m[i][1] * b.m[1][j]) + a.m[i][2] * b.m[2][j];
   return r;
 }
-__device__ __forceinline__ M3 m3_mul_bt(const M3& a, const M3& b) {
-  M3 r;
+template <class T>
+__device__ __forceinline__ M3T<T> m3_mul_bt(const M3T<T>& a, const M3T<T>& b) {
+  M3T<T> r;
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++) r.m[i][j] = (a.m[i][0] * b.m[j][0] + a.m[i][1] * b.m[j][1]) + a.m[i][2] * b.m[j][2];
   return r;
 }
-__device__ __forceinline__ M3 m3_mul_at(const M3& a, const M3& b) {
-  M3 r;
+template <class T>
+__device__ __forceinline__ M3T<T> m3_mul_at(const M3T<T>& a, const M3T<T>& b) {
+  M3T<T> r;
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -103,22 +113,25 @@ __device__ __forceinline__ M3 m3_mul_at(const M3& a, const M3& b) {
   return r;
 }
 // MatrixBase::determinant, 3x3 (Eigen/src/LU/Determinant.h:18-23, 61-68)
-__device__ __forceinline__ double m3_det(const M3& a) {
-  double h0 = a.m[0][0] * (a.m[1][1] * a.m[2][2] - a.m[1][2] * a.m[2][1]);
-  double h1 = a.m[0][1] * (a.m[1][0] * a.m[2][2] - a.m[1][2] * a.m[2][0]);
-  double h2 = a.m[0][2] * (a.m[1][0] * a.m[2][1] - a.m[1][1] * a.m[2][0]);
+template <class T>
+__device__ __forceinline__ T m3_det(const M3T<T>& a) {
+  T h0 = a.m[0][0] * (a.m[1][1] * a.m[2][2] - a.m[1][2] * a.m[2][1]);
+  T h1 = a.m[0][1] * (a.m[1][0] * a.m[2][2] - a.m[1][2] * a.m[2][0]);
+  T h2 = a.m[0][2] * (a.m[1][0] * a.m[2][1] - a.m[1][1] * a.m[2][0]);
   return (h0 - h1) + h2;
 }
-__device__ __forceinline__ double cof3(const M3& a, int i, int j) {
+template <class T>
+__device__ __forceinline__ T cof3(const M3T<T>& a, int i, int j) {
   int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
   return a.m[i1][j1] * a.m[i2][j2] - a.m[i1][j2] * a.m[i2][j1];
 }
 // compute_inverse<...,3> (Eigen/src/LU/Inverse.h:130-158)
-__device__ __forceinline__ M3 m3_inv(const M3& a) {
-  double c0 = cof3(a, 0, 0), c1 = cof3(a, 1, 0), c2 = cof3(a, 2, 0);
-  double det = c0 * a.m[0][0] + (c1 * a.m[1][0] + c2 * a.m[2][0]);
-  double iv = 1.0 / det;
-  M3 r;
+template <class T>
+__device__ __forceinline__ M3T<T> m3_inv(const M3T<T>& a) {
+  T c0 = cof3(a, 0, 0), c1 = cof3(a, 1, 0), c2 = cof3(a, 2, 0);
+  T det = c0 * a.m[0][0] + (c1 * a.m[1][0] + c2 * a.m[2][0]);
+  T iv = T(1) / det;
+  M3T<T> r;
   r.m[0][0] = c0 * iv;
   r.m[0][1] = c1 * iv;
   r.m[0][2] = c2 * iv;
@@ -129,6 +142,7 @@ __device__ __forceinline__ M3 m3_inv(const M3& a) {
   return r;
 }
 __device__ __forceinline__ double sum3(double a, double b, double c) { return a + (b + c); }
+__device__ __forceinline__ float sum3(float a, float b, float c) { return a + (b + c); }
 
 // DEFOR_SOLID_3D::computeF (DEFOR_SOLID_3D.cpp:671-682) on the 8 corner
 // displacements of the cell whose corner 0 is node `base`.
@@ -1090,42 +1104,54 @@ __global__ void k_cfl_vmax(GridDev g, const double* vel, const double* solidMass
 // ----------------------------------------------------- material (a5-a8)
 // Cyclic Jacobi eigen-decomposition of the symmetric F^T F (stands in for
 // Eigen::JacobiSVD in COROTATION::svd, COROTATION.cpp:239; R, S and L are
-// invariant to its sign and order choices).
-__device__ void sym_eig3(const M3& A, double w[3], M3& V) {
-  double a[3][3];
+// invariant to its sign and order choices). Sweeps stop when the
+// off-diagonal mass falls to the type's rounding level.
+template <class T>
+struct JacobiTol;
+template <>
+struct JacobiTol<double> {
+  static constexpr double tiny = 1e-300, rel = 1e-18;
+};
+template <>
+struct JacobiTol<float> {
+  static constexpr float tiny = 1e-30f, rel = 1e-7f;
+};
+template <class T>
+__device__ void sym_eig3(const M3T<T>& A, T w[3], M3T<T>& V) {
+  T a[3][3];
   for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++) a[i][j] = A.m[i][j];
-  M3 v = m3_id();
+  M3T<T> v = m3_id<T>();
   for (int sweep = 0; sweep < 50; sweep++) {
-    double off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
-    double scale = fabs(a[0][0]) + fabs(a[1][1]) + fabs(a[2][2]);
-    if (off == 0.0 || off <= 1e-300 + 1e-18 * scale) break;
+    T off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
+    T scale = fabs(a[0][0]) + fabs(a[1][1]) + fabs(a[2][2]);
+    if (off == T(0) || off <= JacobiTol<T>::tiny + JacobiTol<T>::rel * scale) break;
     for (int p = 0; p < 2; p++)
       for (int q = p + 1; q < 3; q++) {
-        double apq = a[p][q];
-        if (apq == 0.0) continue;
-        double theta = (a[q][q] - a[p][p]) / (2.0 * apq);
-        double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-        double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        T apq = a[p][q];
+        if (apq == T(0)) continue;
+        T theta = (a[q][q] - a[p][p]) / (T(2) * apq);
+        T t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + T(1)));
+        T c = T(1) / sqrt(t * t + T(1)), s = t * c;
         for (int k = 0; k < 3; k++) {
-          double akp = a[k][p], akq = a[k][q];
+          T akp = a[k][p], akq = a[k][q];
           a[k][p] = c * akp - s * akq;
           a[k][q] = s * akp + c * akq;
         }
         for (int k = 0; k < 3; k++) {
-          double apk = a[p][k], aqk = a[q][k];
+          T apk = a[p][k], aqk = a[q][k];
           a[p][k] = c * apk - s * aqk;
           a[q][k] = s * apk + c * aqk;
         }
         for (int k = 0; k < 3; k++) {
-          double vkp = v.m[k][p], vkq = v.m[k][q];
+          T vkp = v.m[k][p], vkq = v.m[k][q];
           v.m[k][p] = c * vkp - s * vkq;
           v.m[k][q] = s * vkp + c * vkq;
         }
       }
   }
   int ord[3] = {0, 1, 2};
-  double d[3] = {a[0][0], a[1][1], a[2][2]};
+  T d[3] = {a[0][0], a[1][1], a[2][2]};
   for (int i = 0; i < 3; i++)
     for (int j = i + 1; j < 3; j++)
       if (d[ord[j]] > d[ord[i]]) {
@@ -1134,30 +1160,34 @@ __device__ void sym_eig3(const M3& A, double w[3], M3& V) {
         ord[j] = t;
       }
   for (int c = 0; c < 3; c++) {
-    w[c] = d[ord[c]] < 0.0 ? 0.0 : d[ord[c]];
+    w[c] = d[ord[c]] < T(0) ? T(0) : d[ord[c]];
     for (int r = 0; r < 3; r++) V.m[r][c] = v.m[r][ord[c]];
   }
 }
 
-struct Corot {
-  double lambda, mu;
-  M3 R, S, L;
-  M3 V, Fh;  // of the decomposition (COROTATION::V(), Fhat())
+template <class T>
+struct CorotT {
+  T lambda, mu;
+  M3T<T> R, S, L;
+  M3T<T> V, Fh;  // of the decomposition (COROTATION::V(), Fhat())
+  T w[3];        // eigenvalues of F^T F, descending
 };
+using Corot = CorotT<double>;
 
 // COROTATION::orthogonalizeU (COROTATION.cpp:127-230)
-__device__ void orthogonalize_u(M3& U, const M3& Fh) {
-  double signU = (m3_det(U) >= 0.0) ? 1.0 : -1.0;
+template <class T>
+__device__ void orthogonalize_u(M3T<T>& U, const M3T<T>& Fh) {
+  T signU = (m3_det(U) >= T(0)) ? T(1) : T(-1);
   int inv[3] = {0, 0, 0}, total = 0;
   for (int x = 0; x < 3; x++)
-    if (Fh.m[x][x] < 1e-4) {
+    if (Fh.m[x][x] < T(1e-4)) {
       inv[x] = 1;
       total++;
     }
   if (total == 0) return;
   if (total == 1) {
     int w = inv[2] ? 2 : (inv[1] ? 1 : 0);
-    double c0[3], c1[3], c2[3];
+    T c0[3], c1[3], c2[3];
     for (int r = 0; r < 3; r++) {
       c0[r] = U.m[r][(w + 1) % 3];
       c1[r] = U.m[r][(w + 2) % 3];
@@ -1165,27 +1195,27 @@ __device__ void orthogonalize_u(M3& U, const M3& Fh) {
     c2[0] = c0[1] * c1[2] - c0[2] * c1[1];
     c2[1] = c0[2] * c1[0] - c0[0] * c1[2];
     c2[2] = c0[0] * c1[1] - c0[1] * c1[0];
-    double n = sqrt(c2[0] * c2[0] + (c2[1] * c2[1] + c2[2] * c2[2]));
-    if (n > 0)
+    T n = sqrt(c2[0] * c2[0] + (c2[1] * c2[1] + c2[2] * c2[2]));
+    if (n > T(0))
       for (int r = 0; r < 3; r++) c2[r] /= n;
     for (int r = 0; r < 3; r++) U.m[r][w] = c2[r];
-    if (signU * m3_det(U) < 0.0)
+    if (signU * m3_det(U) < T(0))
       for (int r = 0; r < 3; r++) U.m[r][w] = -c2[r];
     return;
   }
   if (total == 2) {
     int wv = !inv[2] ? 2 : (!inv[1] ? 1 : 0);
-    double v[3] = {U.m[0][wv], U.m[1][wv], U.m[2][wv]};
+    T v[3] = {U.m[0][wv], U.m[1][wv], U.m[2][wv]};
     int sm = (fabs(v[0]) < fabs(v[1])) ? 0 : 1;
     sm = (fabs(v[2]) < fabs(v[sm])) ? 2 : sm;
-    double sv[3];
+    T sv[3];
     int nx = (sm + 1) % 3, nn = (sm + 2) % 3;
-    sv[sm] = 0.0;
+    sv[sm] = T(0);
     sv[nx] = -v[nn];
     sv[nn] = v[nx];
-    double tv[3] = {v[1] * sv[2] - v[2] * sv[1], v[2] * sv[0] - v[0] * sv[2], v[0] * sv[1] - v[1] * sv[0]};
-    double n = sqrt(tv[0] * tv[0] + (tv[1] * tv[1] + tv[2] * tv[2]));
-    if (n > 0)
+    T tv[3] = {v[1] * sv[2] - v[2] * sv[1], v[2] * sv[0] - v[0] * sv[2], v[0] * sv[1] - v[1] * sv[0]};
+    T n = sqrt(tv[0] * tv[0] + (tv[1] * tv[1] + tv[2] * tv[2]));
+    if (n > T(0))
       for (int r = 0; r < 3; r++) tv[r] /= n;
     nx = (wv + 1) % 3;
     nn = (wv + 2) % 3;
@@ -1193,7 +1223,7 @@ __device__ void orthogonalize_u(M3& U, const M3& Fh) {
       U.m[r][nx] = sv[r];
       U.m[r][nn] = tv[r];
     }
-    if (signU * m3_det(U) < 0.0) {
+    if (signU * m3_det(U) < T(0)) {
       if (Fh.m[nx][nx] < Fh.m[nn][nn])
         for (int r = 0; r < 3; r++) U.m[r][nx] = -sv[r];
       else
@@ -1201,75 +1231,76 @@ __device__ void orthogonalize_u(M3& U, const M3& Fh) {
     }
     return;
   }
-  U = m3_id();
+  U = m3_id<T>();
 }
 
 // COROTATION::init -> decomposeF -> svd (COROTATION.cpp:37-39, 91-107, 235-280)
-__device__ void corot_init(Corot& c, const M3& F) {
-  M3 FtF = m3_mul_at(F, F);
-  double w[3];
-  M3 V;
-  sym_eig3(FtF, w, V);
-  M3 Fh;
+template <class T>
+__device__ void corot_init(CorotT<T>& c, const M3T<T>& F) {
+  M3T<T> FtF = m3_mul_at(F, F);
+  M3T<T> V;
+  sym_eig3(FtF, c.w, V);
+  M3T<T> Fh;
   for (int i = 0; i < 3; i++)
-    for (int j = 0; j < 3; j++) Fh.m[i][j] = 0.0;
+    for (int j = 0; j < 3; j++) Fh.m[i][j] = T(0);
   for (int i = 0; i < 3; i++) {
-    Fh.m[i][i] = sqrt(w[i]);
-    if (isnan(Fh.m[i][i])) Fh.m[i][i] = 0.0;
+    Fh.m[i][i] = sqrt(c.w[i]);
+    if (isnan(Fh.m[i][i])) Fh.m[i][i] = T(0);
   }
-  if (m3_det(V) < 0.0)
-    for (int r = 0; r < 3; r++) V.m[r][0] *= -1.0;
-  M3 D;
+  if (m3_det(V) < T(0))
+    for (int r = 0; r < 3; r++) V.m[r][0] *= T(-1);
+  M3T<T> D;
   for (int i = 0; i < 3; i++)
-    for (int j = 0; j < 3; j++) D.m[i][j] = 0.0;
-  for (int i = 0; i < 3; i++) D.m[i][i] = (Fh.m[i][i] > 0.0) ? 1.0 / Fh.m[i][i] : 0.0;
-  M3 U = m3_mul(m3_mul(F, V), D);
+    for (int j = 0; j < 3; j++) D.m[i][j] = T(0);
+  for (int i = 0; i < 3; i++) D.m[i][i] = (Fh.m[i][i] > T(0)) ? T(1) / Fh.m[i][i] : T(0);
+  M3T<T> U = m3_mul(m3_mul(F, V), D);
   orthogonalize_u(U, Fh);
-  if (m3_det(F) < 0.0) {
+  if (m3_det(F) < T(0)) {
     int sm = (Fh.m[0][0] < Fh.m[1][1]) ? 0 : 1;
     sm = (Fh.m[sm][sm] < Fh.m[2][2]) ? sm : 2;
-    Fh.m[sm][sm] *= -1.0;
-    for (int r = 0; r < 3; r++) U.m[r][sm] *= -1.0;
+    Fh.m[sm][sm] *= T(-1);
+    for (int r = 0; r < 3; r++) U.m[r][sm] *= T(-1);
   }
   c.R = m3_mul_bt(U, V);
   c.S = m3_mul_bt(m3_mul(V, Fh), V);
   c.V = V;
   c.Fh = Fh;
-  double trF = sum3(Fh.m[0][0], Fh.m[1][1], Fh.m[2][2]);
-  double trFm1 = sum3(Fh.m[0][0] - 1.0, Fh.m[1][1] - 1.0, Fh.m[2][2] - 1.0);
-  M3 T;
+  T trF = sum3(Fh.m[0][0], Fh.m[1][1], Fh.m[2][2]);
+  T trFm1 = sum3(Fh.m[0][0] - T(1), Fh.m[1][1] - T(1), Fh.m[2][2] - T(1));
+  M3T<T> Tm;
   for (int i = 0; i < 3; i++)
-    for (int j = 0; j < 3; j++) T.m[i][j] = (i == j ? trF : 0.0) - Fh.m[i][j];
-  M3 Ti = m3_inv(T);
-  double k = c.lambda * trFm1 - 2.0 * c.mu;
-  M3 Ld;
+    for (int j = 0; j < 3; j++) Tm.m[i][j] = (i == j ? trF : T(0)) - Fh.m[i][j];
+  M3T<T> Ti = m3_inv(Tm);
+  T k = c.lambda * trFm1 - T(2) * c.mu;
+  M3T<T> Ld;
   for (int i = 0; i < 3; i++)
-    for (int j = 0; j < 3; j++) Ld.m[i][j] = (i == j ? c.mu : 0.0) + k * Ti.m[i][j];
-  for (int i = 0; i < 3; i++) Ld.m[i][i] = Ld.m[i][i] > 0 ? Ld.m[i][i] : 0;
+    for (int j = 0; j < 3; j++) Ld.m[i][j] = (i == j ? c.mu : T(0)) + k * Ti.m[i][j];
+  for (int i = 0; i < 3; i++) Ld.m[i][i] = Ld.m[i][i] > T(0) ? Ld.m[i][i] : T(0);
   c.L = m3_mul_bt(m3_mul(V, Ld), V);
 }
 
 // COROTATION::firstPKDifferential (COROTATION.cpp:64-84) for dF = e_j (x) gf
 // (row j of dF is gf): the 24 columns of the element stiffness
 // (DEFOR_SOLID_3D.cpp:805-827).
-__device__ M3 corot_dpk_row(const Corot& c, int j, const double* gf) {
-  M3 dFh;  // R^T dF
+template <class T>
+__device__ M3T<T> corot_dpk_row(const CorotT<T>& c, int j, const T* gf) {
+  M3T<T> dFh;  // R^T dF
   for (int a = 0; a < 3; a++)
     for (int b = 0; b < 3; b++) dFh.m[a][b] = c.R.m[j][a] * gf[b];
-  M3 sym, skew;
+  M3T<T> sym, skew;
   for (int a = 0; a < 3; a++)
     for (int b = 0; b < 3; b++) {
-      sym.m[a][b] = 0.5 * (dFh.m[a][b] + dFh.m[b][a]);
-      skew.m[a][b] = 0.5 * (dFh.m[a][b] - dFh.m[b][a]);
+      sym.m[a][b] = T(0.5) * (dFh.m[a][b] + dFh.m[b][a]);
+      skew.m[a][b] = T(0.5) * (dFh.m[a][b] - dFh.m[b][a]);
     }
-  double trs = sum3(sym.m[0][0], sym.m[1][1], sym.m[2][2]);
-  M3 dP;
+  T trs = sum3(sym.m[0][0], sym.m[1][1], sym.m[2][2]);
+  M3T<T> dP;
   for (int a = 0; a < 3; a++)
-    for (int b = 0; b < 3; b++) dP.m[a][b] = (2.0 * c.mu * sym.m[a][b]) + (a == b ? c.lambda * trs : 0.0);
-  double f[3] = {-skew.m[1][2] + skew.m[2][1], -skew.m[2][0] + skew.m[0][2], -skew.m[0][1] + skew.m[1][0]};
-  double tr = c.lambda * sum3(dFh.m[0][0], dFh.m[1][1], dFh.m[2][2]);
+    for (int b = 0; b < 3; b++) dP.m[a][b] = (T(2) * c.mu * sym.m[a][b]) + (a == b ? c.lambda * trs : T(0));
+  T f[3] = {-skew.m[1][2] + skew.m[2][1], -skew.m[2][0] + skew.m[0][2], -skew.m[0][1] + skew.m[1][0]};
+  T tr = c.lambda * sum3(dFh.m[0][0], dFh.m[1][1], dFh.m[2][2]);
   for (int a = 0; a < 3; a++) dP.m[a][a] += tr;
-  double Lf[3];
+  T Lf[3];
   for (int a = 0; a < 3; a++) Lf[a] = (c.L.m[a][0] * f[0] + c.L.m[a][1] * f[1]) + c.L.m[a][2] * f[2];
   dP.m[0][1] += -Lf[2];
   dP.m[0][2] += Lf[1];
@@ -1312,13 +1343,19 @@ __global__ void k_fp_apply(const int* upd, const double* val, long long nc, cons
   }
 }
 
+// slotOf/ncDev (both NULL on the reference's path): entry t of `cells` is
+// the valid cell of ordinal slotOf[t], and only the first *ncDev entries are
+// used (the FP32 kernel's FP64 fallback list, below).
 __global__ void k_element_stiffness(GridDev g, SolidDev s, const long long* cells, long long nc,
-                                    double* Ke, double* nf, double* energyPart) {
+                                    double* Ke, double* nf, double* energyPart,
+                                    const long long* slotOf, const unsigned* ncDev) {
   double dh = g.dh;
   double e = 0;
   const long long off[8] = {0, 1, g.X, g.X + 1, g.slab, g.slab + 1, g.slab + g.X, g.slab + g.X + 1};
-  FOR_N(nc, t) {
-    long long n = cells[t];
+  if (ncDev) nc = *ncDev;
+  FOR_N(nc, tt) {
+    const long long t = slotOf ? slotOf[tt] : tt;
+    long long n = cells[tt];
     M3 F;
     double Jinv = 1.0 / compute_F(g, s.u, n, s.G, F);
     Corot c;
@@ -1425,6 +1462,196 @@ __global__ void k_element_stiffness(GridDev g, SolidDev s, const long long* cell
     double a = 0;
     for (int w = 0; w < (int)blockDim.x / 32; w++) a += sh[w];
     energyPart[blockIdx.x] = a;
+  }
+}
+
+
+// Mixed precision: the stress evaluation and element stiffness of
+// k_element_stiffness in FP32 (F from the displacements in FP64, then the
+// polar decomposition, PK1, forces, energy and the 24x24 stiffness in FP32).
+// A cell whose F is near-degenerate (cond(F) = sqrt(w_max / w_min) > 1e3 from
+// the eigenvalues w of F^T F, or w_min = 0) is not evaluated here: it is
+// appended to a list that k_element_stiffness then evaluates in FP64, the
+// reference's arithmetic. Elastic solids only (plastic ones use the FP64
+// kernel throughout).
+__global__ void k_element_stiffness_f32(GridDev g, SolidDev s, const long long* cells, long long nc,
+                                        double* Ke, double* nf, double* energyPart, long long* fbCells,
+                                        long long* fbSlot, unsigned* fbCount) {
+  const float dh = (float)g.dh;
+  double e = 0;
+  const long long off[8] = {0, 1, g.X, g.X + 1, g.slab, g.slab + 1, g.slab + g.X, g.slab + g.X + 1};
+  FOR_N(nc, t) {
+    long long n = cells[t];
+    M3 Fd;
+    const double Jinvd = 1.0 / compute_F(g, s.u, n, s.G, Fd);
+    M3T<float> F;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) F.m[i][j] = (float)Fd.m[i][j];
+    const float Jinv = (float)Jinvd;
+    CorotT<float> c;
+    c.lambda = (float)s.lambda;
+    c.mu = (float)s.mu;
+    corot_init(c, F);
+    if (!(c.w[2] > 0.0f) || c.w[0] > 1e6f * c.w[2]) {
+      const unsigned k = atomicAdd(fbCount, 1u);
+      fbCells[k] = n;
+      fbSlot[k] = t;
+      continue;
+    }
+    M3T<float> E = c.S;
+    for (int i = 0; i < 3; i++) E.m[i][i] -= 1.0f;
+    M3T<float> tmp;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) tmp.m[i][j] = 2.0f * c.mu * E.m[i][j];
+    const float trE = sum3(E.m[0][0], E.m[1][1], E.m[2][2]);
+    for (int i = 0; i < 3; i++) tmp.m[i][i] += c.lambda * trE;
+    const M3T<float> P = m3_mul(c.R, tmp);
+    M3T<float> JP;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) JP.m[i][j] = Jinv * P.m[i][j];
+    const M3T<float> cs = m3_mul_bt(JP, F);
+    const float G = (float)s.G;
+    float GF[8][3];
+    for (int i = 0; i < 8; i++) {
+      const float gi[3] = {(float)sgnx(i) * G, (float)sgny(i) * G, (float)sgnz(i) * G};
+      for (int j = 0; j < 3; j++) GF[i][j] = (gi[0] * F.m[0][j] + gi[1] * F.m[1][j]) + gi[2] * F.m[2][j];
+    }
+    const float dh3 = dh * dh * dh;
+    double* nft = nf + 24 * t;
+    for (int r = 0; r < 3; r++)
+      for (int m = 0; m < 8; m++) {
+        const float gm[3] = {(float)sgnx(m) * G, (float)sgny(m) * G, (float)sgnz(m) * G};
+        const float v = (cs.m[r][0] * gm[0] + cs.m[r][1] * gm[1]) + cs.m[r][2] * gm[2];
+        nft[r * 8 + m] = (double)(-(v * dh3));
+      }
+    const M3T<float> EtE = m3_mul_at(E, E);
+    e += (double)((c.mu * sum3(EtE.m[0][0], EtE.m[1][1], EtE.m[2][2]) + 0.5f * c.lambda * (trE * trE)) * dh3);
+    double* K = Ke + 576 * t;
+    const float scale = Jinv * dh3;
+    for (int k = 0; k < 24; k++) {
+      const int ci = k / 3, cj = k % 3;
+      const bool on = s.mass[n + off[ci]] != 0;
+      M3T<float> dP;
+      if (on) dP = corot_dpk_row(c, cj, GF[ci]);
+      for (int m = 0; m < 8; m++)
+        for (int r = 0; r < 3; r++) {
+          float v = 0.0f;
+          if (on) v = ((dP.m[r][0] * GF[m][0] + dP.m[r][1] * GF[m][1]) + dP.m[r][2] * GF[m][2]) * scale;
+          K[(m * 3 + r) * 24 + k] = (double)v;
+        }
+    }
+  }
+  __shared__ double sh[32];
+  for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = e;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0;
+    for (int w = 0; w < (int)blockDim.x / 32; w++) a += sh[w];
+    energyPart[blockIdx.x] = a;
+  }
+}
+
+// Mixed precision: semi-Lagrangian advection of the fluid velocity and of the
+// scalar intensity (k_advect_velocity / k_advect_scalar) in FP32 arithmetic
+// on the FP64 fields: the same backtrace, bisection into the fluid and
+// trilinear interpolation (FIELD_3D::get_barycentric's clamping).
+__device__ __forceinline__ void bary_f(float x, float dhInv, int ihigh, int& i, float& f) {
+  x *= dhInv;
+  const float s = floorf(x);
+  const int ii = (int)s;
+  if (ii < 0) {
+    i = 0;
+    f = 0.5f;
+  } else if (ii > ihigh) {
+    i = ihigh;
+    f = 0.5f;
+  } else {
+    i = ii;
+    f = x - s;
+  }
+}
+__device__ __forceinline__ float lerp_f(float a, float b, float f) { return (1.0f - f) * a + f * b; }
+__device__ __forceinline__ long long cell_f(const GridDev& g, const float* p, float o[3], float dhInv,
+                                            float fr[3]) {
+  int i, j, k;
+  bary_f(p[0] - o[0], dhInv, g.X - 2, i, fr[0]);
+  bary_f(p[1] - o[1], dhInv, g.Y - 2, j, fr[1]);
+  bary_f(p[2] - o[2], dhInv, g.Z - 2, k, fr[2]);
+  return i + (long long)j * g.X + k * g.slab;
+}
+__device__ __forceinline__ float interp1_f(const GridDev& g, const double* __restrict__ d, const float* p,
+                                           float o[3], float dhInv) {
+  float f[3];
+  const long long b = cell_f(g, p, o, dhInv, f), X = g.X, sl = g.slab;
+  const float a0 = lerp_f(lerp_f((float)d[b], (float)d[b + 1], f[0]),
+                          lerp_f((float)d[b + X], (float)d[b + X + 1], f[0]), f[1]);
+  const float a1 = lerp_f(lerp_f((float)d[b + sl], (float)d[b + sl + 1], f[0]),
+                          lerp_f((float)d[b + sl + X], (float)d[b + sl + X + 1], f[0]), f[1]);
+  return lerp_f(a0, a1, f[2]);
+}
+__device__ __forceinline__ void interp3_f(const GridDev& g, const double* __restrict__ d, const float* p,
+                                          float o[3], float dhInv, float out[3]) {
+  float f[3];
+  const long long b = cell_f(g, p, o, dhInv, f), X = g.X, sl = g.slab;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const double* e = d + c;
+    const float a0 = lerp_f(lerp_f((float)e[3 * b], (float)e[3 * (b + 1)], f[0]),
+                            lerp_f((float)e[3 * (b + X)], (float)e[3 * (b + X + 1)], f[0]), f[1]);
+    const float a1 = lerp_f(lerp_f((float)e[3 * (b + sl)], (float)e[3 * (b + sl + 1)], f[0]),
+                            lerp_f((float)e[3 * (b + sl + X)], (float)e[3 * (b + sl + X + 1)], f[0]), f[1]);
+    out[c] = lerp_f(a0, a1, f[2]);
+  }
+}
+__global__ void k_advect_velocity_f32(GridDev g, const double* solidMass, const double* vel, double* out,
+                                      double dtd) {
+  float o[3] = {(float)g.o[0], (float)g.o[1], (float)g.o[2]};
+  const float dh = (float)g.dh, dhInv = (float)g.dhInv, dt = (float)dtd;
+  FOR_N(g.T, n) {
+    int x = (int)(n % g.X), y = (int)((n / g.X) % g.Y), z = (int)(n / g.slab);
+    if (x < 1 || x > g.X - 2 || y < 1 || y > g.Y - 2 || z < 1 || z > g.Z - 2) continue;
+    if (solidMass[n] > 0) continue;
+    const float node[3] = {x * dh + o[0], y * dh + o[1], z * dh + o[2]};
+    float p[3], v[3], np[3], r[3];
+    for (int q = 0; q < 3; q++) p[q] = node[q] - 0.5f * (float)vel[3 * n + q] * dt;
+    interp3_f(g, vel, p, o, dhInv, v);
+    for (int q = 0; q < 3; q++) np[q] = node[q] - v[q] * dt;
+    float mass = interp1_f(g, solidMass, np, o, dhInv);
+    float newdt = dt / 2;
+    while (mass > 0.0f && newdt > dt / 16) {
+      for (int q = 0; q < 3; q++) np[q] += v[q] * newdt;
+      newdt /= 2;
+      mass = interp1_f(g, solidMass, np, o, dhInv);
+    }
+    interp3_f(g, vel, np, o, dhInv, r);
+    for (int q = 0; q < 3; q++) out[3 * n + q] = (double)r[q];
+  }
+}
+__global__ void k_advect_scalar_f32(GridDev g, const double* solidMass, const double* vel,
+                                    const double* field, double* out, double dtd) {
+  float o[3] = {(float)g.o[0], (float)g.o[1], (float)g.o[2]};
+  const float dh = (float)g.dh, dhInv = (float)g.dhInv, dt = (float)dtd;
+  FOR_N(g.T, n) {
+    int x = (int)(n % g.X), y = (int)((n / g.X) % g.Y), z = (int)(n / g.slab);
+    if (solidMass[n] > 0) {
+      out[n] = 0.0;
+      continue;
+    }
+    const float node[3] = {x * dh + o[0], y * dh + o[1], z * dh + o[2]};
+    float np[3], v[3];
+    for (int q = 0; q < 3; q++) {
+      v[q] = (float)vel[3 * n + q];
+      np[q] = node[q] - v[q] * dt;
+    }
+    float mass = interp1_f(g, solidMass, np, o, dhInv);
+    float newdt = dt / 2;
+    while (mass > 0.0f && newdt > dt / 16) {
+      for (int q = 0; q < 3; q++) np[q] += v[q] * newdt;
+      newdt /= 2;
+      mass = interp1_f(g, solidMass, np, o, dhInv);
+    }
+    out[n] = (double)interp1_f(g, field, np, o, dhInv);
   }
 }
 

@@ -143,6 +143,8 @@ struct esf_scene {
   long long S = 0;
   esf::DBuf sNode, solidF, solidMv, damped, solidV0, solidPC, solidB1, sysDiag, blocks, nbr, mask;
   esf::DBuf Ke, nf, energy;
+  esf::DBuf fbCells, fbSlot;  // mixed: near-degenerate cells for the FP64 stiffness
+  long long validCells = 0;
   // scratch
   esf::DBuf cubTmp, keys, vals, skeys, svals, bstart, bend, mt, pweights;
   long long mtLen = 0;
@@ -346,7 +348,7 @@ extern "C" esf_status esf_destroy(esf_scene* s) {
   if (s->hInts) cudaFreeHost(s->hInts);
   if (s->hU64) cudaFreeHost(s->hU64);
   DBuf* bufs[] = {&s->sNode, &s->solidF, &s->solidMv, &s->damped, &s->solidV0, &s->solidPC,
-                  &s->solidB1, &s->sysDiag, &s->blocks, &s->nbr, &s->mask, &s->Ke, &s->nf,
+                  &s->solidB1, &s->sysDiag, &s->blocks, &s->nbr, &s->mask, &s->Ke, &s->nf, &s->fbCells, &s->fbSlot,
                   &s->energy, &s->cubTmp, &s->keys, &s->vals, &s->skeys, &s->svals, &s->bstart,
                   &s->bend, &s->mt, &s->pweights};
   for (DBuf* b : bufs) b->release();
@@ -558,6 +560,7 @@ static esf_status compute_solid_mass(esf_scene* sc, Solid* d, int usesdf) {
 // grid barrier timed out raises the scene's sweep error word (dInts[42]),
 // checked when the step or init ends.
 constexpr int kSweepBar = 40, kSweepErr = 42;
+constexpr int kFallbackCount = 44;  // mixed: cells of the FP32 stiffness evaluated again in FP64
 template <bool VEC>
 static esf_status sweep_pass(esf_scene* sc, Solid* d, const Sweep& w, const unsigned long long* ranks) {
   cudaStream_t st = sc->stream;
@@ -845,8 +848,10 @@ static esf_status solid_system(esf_scene* sc, double* energyOut) {
   ESF_CUDA(cudaMemsetAsync(sc->damped.p, 0, 3 * S * 8 + 8, st));
   ESF_CUDA(cudaMemsetAsync(sc->mask.p, 0, S * 4 + 4, st));
   const int EB = 4096;
-  TRY(sc->energy.ensure(EB * 3 * 8));
-  ESF_CUDA(cudaMemsetAsync(sc->energy.p, 0, EB * 3 * 8, st));
+  // energy partials: stiffness, mass-weighted velocity, body forces, FP64
+  // fallback cells of the mixed path's FP32 stiffness
+  TRY(sc->energy.ensure(EB * 4 * 8));
+  ESF_CUDA(cudaMemsetAsync(sc->energy.p, 0, EB * 4 * 8, st));
   double* ePart = sc->energy.as<double>();
   // one solid: its valid-cell list is the one the particles were seeded from
   if (sc->ns != 1 && S > 0) {
@@ -857,6 +862,8 @@ static esf_status solid_system(esf_scene* sc, double* energyOut) {
     Solid* d = sc->s[i];
     ESF_CUDA(cudaMemsetAsync(sc->cellOrd, 0xff, G.R * 4, st));
     long long nc = d->nValid;
+    sc->validCells = nc;
+    sc->hInts[kFallbackCount] = 0;
     TRY(sc->Ke.ensure((576 * nc + 1) * 8));
     TRY(sc->nf.ensure((24 * nc + 1) * 8));
     if (nc > 0 && d->d.plastic) {
@@ -865,10 +872,25 @@ static esf_status solid_system(esf_scene* sc, double* energyOut) {
       d->d.updIdx = d->fpUpd.as<int>();
       d->d.updVal = d->fpVal.as<double>();
     }
-    if (nc > 0) {
+    if (nc > 0 && sc->p.precision == ESF_MIXED && !d->d.plastic) {
+      // stress and stiffness in FP32; near-degenerate cells again in FP64
+      TRY(sc->fbCells.ensure(nc * 8));
+      TRY(sc->fbSlot.ensure(nc * 8));
+      ESF_CUDA(cudaMemsetAsync(sc->dInts + kFallbackCount, 0, sizeof(int), st));
+      unsigned* fbCount = reinterpret_cast<unsigned*>(sc->dInts + kFallbackCount);
+      ESF_COUNTED k_element_stiffness_f32<<<kblocks(nc, 128), 128, 0, st>>>(
+          G, d->d, d->cellList.as<long long>(), nc, sc->Ke.as<double>(), sc->nf.as<double>(), ePart,
+          sc->fbCells.as<long long>(), sc->fbSlot.as<long long>(), fbCount);
+      ESF_COUNTED k_element_stiffness<<<kblocks(nc, 128), 128, 0, st>>>(
+          G, d->d, sc->fbCells.as<long long>(), nc, sc->Ke.as<double>(), sc->nf.as<double>(), ePart + 3 * EB,
+          sc->fbSlot.as<long long>(), fbCount);
+      ESF_CUDA(cudaMemcpyAsync(&sc->hInts[kFallbackCount], fbCount, sizeof(int), cudaMemcpyDeviceToHost, st));
+    } else if (nc > 0) {
       ESF_COUNTED k_element_stiffness<<<kblocks(nc, 128), 128, 0, st>>>(G, d->d, d->cellList.as<long long>(), nc,
                                                              sc->Ke.as<double>(), sc->nf.as<double>(),
-                                                             ePart);
+                                                             ePart, nullptr, nullptr);
+    }
+    if (nc > 0) {
       if (d->d.plastic) {
         ESF_CUDA(cudaMemsetAsync(d->fpWin.p, 0xff, d->pn * 4, st));
         ESF_COUNTED k_fp_winner<<<kblocks(nc), KT, 0, st>>>(d->d.updIdx, nc, d->fpWin.as<int>());
@@ -997,7 +1019,7 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
                                           sc->sysDiag.as<double>());
     ESF_LAUNCH_CHECK();
   }
-  double energy = sum_partials(sc, 3 * EB);
+  double energy = sum_partials(sc, 4 * EB);
   // ---- pcrImplicitSolve (:662-764)
   int it[3] = {0, 0, 0}, cv[3] = {0, 0, 0}, rf[3] = {0, 0, 0}, it64 = 0;
   double rr[3] = {0, 0, 0};
@@ -1197,9 +1219,17 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     tm.mark("gather solid masses");
   }
   ESF_CUDA(cudaEventRecord(sc->ph[12], st));
-  ESF_COUNTED k_advect_velocity<<<kblocks(G.T), KT, 0, st>>>(G, sc->solidMass, sc->vel, sc->vws, dt);
-  std::swap(sc->vel, sc->vws);
-  ESF_COUNTED k_advect_scalar<<<kblocks(G.T), KT, 0, st>>>(G, sc->solidMass, sc->vel, sc->intensity, sc->ws, dt);
+  // fluid velocity and intensity: FP32 arithmetic in mixed precision (the
+  // solid's material coordinates, which decide its cell flags, stay FP64)
+  if (prec == ESF_MIXED) {
+    ESF_COUNTED k_advect_velocity_f32<<<kblocks(G.T), KT, 0, st>>>(G, sc->solidMass, sc->vel, sc->vws, dt);
+    std::swap(sc->vel, sc->vws);
+    ESF_COUNTED k_advect_scalar_f32<<<kblocks(G.T), KT, 0, st>>>(G, sc->solidMass, sc->vel, sc->intensity, sc->ws, dt);
+  } else {
+    ESF_COUNTED k_advect_velocity<<<kblocks(G.T), KT, 0, st>>>(G, sc->solidMass, sc->vel, sc->vws, dt);
+    std::swap(sc->vel, sc->vws);
+    ESF_COUNTED k_advect_scalar<<<kblocks(G.T), KT, 0, st>>>(G, sc->solidMass, sc->vel, sc->intensity, sc->ws, dt);
+  }
   std::swap(sc->intensity, sc->ws);
   TRY(recover_velocity(sc));
   ESF_COUNTED k_dirichlet<<<kblocks(G.T), KT, 0, st>>>(G, sc->vel, sc->intensity);
@@ -1220,6 +1250,8 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     }
     rep->prone_to_contact = prone;
     rep->fp64_iterations = it64;
+    rep->fp64_stress_cells = prec == ESF_MIXED ? sc->hInts[kFallbackCount] : (int)sc->validCells;
+    rep->valid_cells = (int)sc->validCells;
     long long np = 0;
     for (int i = 0; i < sc->ns; i++) np += sc->s[i]->np;
     rep->num_particles = (int)np;

@@ -126,6 +126,9 @@ typedef struct esf_step_report {
    * grid, 8 velocity extension, 9 solid displacement update, 10 solid mass,
    * 11 surface mesh + SDF + particle seeding, 12 fluid advection + walls */
   double phase_ms[13];
+  int fp64_stress_cells;      /* mixed: valid cells whose stress was evaluated in FP64
+                                 (cond(F) > 1e3); the others use FP32 */
+  int valid_cells;            /* valid solid cells of the step's stiffness sweep */
 } esf_step_report;
 
 /* Field identifiers for esf_get_field / esf_set_field / esf_field_info. */

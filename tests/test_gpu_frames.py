@@ -107,7 +107,9 @@ def test_reads_reference_frame_and_steps_like_the_reference(tmp_path, gpu_lib):
     desc, z = _reference_frames(tmp_path)
     G = E.make_scene(desc)
     G.readFrame(0, debug=True, data_path=str(tmp_path) + "/")
-    fails = _compare(G.get, z, "r0.")
+    # (the pressure warm start is not part of a frame: the reference's is the
+    # static left by its last solve)
+    fails = _compare(G.get, z, "r0.", skip=("lambda1",))
     assert not fails, fails
     G.set("lambda1", z["r0.lambda1"])
     r = G.stepImplicit()
@@ -122,11 +124,11 @@ def test_reads_reference_frame_and_steps_like_the_reference(tmp_path, gpu_lib):
     G.close()
 
 
-def _compare(get, z, pre, tol=1e-6):
+def _compare(get, z, pre, tol=1e-6, skip=()):
     from common import EXACT, NAME, rel_err
     fails = []
     for k in z.files:
-        if not k.startswith(pre):
+        if not k.startswith(pre) or k[len(pre):] in skip:
             continue
         f = k[len(pre):]
         mine, ref = np.asarray(get(NAME[f])), z[k]
