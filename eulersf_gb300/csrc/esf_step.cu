@@ -144,6 +144,7 @@ struct esf_scene {
   esf::DBuf sNode, solidF, solidMv, damped, solidV0, solidPC, solidB1, sysDiag, blocks, nbr, mask;
   esf::DBuf Ke, nf, energy;
   esf::DBuf fbCells, fbSlot;  // mixed: near-degenerate cells for the FP64 stiffness
+  long long Sstep = 0;        // solid nodes of the last step's solid system
   long long validCells = 0;
   // scratch
   esf::DBuf cubTmp, keys, vals, skeys, svals, bstart, bend, mt, pweights;
@@ -833,6 +834,7 @@ static esf_status solid_system(esf_scene* sc, double* energyOut) {
   const GridDev& G = sc->g;
   cudaStream_t st = sc->stream;
   const long long S = sc->S;
+  sc->Sstep = S;
   TRY(sc->solidF.ensure((3 * S + 1) * 8));
   TRY(sc->solidMv.ensure((3 * S + 1) * 8));
   TRY(sc->damped.ensure((3 * S + 1) * 8));
@@ -1282,7 +1284,10 @@ struct FieldRef {
 
 static esf_status field_ref(esf_scene* s, int f, int si, FieldRef& r) {
   const GridDev& G = s->g;
-  const size_t T = G.T, R = G.R, D = 3ull * (G.X - 2) * (G.Y - 2) * (G.Z - 2), S3 = 3ull * s->S;
+  const size_t T = G.T, R = G.R, D = 3ull * (G.X - 2) * (G.Y - 2) * (G.Z - 2);
+  // the solid system of the last step is sized by the solid nodes it was
+  // assembled for (the step's closing mass update can change their count)
+  const size_t S3 = 3ull * s->Sstep;
   Solid* d = (si >= 0 && si < s->ns) ? s->s[si] : nullptr;
   switch (f) {
     case ESF_F_VELOCITY: r = {s->vel, T * 3, 8, 0, true}; return ESF_OK;
@@ -1304,8 +1309,8 @@ static esf_status field_ref(esf_scene* s, int f, int si, FieldRef& r) {
     case ESF_F_SOLID_PRESSURE_CORRECTION: r = {s->solidPC.p, S3, 8, 0, false}; return ESF_OK;
     case ESF_F_DAMPED_SOLID_MASS: r = {s->damped.p, S3, 8, 0, false}; return ESF_OK;
     case ESF_F_SYSTEM_DIAG: r = {s->sysDiag.p, S3, 8, 0, false}; return ESF_OK;
-    case ESF_F_SYSTEM_BLOCKS: r = {s->blocks.p, 243ull * s->S, 8, 5, false}; return ESF_OK;
-    case ESF_F_SYSTEM_MASK: r = {s->mask.p, (size_t)s->S, 4, 0, false}; return ESF_OK;
+    case ESF_F_SYSTEM_BLOCKS: r = {s->blocks.p, 243ull * s->Sstep, 8, 5, false}; return ESF_OK;
+    case ESF_F_SYSTEM_MASK: r = {s->mask.p, (size_t)s->Sstep, 4, 0, false}; return ESF_OK;
     default: break;
   }
   if (!d) {
@@ -1378,7 +1383,7 @@ extern "C" esf_status esf_get_field(esf_scene* s, esf_field f, int si, void* hos
     return ESF_OK;
   }
   if (r.kind == 5) {  // system blocks: device entry-major -> [node][27][3][3]
-    const long long S = s->S;
+    const long long S = s->Sstep;
     std::vector<double> tmp(243 * rows32(S));
     if (S) ESF_CUDA(cudaMemcpy(tmp.data(), r.dev, tmp.size() * 8, cudaMemcpyDeviceToHost));
     double* o = (double*)host;
