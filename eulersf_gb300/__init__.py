@@ -26,7 +26,7 @@ EXPORTS = [
     "esf_pressure_solve", "esf_pressure_solve_batch", "esf_pressure_solve_static", "esf_write_frame", "esf_read_frame", "esf_kernel_launches",
     "esf_time_pressure_kernels", "esf_scene_footprint", "esf_server_create", "esf_server_submit",
     "esf_server_poll", "esf_server_wait", "esf_server_get_field", "esf_server_release",
-    "esf_server_destroy", "esf_server_batch_stats", "esf_selftest_bounded_wait",
+    "esf_server_destroy", "esf_server_batch_stats", "esf_selftest_bounded_wait", "esf_rasterize_solid",
 ]
 
 
@@ -66,6 +66,9 @@ def load(build_if_missing: bool = False) -> C.CDLL:
     from . import serve as _serve
     _serve.declare(lib)
     lib.esf_read_frame.argtypes = [vp, C.c_char_p, C.c_int, C.c_int]
+    lib.esf_rasterize_solid.argtypes = [vp, C.c_int, vp, C.c_int, C.c_double, C.c_double,
+                                        C.POINTER(C.c_int), C.POINTER(C.c_double), vp, C.c_size_t,
+                                        C.POINTER(C.c_double)]
     lib.esf_selftest_bounded_wait.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]
     _lib = lib
     return lib

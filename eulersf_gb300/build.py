@@ -5,6 +5,7 @@ Three translation units, compiled in parallel:
   esf_step.cu    every other kernel and the C ABI, -fmad=false so flags, maps
                  and particle seeding keep the reference's non-FMA arithmetic
   esf_config.cpp the cfg reader
+  esf_bake.cu    offline mass baking of a solid's rest mass from its mesh
   esf_io.cpp     frame files (gz fields, OBJ); zlib is loaded at run time
   esf_serve.cpp  the multi-scene server (host threads, one stream per scene)
 Host code is compiled with -ffp-contract=off for the same reason (the box's
@@ -36,6 +37,7 @@ def _sources():
     return {
         "esf_solver.cu": ["-O3", "-lineinfo"],
         "esf_step.cu": ["-O3", "-lineinfo", "-fmad=false"],
+        "esf_bake.cu": ["-O3", "-lineinfo"],
         "esf_config.cpp": ["-O2"],
         "esf_io.cpp": ["-O2"],
         "esf_serve.cpp": ["-O2"],

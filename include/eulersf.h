@@ -298,6 +298,23 @@ esf_status esf_pressure_solve_static(const esf_grid* grid, const double* mass_in
  * NULL) is the kernel's device time. The context stays usable afterwards. */
 esf_status esf_selftest_bounded_wait(int kind, int* gave_up, double* elapsed_ms);
 
+/* Offline mass baking (projects/rasterizeSolid/main.cpp:20-80, the
+ * reference's rasterizeSolid tool) on the GPU: the rest-pose mass grid of a
+ * solid from its closed triangle mesh (num_vertices x 3 doubles,
+ * num_triangles x 3 vertex indices, 0-based, host memory). The grid is the
+ * mesh's bounding box grown by 10 cells on every side, res[k] = (int)(extent
+ * / mass_dh), origin = the grown box's minimum; a node carries `density`
+ * where its signed distance to the surface is at most mass_dh / 2. The
+ * reference reads that distance from a DT-Grid narrow-band SDF (.svol);
+ * here it is the exact distance to the triangles, signed by the winding
+ * number, so nodes within the SDF's interpolation error of the threshold can
+ * differ. Call with mass = NULL to get res and origin; then with a host
+ * buffer of res[0]*res[1]*res[2] doubles (x fastest). total_mass (may be
+ * NULL) = nodes with mass x density x mass_dh^3, as the tool prints. */
+esf_status esf_rasterize_solid(const double* vertices, int num_vertices, const int* triangles,
+                               int num_triangles, double mass_dh, double density, int res[3],
+                               double origin[3], double* mass, size_t capacity, double* total_mass);
+
 /* ---- serving: many scenes on one GPU -------------------------------------
  * No reference counterpart: the reference runs one scene per process (its
  * function-local statics pin one grid size per process). Requests arrive at

@@ -17,9 +17,12 @@ fields at every solid node:
 
     python tests/golden/make_golden.py --big config1_64 config2_128 [--keep DIR]
 
-and the reference's own frame files with a restart from them (``run_frame``):
+and the reference's own frame files with a restart from them (``run_frame``),
+and its offline mass baking of the shipped sphere (``run_mass``,
+``make -C oracle rasterize`` first):
 
     python tests/golden/make_golden.py --frame
+    python tests/golden/make_golden.py --mass
 
 ``--keep DIR`` keeps the harness's raw dumps there and reuses a completed run.
 """
@@ -166,6 +169,48 @@ def run_frame(out_dir):
         shutil.rmtree(tmp, ignore_errors=True)
 
 
+# Mass baking: the reference's rasterizeSolid tool on its shipped sphere
+# (meshes/sphere/sphere.obj and its DT-Grid SDF sphere.svol, cfg/sphere.cfg's
+# mass dh 0.001 and density 1000). The fixture holds the mesh (vertices,
+# 0-based triangles) and the baked grid (resolution, dh, origin, density and
+# the nodes that carry mass as a bit mask).
+RASTERIZE = os.path.join(ROOT, "oracle", "_ref", "rasterize_solid")
+
+
+def read_obj(path):
+    """Vertices and 0-based triangles of an OBJ ("f a/b/c ..." entries)."""
+    verts, tris = [], []
+    for line in open(path):
+        t = line.split()
+        if not t:
+            continue
+        if t[0] == "v":
+            verts.append([float(x) for x in t[1:4]])
+        elif t[0] == "f":
+            tris.append([int(x.split("/")[0]) - 1 for x in t[1:4]])
+    return np.array(verts, dtype=np.float64), np.array(tris, dtype=np.int32)
+
+
+def run_mass(out_dir):
+    from eulersf_gb300.scene import read_field_gz
+    ref = os.environ.get("EULERSF_REFERENCE", "/root/reference")
+    obj, svol = os.path.join(ref, "meshes/sphere/sphere.obj"), os.path.join(ref, "meshes/sphere/sphere.svol")
+    tmp = tempfile.mkdtemp(prefix="esf_golden_")
+    try:
+        cfg = os.path.join(tmp, "sphere.cfg")
+        with open(cfg, "w") as f:
+            f.write(f"mesh file name = {obj}\nsdf file name = {svol}\n"
+                    f"mass file name = {tmp}/sphere.mass\nsolid mass density = 1000\nmass dh = 0.001\n")
+        subprocess.run([RASTERIZE, cfg], check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        res, dh, origin, data = read_field_gz(os.path.join(tmp, "sphere.mass"))
+        verts, tris = read_obj(obj)
+        np.savez_compressed(os.path.join(out_dir, "sphere_mass.npz"), vertices=verts, triangles=tris,
+                            res=np.array(res), dh=np.array(dh), origin=np.array(origin), density=np.array(1000.0),
+                            solid=np.packbits(data.reshape(-1) > 0), total=np.array(float(data.sum()) * dh ** 3))
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+
+
 def big_scenes():
     """The rubber-ball scene at the benchmark's 64^3 and 128^3 sizes; the
     fluid-noise seed is 0 for both. The mass sample spacing divides dh by a
@@ -285,6 +330,10 @@ def main():
         return
     if not os.path.exists(HARNESS):
         sys.exit(f"{HARNESS} missing: build it with make -C oracle")
+    if args == ["--mass"]:
+        run_mass(HERE)
+        print("sphere_mass", os.path.getsize(os.path.join(HERE, "sphere_mass.npz")), "bytes")
+        return
     if args == ["--frame"]:
         run_frame(HERE)
         print(FRAME_SCENE[0], os.path.getsize(os.path.join(HERE, FRAME_SCENE[0] + ".npz")), "bytes")

@@ -1,0 +1,37 @@
+"""Offline mass baking on the GPU (esf_rasterize_solid) against the
+reference's rasterizeSolid tool on its shipped sphere (tests/golden/
+sphere_mass.npz: the mesh and the grid the tool baked from its DT-Grid SDF).
+
+The grid (resolution, spacing, origin) is the reference's exactly. The nodes
+that carry mass differ only where the reference's interpolated narrow-band
+SDF and the exact distance to the triangles fall on different sides of the
+dh/2 threshold: a thin shell, bounded here, and far thinner than the
+difference between the reference's grid and an exact sphere's.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from common import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+def test_baked_mass_matches_the_reference_tool(gpu_lib):
+    from eulersf_gb300.bake import rasterize_solid
+    z = np.load(os.path.join(GOLDEN, "sphere_mass.npz"))
+    res, dh, origin, mass, total = rasterize_solid(z["vertices"], z["triangles"], float(z["dh"]),
+                                                   float(z["density"]))
+    assert tuple(res) == tuple(z["res"]) and dh == float(z["dh"])
+    assert np.array_equal(np.array(origin), z["origin"])
+    ref = np.unpackbits(z["solid"])[: mass.size].astype(bool)
+    mine = mass.reshape(-1) > 0
+    assert np.all(mass.reshape(-1)[mine] == float(z["density"]))
+    differ = int(np.count_nonzero(mine != ref))
+    # the exact sphere of the mesh's radius rasterised the same way differs
+    # from the reference's grid at 80,420 nodes (the boundary shell)
+    print(f"baked vs reference: {differ} of {int(ref.sum())} solid nodes differ; "
+          f"total mass {total:.6f} vs {float(z['total']):.6f}")
+    assert differ <= 0.01 * ref.sum()
+    assert abs(total - float(z["total"])) <= 0.005 * float(z["total"])
