@@ -23,7 +23,7 @@ EXPORTS = [
     "esf_abi_version", "esf_last_error", "esf_params_default", "esf_parse_config", "esf_create",
     "esf_destroy", "esf_add_solid", "esf_set_fluid", "esf_init", "esf_set_max_dt", "esf_step",
     "esf_dt", "esf_field_info", "esf_get_field", "esf_set_field", "esf_pressure_apply",
-    "esf_pressure_solve", "esf_pressure_solve_batch", "esf_pressure_solve_static", "esf_write_frame", "esf_read_frame", "esf_kernel_launches",
+    "esf_pressure_solve", "esf_pressure_solve_batch", "esf_pressure_solve_static", "esf_write_frame", "esf_read_frame", "esf_write_frame_async", "esf_frame_wait", "esf_kernel_launches",
     "esf_time_pressure_kernels", "esf_scene_footprint", "esf_server_create", "esf_server_submit",
     "esf_server_poll", "esf_server_wait", "esf_server_get_field", "esf_server_release",
     "esf_server_destroy", "esf_server_batch_stats", "esf_selftest_bounded_wait", "esf_rasterize_solid",
@@ -66,6 +66,8 @@ def load(build_if_missing: bool = False) -> C.CDLL:
     from . import serve as _serve
     _serve.declare(lib)
     lib.esf_read_frame.argtypes = [vp, C.c_char_p, C.c_int, C.c_int]
+    lib.esf_write_frame_async.argtypes = [vp, C.c_char_p, C.c_int, C.c_int]
+    lib.esf_frame_wait.argtypes = [vp]
     lib.esf_rasterize_solid.argtypes = [vp, C.c_int, vp, C.c_int, C.c_double, C.c_double,
                                         C.POINTER(C.c_int), C.POINTER(C.c_double), vp, C.c_size_t,
                                         C.POINTER(C.c_double)]

@@ -145,6 +145,12 @@ struct esf_scene {
   esf::DBuf Ke, nf, energy;
   esf::DBuf fbCells, fbSlot;  // mixed: near-degenerate cells for the FP64 stiffness
   long long Sstep = 0;        // solid nodes of the last step's solid system
+  // asynchronous frame writing (esf_write_frame_async)
+  double* framePinned = nullptr;
+  size_t frameWords = 0;
+  cudaEvent_t frameEv = nullptr;
+  std::thread frameThread;
+  int frameStatus = 0;
   long long validCells = 0;
   // scratch
   esf::DBuf cubTmp, keys, vals, skeys, svals, bstart, bend, mt, pweights;
@@ -337,8 +343,13 @@ static void free_solid(Solid* d) {
   delete d;
 }
 
+extern "C" esf_status esf_frame_wait(esf_scene* s);
+
 extern "C" esf_status esf_destroy(esf_scene* s) {
   if (!s) return ESF_OK;
+  esf_frame_wait(s);
+  if (s->framePinned) cudaFreeHost(s->framePinned);
+  if (s->frameEv) cudaEventDestroy(s->frameEv);
   if (s->stream) cudaStreamSynchronize(s->stream);
   for (int i = 0; i < s->ns; i++) free_solid(s->s[i]);
   double* d64[] = {s->vel, s->vws, s->vort, s->intensity, s->ws, s->solidMass, s->nodeVF, s->quarter,
@@ -1637,6 +1648,57 @@ extern "C" esf_status esf_selftest_bounded_wait(int kind, int* gave_up, double* 
 // "frame.NNNN.solid.i" + .displacement/.velocity/.phi (every 10th frame or
 // debug) and .obj (always); the fluid .velocity (every 10th frame or debug)
 // and .intensity (always). The .pbrt render export is not written.
+// A frame's content in host memory: per solid its displacement, velocity,
+// phi, FpInv (row-major, plastic solids) and mesh vertices; the grid velocity,
+// the pressure warm start and the intensity. Fields a partial frame (not
+// every 10th, not debug) does not write may be null.
+namespace {
+struct FrameSnap {
+  bool full = false;
+  std::vector<const double*> u, vel, phi, fp, verts;
+  const double *gridVel = nullptr, *lambda = nullptr, *intensity = nullptr;
+};
+}  // namespace
+
+// The files of COUPLED_INTEGRATOR_3D::writeFrame (COUPLED_INTEGRATOR_3D.cpp:
+// 997-1012) and DEFOR_SOLID_3D::writeFrame (DEFOR_SOLID_3D.cpp:1362-1370)
+// from a snapshot.
+static esf_status write_frame_files(esf_scene* s, const FrameSnap& f, const std::string& base) {
+  const GridDev& G = s->g;
+  const int res[3] = {G.X, G.Y, G.Z};
+  for (int i = 0; i < s->ns; i++) {
+    Solid* d = s->s[i];
+    const std::string fn = base + ".solid." + std::to_string(i);
+    if (f.full) {
+      TRY(write_field_gz(fn + ".displacement", res, G.dh, G.o, f.u[i], G.T * 3));
+      TRY(write_field_gz(fn + ".velocity", res, G.dh, G.o, f.vel[i], G.T * 3));
+      TRY(write_field_gz(fn + ".phi", res, G.dh, G.o, f.phi[i], G.T));
+      if (d->d.plastic) {
+        // MATRIX3_FIELD_3D::writeGz: 9 doubles per cell, column-major
+        std::vector<double> cm((size_t)d->pn * 9);
+        const double* fp = f.fp[i];
+        for (long long c = 0; c < d->pn; c++)
+          for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) cm[9 * c + 3 * b + a] = fp[9 * c + 3 * a + b];
+        TRY(write_field_gz(fn + ".plasticdefor", d->d.pres, d->d.pdh, d->d.porig, cm.data(), cm.size()));
+      }
+    }
+    TRY(write_obj(fn + ".obj", f.verts[i], d->nv, d->tris.data(), d->ntri));
+  }
+  if (f.full) {
+    TRY(write_field_gz(base + ".velocity", res, G.dh, G.o, f.gridVel, G.T * 3));
+    // extension: the pressure warm start, which the reference keeps in a
+    // function-local static and never writes; a cell field (cell centres)
+    const int cres[3] = {G.cX, G.cY, G.cZ};
+    const double corig[3] = {G.o[0] + 0.5 * G.dh, G.o[1] + 0.5 * G.dh, G.o[2] + 0.5 * G.dh};
+    TRY(write_field_gz(base + ".lambda1", cres, G.dh, corig, f.lambda, G.R));
+  }
+  TRY(write_field_gz(base + ".intensity", res, G.dh, G.o, f.intensity, G.T));
+  return ESF_OK;
+}
+
+extern "C" esf_status esf_frame_wait(esf_scene* s);
+
 extern "C" esf_status esf_write_frame(esf_scene* s, const char* path, int frame, int debug) {
   if (!s || !path) {
     set_error("esf_write_frame: invalid argument");
@@ -1646,48 +1708,117 @@ extern "C" esf_status esf_write_frame(esf_scene* s, const char* path, int frame,
     set_error("esf_write_frame: scene not initialised");
     return ESF_ERR_STATE;
   }
+  TRY(esf_frame_wait(s));  // an asynchronous frame still being written goes first
   const GridDev& G = s->g;
-  const int res[3] = {G.X, G.Y, G.Z};
-  const bool full = debug || (frame % 10 == 0);
-  const std::string base = frame_prefix(path, frame);
-  std::vector<double> buf((size_t)G.T * 3);
+  FrameSnap f;
+  f.full = debug || (frame % 10 == 0);
+  std::vector<std::vector<double>> keep;
+  auto get = [&](esf_field id, int si, size_t n) -> const double* {
+    keep.emplace_back(n);
+    return esf_get_field(s, id, si, keep.back().data(), n * 8) == ESF_OK ? keep.back().data() : nullptr;
+  };
+  keep.reserve(8 + 6 * s->ns);
   for (int i = 0; i < s->ns; i++) {
     Solid* d = s->s[i];
-    const std::string fn = base + ".solid." + std::to_string(i);
-    if (full) {
-      TRY(esf_get_field(s, ESF_F_S_U, i, buf.data(), G.T * 24));
-      TRY(write_field_gz(fn + ".displacement", res, G.dh, G.o, buf.data(), G.T * 3));
-      TRY(esf_get_field(s, ESF_F_S_VELOCITY, i, buf.data(), G.T * 24));
-      TRY(write_field_gz(fn + ".velocity", res, G.dh, G.o, buf.data(), G.T * 3));
-      TRY(esf_get_field(s, ESF_F_S_PHI, i, buf.data(), G.T * 8));
-      TRY(write_field_gz(fn + ".phi", res, G.dh, G.o, buf.data(), G.T));
-      if (d->d.plastic) {
-        // MATRIX3_FIELD_3D::writeGz: 9 doubles per cell, column-major
-        std::vector<double> fp((size_t)d->pn * 9), cm((size_t)d->pn * 9);
-        TRY(esf_get_field(s, ESF_F_S_FPINV, i, fp.data(), fp.size() * 8));
-        for (long long c = 0; c < d->pn; c++)
-          for (int a = 0; a < 3; a++)
-            for (int b = 0; b < 3; b++) cm[9 * c + 3 * b + a] = fp[9 * c + 3 * a + b];
-        TRY(write_field_gz(fn + ".plasticdefor", d->d.pres, d->d.pdh, d->d.porig, cm.data(), cm.size()));
-      }
-    }
-    std::vector<double> v((size_t)d->nv * 3);
-    TRY(esf_get_field(s, ESF_F_S_MESH_VERTICES, i, v.data(), v.size() * 8));
-    TRY(write_obj(fn + ".obj", v.data(), d->nv, d->tris.data(), d->ntri));
+    f.u.push_back(f.full ? get(ESF_F_S_U, i, G.T * 3) : nullptr);
+    f.vel.push_back(f.full ? get(ESF_F_S_VELOCITY, i, G.T * 3) : nullptr);
+    f.phi.push_back(f.full ? get(ESF_F_S_PHI, i, G.T) : nullptr);
+    f.fp.push_back(f.full && d->d.plastic ? get(ESF_F_S_FPINV, i, (size_t)d->pn * 9) : nullptr);
+    f.verts.push_back(get(ESF_F_S_MESH_VERTICES, i, (size_t)d->nv * 3));
+    if ((f.full && (!f.u.back() || !f.vel.back() || !f.phi.back() || (d->d.plastic && !f.fp.back()))) ||
+        !f.verts.back())
+      return ESF_ERR_CUDA;
   }
+  if (f.full && (!(f.gridVel = get(ESF_F_VELOCITY, 0, G.T * 3)) || !(f.lambda = get(ESF_F_PRESSURE, 0, G.R))))
+    return ESF_ERR_CUDA;
+  if (!(f.intensity = get(ESF_F_INTENSITY, 0, G.T))) return ESF_ERR_CUDA;
+  return write_frame_files(s, f, frame_prefix(path, frame));
+}
+
+// Asynchronous frame: the fields are copied on the scene's stream into pinned
+// host memory, behind the work queued so far, and a host thread compresses
+// and writes the files once the copies have landed, while the caller goes on
+// stepping. One frame is in flight per scene: the next call (or
+// esf_write_frame, esf_read_frame, esf_destroy) first waits for it;
+// esf_frame_wait returns its status.
+extern "C" esf_status esf_write_frame_async(esf_scene* s, const char* path, int frame, int debug) {
+  if (!s || !path) {
+    set_error("esf_write_frame_async: invalid argument");
+    return ESF_ERR_INVALID_ARG;
+  }
+  if (!s->inited) {
+    set_error("esf_write_frame_async: scene not initialised");
+    return ESF_ERR_STATE;
+  }
+  TRY(esf_frame_wait(s));
+  cudaSetDevice(s->device);
+  const GridDev& G = s->g;
+  const bool full = debug || (frame % 10 == 0);
+  // pinned snapshot: [grid velocity | lambda | intensity | per solid u, vel, phi, FpInv, vertices]
+  size_t words = (full ? G.T * 3 + G.R : 0) + G.T;
+  for (int i = 0; i < s->ns; i++) {
+    Solid* d = s->s[i];
+    words += (full ? G.T * 7 + (d->d.plastic ? (size_t)d->pn * 9 : 0) : 0) + (size_t)d->nv * 3;
+  }
+  if (s->frameWords < words) {
+    if (s->framePinned) cudaFreeHost(s->framePinned);
+    s->framePinned = nullptr;
+    s->frameWords = 0;
+    ESF_CUDA(cudaMallocHost(&s->framePinned, words * 8));
+    s->frameWords = words;
+  }
+  if (!s->frameEv) ESF_CUDA(cudaEventCreateWithFlags(&s->frameEv, cudaEventDisableTiming));
+  cudaStream_t st = s->stream;
+  double* h = s->framePinned;
+  auto copy = [&](const double* dev, size_t n) -> const double* {
+    const double* at = h;
+    if (cudaMemcpyAsync(h, dev, n * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess) return nullptr;
+    h += n;
+    return at;
+  };
+  FrameSnap f;
+  f.full = full;
+  bool ok = true;
   if (full) {
-    TRY(esf_get_field(s, ESF_F_VELOCITY, 0, buf.data(), G.T * 24));
-    TRY(write_field_gz(base + ".velocity", res, G.dh, G.o, buf.data(), G.T * 3));
-    // extension: the pressure warm start, which the reference keeps in a
-    // function-local static and never writes; a cell field (cell centres)
-    const int cres[3] = {G.cX, G.cY, G.cZ};
-    const double corig[3] = {G.o[0] + 0.5 * G.dh, G.o[1] + 0.5 * G.dh, G.o[2] + 0.5 * G.dh};
-    TRY(esf_get_field(s, ESF_F_PRESSURE, 0, buf.data(), G.R * 8));
-    TRY(write_field_gz(base + ".lambda1", cres, G.dh, corig, buf.data(), G.R));
+    ok = ok && (f.gridVel = copy(s->vel, G.T * 3)) && (f.lambda = copy(s->lambda, G.R));
   }
-  TRY(esf_get_field(s, ESF_F_INTENSITY, 0, buf.data(), G.T * 8));
-  TRY(write_field_gz(base + ".intensity", res, G.dh, G.o, buf.data(), G.T));
+  ok = ok && (f.intensity = copy(s->intensity, G.T));
+  for (int i = 0; i < s->ns && ok; i++) {
+    Solid* d = s->s[i];
+    const double *u = nullptr, *v = nullptr, *ph = nullptr, *fp = nullptr, *vx = nullptr;
+    if (full) {
+      ok = (u = copy(d->d.u, G.T * 3)) && (v = copy(d->d.vel, G.T * 3)) && (ph = copy(d->d.phi, G.T));
+      if (ok && d->d.plastic) ok = (fp = copy(d->d.FpInv, (size_t)d->pn * 9)) != nullptr;
+    }
+    ok = ok && (vx = copy(d->dVerts, (size_t)d->nv * 3));
+    f.u.push_back(u);
+    f.vel.push_back(v);
+    f.phi.push_back(ph);
+    f.fp.push_back(fp);
+    f.verts.push_back(vx);
+  }
+  if (!ok || cudaEventRecord(s->frameEv, st) != cudaSuccess) {
+    set_error("esf_write_frame_async: %s", cudaGetErrorString(cudaGetLastError()));
+    cudaStreamSynchronize(st);
+    return ESF_ERR_CUDA;
+  }
+  const std::string base = frame_prefix(path, frame);
+  const int dev = s->device;
+  s->frameStatus = ESF_OK;
+  s->frameThread = std::thread([s, f, base, dev] {
+    cudaSetDevice(dev);
+    s->frameStatus = cudaEventSynchronize(s->frameEv) == cudaSuccess ? write_frame_files(s, f, base)
+                                                                      : ESF_ERR_CUDA;
+  });
   return ESF_OK;
+}
+
+extern "C" esf_status esf_frame_wait(esf_scene* s) {
+  if (!s) return ESF_ERR_INVALID_ARG;
+  if (s->frameThread.joinable()) s->frameThread.join();
+  const esf_status e = (esf_status)s->frameStatus;
+  s->frameStatus = ESF_OK;
+  return e;
 }
 
 // COUPLED_INTEGRATOR_3D::readFrame (COUPLED_INTEGRATOR_3D.cpp:977-996) with
@@ -1707,6 +1838,7 @@ extern "C" esf_status esf_read_frame(esf_scene* s, const char* path, int frame, 
     set_error("esf_read_frame: scene not initialised");
     return ESF_ERR_STATE;
   }
+  TRY(esf_frame_wait(s));
   cudaSetDevice(s->device);
   const GridDev& G = s->g;
   cudaStream_t st = s->stream;

@@ -113,6 +113,14 @@ class CoupledIntegrator3D:
         """COUPLED_INTEGRATOR_3D::writeFrame: files "<data_path>frame.NNNN.*"."""
         self._call("write_frame", self._h, data_path.encode(), int(frame), int(bool(debug)))
 
+    def writeFrameAsync(self, frame: int, debug: bool = False, data_path: str = ""):
+        """writeFrame through pinned memory and a writer thread; returns at once
+        (esf_write_frame_async). frameWait() waits for it."""
+        self._call("write_frame_async", self._h, data_path.encode(), int(frame), int(bool(debug)))
+
+    def frameWait(self):
+        self._call("frame_wait", self._h)
+
     def readFrame(self, frame: int, debug: bool = False, data_path: str = ""):
         """COUPLED_INTEGRATOR_3D::readFrame of files written by writeFrame (or the reference)."""
         self._call("read_frame", self._h, data_path.encode(), int(frame), int(bool(debug)))

@@ -420,6 +420,15 @@ esf_status esf_time_pressure_kernels(esf_scene* scene, int reps, double* update_
  * ESF_ERR_IO on a missing or mismatched file. */
 esf_status esf_write_frame(esf_scene* scene, const char* data_path, int frame, int debug);
 esf_status esf_read_frame(esf_scene* scene, const char* data_path, int frame, int debug);
+/* Asynchronous esf_write_frame: the frame's fields are copied on the scene's
+ * stream into pinned host memory, behind the work queued so far, and a host
+ * thread compresses and writes the same files once the copies have landed,
+ * while the caller goes on stepping (the reference writes its frames
+ * synchronously). One frame in flight per scene: the next asynchronous or
+ * synchronous write, a read, or esf_destroy first waits for it;
+ * esf_frame_wait waits and returns its status. */
+esf_status esf_write_frame_async(esf_scene* scene, const char* data_path, int frame, int debug);
+esf_status esf_frame_wait(esf_scene* scene);
 
 #ifdef __cplusplus
 }

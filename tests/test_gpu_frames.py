@@ -168,3 +168,29 @@ def test_written_frame_is_the_reference_frame(tmp_path, gpu_lib):
         else:
             assert gzip.decompress(mine) == gzip.decompress(ref), n
     G.close()
+
+
+def test_asynchronous_frame_is_the_synchronous_frame(tmp_path, gpu_lib):
+    """esf_write_frame_async snapshots the state when it is called: stepping on
+    at once does not change what it writes, which is what esf_write_frame
+    writes (gz fields decompressing to the same bytes, the same OBJ)."""
+    import gzip
+    import eulersf_gb300 as E
+    a, b = tmp_path / "sync", tmp_path / "async"
+    a.mkdir()
+    b.mkdir()
+    G = E.make_scene(DESC)
+    G.stepImplicit()
+    G.writeFrame(0, data_path=str(a) + "/")
+    G.writeFrameAsync(0, data_path=str(b) + "/")
+    G.stepImplicit()  # the state moves on while the frame is written
+    G.frameWait()
+    names = sorted(os.listdir(a))
+    assert names == sorted(os.listdir(b)) and len(names) >= 7
+    for n in names:
+        x, y = (a / n).read_bytes(), (b / n).read_bytes()
+        if n.endswith(".obj"):
+            assert x == y, n
+        else:
+            assert gzip.decompress(x) == gzip.decompress(y), n
+    G.close()
