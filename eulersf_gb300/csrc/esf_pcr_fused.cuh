@@ -96,16 +96,13 @@ __device__ __forceinline__ void finish_fused(PcrState* st, double dl, double mu,
   }
 }
 
-// One block's share of a pass over the scene (g, tm, p, partial, st): the
-// span [u0, u1) of cell layers in column-major order, layer z of the 64 x
-// 8-cell column c (c = bx + gx by) being unit c cZ + z. A span can run into
-// the next column; each column's run is z-marched on its own (its own halo
-// layers), the sums accumulating over the whole span. The pass has nb
-// blocks; bid is this block's place among them (the order in which the last
-// block folds the partial sums).
+// One block's share of a pass: the 64 x 8-cell column (bx, by) over the cell
+// layers bz*cz .. bz*cz+cz-1 of the scene (g, tm, p, partial, st), whose
+// pass has nb blocks; bid is this block's place among them (the order in
+// which the last block folds the partial sums).
 __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm, const FusedPtrs& p,
-                                           double* partial, PcrState* st, long long u0, long long u1,
-                                           int gx, int nb, int bid, unsigned char* smem) {
+                                           double* partial, PcrState* st, int cz, int bx, int by,
+                                           int bz, int nb, int bid, unsigned char* smem) {
   unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem + FU_OFF_BAR);
   float* sP = reinterpret_cast<float*>(smem + FU_OFF_P);
   float* sQ = reinterpret_cast<float*>(smem + FU_OFF_SQ);
@@ -122,20 +119,18 @@ __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm
   const int pin = st->pp & 1, pout = pin ^ 1;
   const float alpha = (float)st->alpha, beta = (float)st->beta;
   const int tid = threadIdx.x;
-  // the current column run: cells x0.., y0.., layers z0 .. z1-1, marched as
-  // nsteps = z1 - z0 + 2 layer steps (z0-1 .. z1); g0 counts the steps of the
-  // earlier runs, so stage slots and mbarrier phases follow the global step
-  int x0 = 0, y0 = 0, z0 = 0, z1 = 0, nsteps = 0;
-  int g0 = 0;
+  const int x0 = bx * TXW, y0 = by * TY, z0 = bz * cz;
+  const int z1 = min(z0 + cz, g.cZ);
+  const int nsteps = z1 - z0 + 2;  // cell layers z0-1 .. z1
 
   const CUtensorMap* mR = pin ? &tm.r[1] : &tm.r[0];
   const CUtensorMap* mT = pin ? &tm.t[1] : &tm.t[0];
   const CUtensorMap* mQ = pin ? &tm.q[1] : &tm.q[0];
-  auto stage = [&](int gi) { return smem + (gi % TMA_STAGES) * FU_STAGE_BYTES; };
+  auto stage = [&](int i) { return smem + (i % TMA_STAGES) * FU_STAGE_BYTES; };
   auto issue = [&](int i) {
     const int kk = z0 - 1 + i;
-    unsigned char* s = stage(g0 + i);
-    unsigned long long* b = &bar[(g0 + i) % TMA_STAGES];
+    unsigned char* s = stage(i);
+    unsigned long long* b = &bar[i % TMA_STAGES];
     const bool own = kk >= z0 && kk < z1;
     const bool node = kk >= z0;
     mbar_expect_tx(b, 3 * TMA_HALO_BYTES + (own ? 3 * TMA_OWN_BYTES : 0) + (node ? TMA_NODE_BYTES : 0));
@@ -152,13 +147,15 @@ __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm
   if (tid == 0) {
     for (int i = 0; i < TMA_STAGES; i++) mbar_init(&bar[i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    for (int i = 0; i < TMA_STAGES && i < nsteps; i++) issue(i);
   }
+  __syncthreads();
 
   const int lane = tid & 31, w = tid >> 5;
   const int cx = 2 * lane;
-  int cgx = 0, cgy = 0;
-  bool cin = false;
-  long long ccol = 0;
+  const int cgx = x0 + cx, cgy = y0 + w;
+  const bool cin = cgx < g.cX && cgy < g.cY;  // cX is a multiple of 4
+  const long long ccol = cgx + (long long)cgy * g.cX;
   const int bM = (cx + 4) + (w + 1) * TMA_HW;
   const int pM = (cx + 2) + (w + 1) * TW_PP;
   const int oM = cx + w * TXW;                  // own pair in the 64 x 8 boxes
@@ -187,39 +184,19 @@ __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm
   float* qOut = pout ? p.q[1] : p.q[0];
   float* tOut = pout ? p.t[1] : p.t[0];
   float sDl = 0, sMu = 0, sNu = 0, sOm = 0;
-  bool ok = true;
-  int landed = 0, issued = 0;  // global steps whose copies have landed / been issued
-  for (long long u = u0; u < u1 && ok;) {
-  {
-    const long long c = u / g.cZ;
-    z0 = (int)(u - c * g.cZ);
-    z1 = (int)min((long long)g.cZ, z0 + (u1 - u));
-    u += z1 - z0;
-    x0 = (int)(c % gx) * TXW;
-    y0 = (int)(c / gx) * TY;
-    nsteps = z1 - z0 + 2;
-    cgx = x0 + cx;
-    cgy = y0 + w;
-    cin = cgx < g.cX && cgy < g.cY;  // cX is a multiple of 4
-    ccol = cgx + (long long)cgy * g.cX;
-    // the previous run's last layer has been read by every thread
-    __syncthreads();
-    if (tid == 0) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      for (int i = 0; i < TMA_STAGES && i < nsteps; i++) issue(i);
-      issued = g0 + (TMA_STAGES < nsteps ? TMA_STAGES : nsteps);
-    }
-  }
   float prev0 = 0, prev1 = 0, prevE = 0, vOwn0 = 0, vOwn1 = 0;
   float qCur0 = 0, qCur1 = 0, ivCur0 = 0, ivCur1 = 0;
   float mpx0 = 0, mpy0 = 0, mpz0 = 0, mpx1 = 0, mpy1 = 0, mpz1 = 0, mpxE = 0, mpyE = 0, mpzE = 0;
+  bool ok = true;
+  int landed = 0;
+  int issued = TMA_STAGES < nsteps ? TMA_STAGES : nsteps;
   for (int i = 0; i < nsteps; i++) {
     const int kk = z0 - 1 + i;
     if (ok) {
-      ok = mbar_wait(&bar[(g0 + i) % TMA_STAGES], (unsigned)((g0 + i) / TMA_STAGES) & 1u);
-      if (ok) landed = g0 + i + 1;
+      ok = mbar_wait(&bar[i % TMA_STAGES], (unsigned)(i / TMA_STAGES) & 1u);
+      if (ok) landed = i + 1;
     }
-    const unsigned char* s = stage(g0 + i);
+    const unsigned char* s = stage(i);
     const float* R = reinterpret_cast<const float*>(s + FU_OFF_R);
     const float* Tt = reinterpret_cast<const float*>(s + FU_OFF_T);
     const float* Qq = reinterpret_cast<const float*>(s + FU_OFF_Q);
@@ -310,7 +287,7 @@ __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm
     if (tid == 0 && ok && i + TMA_STAGES < nsteps) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       issue(i + TMA_STAGES);
-      issued = g0 + i + TMA_STAGES + 1;
+      issued = i + TMA_STAGES + 1;
     }
     // (c) s' and t' = s'/diag at the tile's cells of layer kk-1
     if (kk >= z0 + 1 && cin) {
@@ -341,11 +318,7 @@ __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm
       sNu += o0 * qPrev0 + o1 * qPrev1;
     }
   }
-  g0 += nsteps;
-  ok = !__syncthreads_or(!ok);
-  }
-  if (!ok) {
-    __syncthreads();
+  if (__syncthreads_or(!ok)) {
     if (tid == 0) {
       st->status = ESF_ERR_CUDA;
       st->done = 1;
@@ -384,13 +357,12 @@ __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm
 }
 
 __global__ void __launch_bounds__(NT, 4) pcr_iteration_fused(GridDev g, const __grid_constant__ FusedMaps tm,
-                                                             FusedPtrs p, double* partial, PcrState* st) {
+                                                             FusedPtrs p, double* partial, PcrState* st,
+                                                             int cz) {
   extern __shared__ __align__(128) unsigned char smem[];
-  // spans of equal length over the column-major layer sequence, one per block
-  const int gx = (g.cX + TXW - 1) / TXW, gy = (g.cY + TY - 1) / TY;
-  const long long U = (long long)gx * gy * g.cZ, B = gridDim.x;
-  fused_pass(g, tm, p, partial, st, blockIdx.x * U / B, (blockIdx.x + 1) * U / B, gx, (int)B,
-             (int)blockIdx.x, smem);
+  fused_pass(g, tm, p, partial, st, cz, blockIdx.x, blockIdx.y, blockIdx.z,
+             gridDim.x * gridDim.y * gridDim.z,
+             blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z), smem);
 }
 
 // ---- several scenes' inner solves in one launch (continuous batching).
@@ -432,11 +404,8 @@ __global__ void __launch_bounds__(NT, 4) pcr_iteration_fused_batch(const FusedTa
   const int local = blk - b.first[lo];
   const int nb = t.gx * t.gy * t.gz;
   if (local >= nb) return;
-  // the single-column runs of the z-chunked shape (cz layers per block)
   const int bx = local % t.gx, by = (local / t.gx) % t.gy, bz = local / (t.gx * t.gy);
-  const long long c = bx + (long long)t.gx * by;
-  const int zA = bz * t.cz, zB = min(zA + t.cz, t.g.cZ);
-  fused_pass(t.g, t.tm, t.p, t.partial, t.st, c * t.g.cZ + zA, c * t.g.cZ + zB, t.gx, nb, local, smem);
+  fused_pass(t.g, t.tm, t.p, t.partial, t.st, t.cz, bx, by, bz, nb, local, smem);
 }
 
 // The states of a batch's tasks, in list order, for one copy to the host.

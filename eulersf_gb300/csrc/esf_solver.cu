@@ -709,26 +709,6 @@ static int fused_cz(const GridDev& g) {
   }
   return best;
 }
-// Blocks of a single scene's one-pass iteration: one wave (the SMs' resident
-// blocks) of equal spans over the column-major layer sequence, so no last
-// wave runs part-empty; spans of at least 4 layers, so a small scene gets
-// fewer blocks. ESF_FUSED_BLOCKS overrides the count, for tuning.
-static int fused_blocks(const GridDev& g) {
-  const long long U = (long long)((g.cX + TXW - 1) / TXW) * ((g.cY + TY - 1) / TY) * g.cZ;
-  const char* e = getenv("ESF_FUSED_BLOCKS");
-  if (e && atoi(e) >= 1) return (int)std::min<long long>(atoi(e), U);
-  static const int slots = [] {
-    int dev = 0, sms = 152, per = 4;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pcr_iteration_fused, NT, FU_SMEM) !=
-            cudaSuccess ||
-        per < 1)
-      per = 4;
-    return sms * per;
-  }();
-  return (int)std::max<long long>(1, std::min<long long>(slots, (U + 3) / 4));
-}
 template <typename T>
 static dim3 stencil_grid(const GridDev& g) {
   int cz = stencil_cz(g);
@@ -890,7 +870,7 @@ static esf_status prepare_tma(PressureWork* w, const GridDev& g, const double* m
   }
   *out = &w->tmaps;
   if (path) *path = P32_TMA;
-  const dim3 gr(fused_blocks(g), 1, 1);
+  const dim3 gr = tma_grid(g, fused_cz(g));
   const bool fits = (long long)gr.x * gr.y * gr.z * FU_SUMS <= ESF_MAX_PARTIALS / 2;
   if (!path || !fits || (pick && strcmp(pick, "tma") == 0)) return ESF_OK;
   if (!w->fusedOk) {
@@ -930,7 +910,8 @@ struct FusedKernels {
   double* partial;
   PcrState* st;
   void iteration(cudaStream_t cs) const {
-    ESF_COUNTED pcr_iteration_fused<<<fused_blocks(g), NT, FU_SMEM, cs>>>(g, *tm, p, partial, st);
+    const int cz = fused_cz(g);
+    ESF_COUNTED pcr_iteration_fused<<<tma_grid(g, cz), NT, FU_SMEM, cs>>>(g, *tm, p, partial, st, cz);
   }
   // graph capture interface of PressureKernels (inner solves only)
   void setup_warm(cudaStream_t) const {}
@@ -1158,7 +1139,7 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
   const FusedKernels kf = fused_kernels(w, g, w->st32);
   const void* key[8] = {w->minv32, w->invd32, w->b32, w->x32, tma, &w->fmaps,
                         reinterpret_cast<const void*>(static_cast<uintptr_t>(path + 1)),
-                        reinterpret_cast<const void*>(static_cast<uintptr_t>(fused_blocks(g)))};
+                        reinterpret_cast<const void*>(static_cast<uintptr_t>(fused_cz(g)))};
   if (!w->graphsFor32 || memcmp(key, w->keyB, sizeof key) != 0) {
     esf_status e = fused ? capture(w->capStream, kf, false, false, &w->gChunk32, &w->kChunk32)
                          : capture(w->capStream, k32, false, false, &w->gChunk32, &w->kChunk32);
