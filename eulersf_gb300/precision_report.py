@@ -6,6 +6,7 @@ solid displacement between the two trajectories, relative to the FP64
 field's max-norm.
 
     python -m eulersf_gb300.precision_report [--size 256] [--steps 6] [--seed 7]
+    python -m eulersf_gb300.precision_report --fp64-only --size 128 --steps 50 --seed 0
 
 Prints one JSON line per step and a summary line.
 """
@@ -26,6 +27,35 @@ def _linf(a, b):
     s = float(np.abs(b).max()) if b.size else 0.0
     d = float(np.abs(a - b).max()) if b.size else 0.0
     return d / s if s > 0 else d
+
+
+def run_fp64(size=128, steps=50, seed=0, mass_sample_dh=None, out=print):
+    """The plain FP64 path alone (the benchmark's plain-method configurations):
+    per step its device time, wall time and solver iterations, and a summary
+    of steps/s, cells/s and pressure iterations/s."""
+    import time
+    desc = SceneDesc(N=size, noise_seed=seed, mass_sample_dh=mass_sample_dh or (1.0 / size) / 4,
+                     solids=[SolidDesc(center=(0.5, 0.65, 0.5), radius=0.15, density=1100.0,
+                                       E=2e5, nu=0.45)])
+    A = make_scene(desc, precision=abi.ESF_FP64)
+    rows = []
+    for k in range(steps):
+        t0 = time.perf_counter()
+        r = A.stepImplicit()
+        rows.append({"step": k, "device_ms": r["device_ms"], "wall_ms": (time.perf_counter() - t0) * 1e3,
+                     "iterations": r["iterations"], "rel_residual": max(r["rel_residual"])})
+        out(json.dumps(rows[-1]))
+    A.close()
+    t = sum(r["device_ms"] for r in rows) * 1e-3
+    tw = sum(r["wall_ms"] for r in rows) * 1e-3
+    piters = sum(r["iterations"][1] for r in rows)
+    summary = {"summary": True, "precision": "fp64", "size": size, "steps": steps, "seed": seed,
+               "mass_sample_dh": desc.mass_sample_dh, "steps_per_s": steps / t, "wall_steps_per_s": steps / tw,
+               "cells_per_s": size ** 3 * steps / t, "pressure_iters_per_s": piters / t,
+               "pressure_iters_per_step": piters / steps,
+               "max_rel_residual": max(r["rel_residual"] for r in rows)}
+    out(json.dumps(summary))
+    return rows, summary
 
 
 def run(size=256, steps=6, seed=7, out=print):
@@ -68,8 +98,13 @@ def main(argv=None):
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--steps", type=int, default=6)
     ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--fp64-only", action="store_true", help="the plain FP64 path alone")
+    ap.add_argument("--mass-sample-dh", type=float, default=None)
     a = ap.parse_args(argv)
-    run(a.size, a.steps, a.seed)
+    if a.fp64_only:
+        run_fp64(a.size, a.steps, a.seed, a.mass_sample_dh)
+    else:
+        run(a.size, a.steps, a.seed)
     return 0
 
 
