@@ -206,5 +206,13 @@ long long solid_work_capacity(const SolidWork* w);
 esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const int* nbr,
                        const double* diag, const double* b, double* x, double eps, int maxIt,
                        int precision, double innerEps, int maxRefine, int* iters, double* relres,
-                       int* refinements, int* converged, cudaStream_t st);
+                       int* refinements, int* converged, cudaStream_t st, const double* damped = nullptr);
+// Mixed precision: the inner solves apply the stiffness matrix-free from the
+// valid cells' recorded corotation data (cell: 43 planes of nc floats;
+// corner: 8 planes of nc corner solid DOFs) instead of FP32 blocks; cell =
+// NULL turns it off. damped (the assembled diagonal's mass part) is then
+// passed to solid_solve.
+esf_status solid_work_set_matrix_free(SolidWork* w, const GridDev& g, long long nc, const float* cell,
+                                      const int* corner, const long long* sNode, const int* cellOrd,
+                                      double mu, double lambda, double scale);
 }  // namespace esf

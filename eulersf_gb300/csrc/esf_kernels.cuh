@@ -64,7 +64,15 @@ struct SolidDev {
   double* FpInv;    // 9 per material cell, row-major
   int* updIdx;      // per valid cell: material cell it updates, or -1
   double* updVal;   // per valid cell: the updated FpInv
+  // mixed precision: per valid cell, the data of the matrix-free FP32
+  // stiffness (MF_PLANES planes of nc floats: R, L, GF, Jinv dh^3), or null
+  float* mf;
+  long long mfCells;
 };
+// planes of the per-cell matrix-free data: R (row-major) 0-8, L 9-17, the
+// F-weighted corner gradients GF 18-41 (corner i, component b at 18+3i+b),
+// Jinv dh^3 at 42
+constexpr int MF_PLANES = 43;
 
 // --------------------------------------------------------- 3x3 helpers
 // Templated on the arithmetic type: double everywhere on the reference's
@@ -1426,6 +1434,17 @@ __global__ void k_element_stiffness(GridDev g, SolidDev s, const long long* cell
       double gi[3] = {sgnx(i) * s.G, sgny(i) * s.G, sgnz(i) * s.G};
       for (int j = 0; j < 3; j++) GF[i][j] = (gi[0] * F.m[0][j] + gi[1] * F.m[1][j]) + gi[2] * F.m[2][j];
     }
+    if (s.mf) {
+      float* q = s.mf + t;
+      const long long P = s.mfCells;
+      for (int i = 0; i < 9; i++) {
+        q[i * P] = (float)c.R.m[i / 3][i % 3];
+        q[(9 + i) * P] = (float)c.L.m[i / 3][i % 3];
+      }
+      for (int i = 0; i < 8; i++)
+        for (int b = 0; b < 3; b++) q[(18 + 3 * i + b) * P] = (float)GF[i][b];
+      q[42 * P] = (float)(((Jinv * dh) * dh) * dh);
+    }
     double* nft = nf + 24 * t;
     for (int r = 0; r < 3; r++)
       for (int m = 0; m < 8; m++) {
@@ -1517,6 +1536,17 @@ __global__ void k_element_stiffness_f32(GridDev g, SolidDev s, const long long* 
       for (int j = 0; j < 3; j++) GF[i][j] = (gi[0] * F.m[0][j] + gi[1] * F.m[1][j]) + gi[2] * F.m[2][j];
     }
     const float dh3 = dh * dh * dh;
+    if (s.mf) {
+      float* q = s.mf + t;
+      const long long P = s.mfCells;
+      for (int i = 0; i < 9; i++) {
+        q[i * P] = c.R.m[i / 3][i % 3];
+        q[(9 + i) * P] = c.L.m[i / 3][i % 3];
+      }
+      for (int i = 0; i < 8; i++)
+        for (int b = 0; b < 3; b++) q[(18 + 3 * i + b) * P] = GF[i][b];
+      q[42 * P] = Jinv * dh3;
+    }
     double* nft = nf + 24 * t;
     for (int r = 0; r < 3; r++)
       for (int m = 0; m < 8; m++) {
@@ -2014,3 +2044,14 @@ __global__ void k_dirichlet(GridDev g, double* vel, double* intensity) {
 }
 
 }  // namespace esf
+
+// ------------------------------------- matrix-free FP32 solid stiffness
+// The solid DOF of each corner of each valid cell (-1: not a solid node),
+// 8 planes of nc ints, for the matrix-free apply.
+__global__ void k_mf_corners(GridDev g, const long long* cells, long long nc, const int* sdof, int* ci) {
+  const long long off[8] = {0, 1, g.X, g.X + 1, g.slab, g.slab + 1, g.slab + g.X, g.slab + g.X + 1};
+  FOR_N(nc, t) {
+    const long long n = cells[t];
+    for (int i = 0; i < 8; i++) ci[i * nc + t] = sdof[n + off[i]];
+  }
+}

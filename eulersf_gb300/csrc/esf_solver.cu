@@ -1487,6 +1487,132 @@ __global__ void __launch_bounds__(VT) solid_spmv(long long S, const T* __restric
   }
 }
 
+// ---- matrix-free FP32 stiffness for the solid inner solves (mixed
+// precision). The assembled A_s = scale K + diag(damped mass) streams 27
+// 3x3 blocks a row (~1 KB); applied cell by cell instead, K x needs per valid
+// cell only the corotation R, L, the F-weighted corner gradients GF and
+// Jinv dh^3 (43 floats, recorded by the stiffness kernels) and the corners'
+// solid DOFs: the element's share for corner m is
+//   y_m = scale Jinv dh^3  dPK(dF) . GF_m,   dF = sum_i x_i (x) GF_i,
+// with dPK COROTATION::firstPKDifferential (COROTATION.cpp:64-84) as a
+// linear map of dF (the map whose value on e_j (x) gf is the stiffness
+// kernel's dPK row). Two kernels: one per valid cell writes its 24 shares,
+// one per solid node sums the shares of the (up to 8) valid cells around it
+// in a fixed order, adds the damped mass and forms the r.s partial of the
+// PCR update, as solid_spmv<S_UPDATE> does. The FP64 refinement keeps the
+// assembled FP64 matrix for its residual.
+struct SolidMF {
+  GridDev g;
+  long long nc;          // valid cells
+  const float* cell;     // MF_PLANES planes of nc floats
+  const int* corner;     // 8 planes of nc ints: corner solid DOFs
+  const long long* sNode;  // grid node of each solid DOF node
+  const int* cellOrd;    // cell -> valid ordinal, or -1
+  float mu, lambda, scale;
+};
+constexpr int MF_CELL_PLANES = 43;
+
+__global__ void __launch_bounds__(VT) k_mf_cell(SolidMF m, const float* __restrict__ x,
+                                                 float* __restrict__ share, const PcrState* st) {
+  if (st->done) return;
+  const long long nc = m.nc;
+  for (long long t = blockIdx.x * (long long)VT + threadIdx.x; t < nc; t += (long long)gridDim.x * VT) {
+    const float* q = m.cell + t;
+    float GF[8][3], dF[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      const int j = m.corner[i * nc + t];
+      float xi[3] = {0.0f, 0.0f, 0.0f};
+      if (j >= 0) {
+        xi[0] = x[3 * (long long)j];
+        xi[1] = x[3 * (long long)j + 1];
+        xi[2] = x[3 * (long long)j + 2];
+      }
+#pragma unroll
+      for (int b = 0; b < 3; b++) GF[i][b] = q[(18 + 3 * i + b) * nc];
+#pragma unroll
+      for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) dF[a][b] += xi[a] * GF[i][b];
+    }
+    float R[3][3], L[3][3];
+#pragma unroll
+    for (int i = 0; i < 9; i++) {
+      R[i / 3][i % 3] = q[i * nc];
+      L[i / 3][i % 3] = q[(9 + i) * nc];
+    }
+    // dPK(dF) = R (2 mu sym + lambda tr(sym) I + lambda tr(R^T dF) I + [L f]x),
+    // R^T dF = dFh, sym/skew of dFh, f the axial vector of the skew part
+    float h[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++) h[a][b] = (R[0][a] * dF[0][b] + R[1][a] * dF[1][b]) + R[2][a] * dF[2][b];
+    const float trh = h[0][0] + (h[1][1] + h[2][2]);
+    float P[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++) P[a][b] = m.mu * (h[a][b] + h[b][a]) + (a == b ? 2.0f * m.lambda * trh : 0.0f);
+    const float f[3] = {-0.5f * (h[1][2] - h[2][1]) + 0.5f * (h[2][1] - h[1][2]),
+                        -0.5f * (h[2][0] - h[0][2]) + 0.5f * (h[0][2] - h[2][0]),
+                        -0.5f * (h[0][1] - h[1][0]) + 0.5f * (h[1][0] - h[0][1])};
+    float Lf[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) Lf[a] = (L[a][0] * f[0] + L[a][1] * f[1]) + L[a][2] * f[2];
+    P[0][1] -= Lf[2];
+    P[0][2] += Lf[1];
+    P[1][0] += Lf[2];
+    P[1][2] -= Lf[0];
+    P[2][0] -= Lf[1];
+    P[2][1] += Lf[0];
+    float D[3][3];  // R P
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++) D[a][b] = (R[a][0] * P[0][b] + R[a][1] * P[1][b]) + R[a][2] * P[2][b];
+    const float w = q[42 * nc] * m.scale;
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+#pragma unroll
+      for (int r = 0; r < 3; r++)
+        share[(3 * i + r) * nc + t] = w * ((D[r][0] * GF[i][0] + D[r][1] * GF[i][1]) + D[r][2] * GF[i][2]);
+  }
+}
+
+__global__ void __launch_bounds__(VT) k_mf_gather(SolidMF m, long long S, const float* __restrict__ share,
+                                                   const float* __restrict__ damped, const float* in, float* out,
+                                                   double* partial, PcrState* st) {
+  __shared__ double sred[32];
+  if (st->done) return;
+  const GridDev& g = m.g;
+  float accT = 0;
+  for (long long a = blockIdx.x * (long long)VT + threadIdx.x; a < S; a += (long long)gridDim.x * VT) {
+    const long long n = m.sNode[a];
+    const int nx = (int)(n % g.X), ny = (int)((n / g.X) % g.Y), nz = (int)(n / g.slab);
+    float y[3] = {0.0f, 0.0f, 0.0f};
+    for (int ia = 7; ia >= 0; ia--) {  // the cells around the node, corner ia of each
+      const int cx = nx - (ia & 1), cy = ny - ((ia >> 1) & 1), cz = nz - ((ia >> 2) & 1);
+      if (cx < 0 || cy < 0 || cz < 0 || cx > g.X - 2 || cy > g.Y - 2 || cz > g.Z - 2) continue;
+      const int ord = m.cellOrd[cx + (long long)cy * g.cX + (long long)cz * g.cslab];
+      if (ord < 0) continue;
+#pragma unroll
+      for (int r = 0; r < 3; r++) y[r] += share[(3 * ia + r) * m.nc + ord];
+    }
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      const long long i = 3 * a + r;
+      y[r] += damped[i] * in[i];
+      out[i] = y[r];
+      accT += in[i] * y[r];
+    }
+  }
+  const double bs = block_sum<VT>((double)accT, sred);
+  double total;
+  if (last_block_sum<VT>(bs, partial, &st->ticket[1], gridDim.x, &total, sred) && threadIdx.x == 0)
+    finish_update(st, total);
+}
+
 // x += alpha d; r -= alpha Ap/diag (pointwise part of phase B).
 template <typename T>
 __global__ void __launch_bounds__(VT) pcr_update_xr(long long n, T* x, const T* d, T* r, const T* Ap,
@@ -1509,7 +1635,13 @@ struct SolidWork {
   cudaStream_t capStream;
   cudaGraphExec_t gFirst[2], gChunk[2];
   unsigned long long kFirst[2], kChunk[2];
-  const void* key[2][10];
+  const void* key[2][16];
+  // matrix-free FP32 operator of the inner solves (solid_work_set_matrix_free)
+  bool mfOn;
+  SolidMF mf;
+  float* mfShare;       // 24 planes of the valid cells
+  long long mfShareCap;
+  float* damped32;      // damped mass (the assembled diagonal's mass part), FP32
   double *r, *d, *Ap, *s, *invd, *partial;
   float *blocks32, *x32, *r32, *d32, *Ap32, *s32, *invd32, *b32;
   PcrState *st, *st32;
@@ -1566,7 +1698,38 @@ void solid_work_free(SolidWork* w) {
     if (w->gChunk[p]) cudaGraphExecDestroy(w->gChunk[p]);
   }
   if (w->capStream) cudaStreamDestroy(w->capStream);
+  cudaFree(w->mfShare);
+  cudaFree(w->damped32);
   delete w;
+}
+
+esf_status solid_work_set_matrix_free(SolidWork* w, const GridDev& g, long long nc, const float* cell,
+                                      const int* corner, const long long* sNode, const int* cellOrd,
+                                      double mu, double lambda, double scale) {
+  if (!w) return ESF_ERR_STATE;
+  if (!cell) {
+    w->mfOn = false;
+    return ESF_OK;
+  }
+  if (w->mfShareCap < nc) {
+    cudaFree(w->mfShare);
+    w->mfShare = nullptr;
+    w->mfShareCap = 0;
+    ESF_CUDA(cudaMalloc(&w->mfShare, (size_t)24 * (nc + nc / 4 + 16) * 4));
+    w->mfShareCap = nc + nc / 4 + 16;
+  }
+  if (!w->damped32) ESF_CUDA(cudaMalloc(&w->damped32, (size_t)3 * w->cap * 4));
+  w->mf.g = g;
+  w->mf.nc = nc;
+  w->mf.cell = cell;
+  w->mf.corner = corner;
+  w->mf.sNode = sNode;
+  w->mf.cellOrd = cellOrd;
+  w->mf.mu = (float)mu;
+  w->mf.lambda = (float)lambda;
+  w->mf.scale = (float)scale;
+  w->mfOn = nc > 0;
+  return ESF_OK;
 }
 
 // The assembled-matrix PCR (CONJUGATE_RESIDUAL.inl:194-276) of the solid
@@ -1580,11 +1743,26 @@ struct SolidKernels {
   T *x, *r, *d, *Ap, *s;
   double* partial;
   PcrState* st;
+  // FP32 inner solves: the matrix-free operator instead of the blocks
+  const SolidMF* mf = nullptr;
+  float* share = nullptr;
+  const float* damped = nullptr;
+  // s = A r with the r.s partial of the PCR update
+  void apply_update(cudaStream_t cs) const {
+    if constexpr (std::is_same<T, float>::value) {
+      if (mf) {
+        ESF_COUNTED k_mf_cell<<<vec_blocks(mf->nc), VT, 0, cs>>>(*mf, r, share, st);
+        ESF_COUNTED k_mf_gather<<<vec_blocks(S), VT, 0, cs>>>(*mf, S, share, damped, r, s, partial, st);
+        return;
+      }
+    }
+    ESF_COUNTED solid_spmv<T, S_UPDATE><<<vec_blocks(S), VT, 0, cs>>>(S, blocks, nbr, r, nullptr, nullptr, s,
+                                                                      nullptr, partial, st);
+  }
   void setup_zero(cudaStream_t cs) const {
     const long long n = 3 * S;
     ESF_COUNTED pcr_zero_start<T><<<vec_blocks(n), VT, 0, cs>>>(n, b, invd, x, r, d, Ap, partial, st);
-    ESF_COUNTED solid_spmv<T, S_UPDATE><<<vec_blocks(S), VT, 0, cs>>>(S, blocks, nbr, r, nullptr, nullptr, s,
-                                                                      nullptr, partial, st);
+    apply_update(cs);
   }
   void chunk(cudaStream_t cs, int n_it, bool check) const {
     const long long n = 3 * S;
@@ -1592,8 +1770,7 @@ struct SolidKernels {
     for (int k = 0; k < n_it; k++) {
       ESF_COUNTED pcr_phase_a<T, false><<<vb, VT, 0, cs>>>(n, d, r, Ap, s, invd, partial, st);
       ESF_COUNTED pcr_update_xr<T><<<vb, VT, 0, cs>>>(n, x, d, r, Ap, invd, st);
-      ESF_COUNTED solid_spmv<T, S_UPDATE><<<sb, VT, 0, cs>>>(S, blocks, nbr, r, nullptr, nullptr, s, nullptr,
-                                                             partial, st);
+      apply_update(cs);
     }
     if (check)
       ESF_COUNTED solid_spmv<T, S_CHECK><<<sb, VT, 0, cs>>>(S, blocks, nbr, x, b, nullptr, nullptr, nullptr,
@@ -1633,8 +1810,24 @@ static esf_status solid_pcr_graph(SolidWork* w, int slot, long long S, const T* 
                                   PcrState* dst, double eps, int maxIt, cudaStream_t st, PcrState* out,
                                   int inner) {
   SolidKernels<T> k{S, blocks, invd, b, nbr, x, r, d, Ap, s, w->partial, dst};
-  const void* key[10] = {(const void*)(intptr_t)S, blocks, nbr, invd, b, x, r, d, dst,
-                         (const void*)(intptr_t)inner};
+  const bool mf = std::is_same<T, float>::value && w->mfOn;
+  if (mf) {
+    k.mf = &w->mf;
+    k.share = w->mfShare;
+    k.damped = w->damped32;
+  }
+  // the captured graphs hold every pointer and scalar of their launches
+  uint64_t mfBits = 0;
+  if (mf) {
+    const float sc[3] = {w->mf.scale, w->mf.mu, w->mf.lambda};
+    uint32_t u[3];
+    memcpy(u, sc, sizeof u);
+    mfBits = ((uint64_t)u[0] << 32) ^ ((uint64_t)u[1] * 2654435761u) ^ (uint64_t)u[2] ^ (uint64_t)w->mf.nc << 1;
+  }
+  const void* key[16] = {(const void*)(intptr_t)S, blocks, nbr, invd, b, x, r, d, dst,
+                         (const void*)(intptr_t)inner, mf ? w->mf.cell : nullptr, mf ? w->mf.corner : nullptr,
+                         mf ? w->mf.cellOrd : nullptr, mf ? (const void*)w->mfShare : nullptr,
+                         mf ? (const void*)w->damped32 : nullptr, (const void*)(uintptr_t)mfBits};
   if (!w->gFirst[slot] || memcmp(key, w->key[slot], sizeof key) != 0) {
     esf_status e = capture_solid(w->capStream, k, true, !inner, &w->gFirst[slot], &w->kFirst[slot]);
     if (e) return e;
@@ -1651,7 +1844,7 @@ static esf_status solid_pcr_graph(SolidWork* w, int slot, long long S, const T* 
 esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const int* nbr,
                        const double* diag, const double* b, double* x, double eps, int maxIt,
                        int precision, double innerEps, int maxRefine, int* iters, double* relres,
-                       int* refinements, int* converged, cudaStream_t st) {
+                       int* refinements, int* converged, cudaStream_t st, const double* damped) {
   if (S <= 0) {
     if (iters) *iters = 0;
     if (converged) *converged = 0;
@@ -1674,9 +1867,18 @@ esf_status solid_solve(SolidWork* w, long long S, const double* blocks, const in
     if (relres) *relres = h.bnorm2 > 0 ? sqrt(h.resid2 / h.bnorm2) : sqrt(h.resid2);
     return h.status ? (esf_status)h.status : ESF_OK;
   }
-  // mixed: FP32 blocks; x starts at 0 as in the assembled reference variant
-  ESF_COUNTED convert_vec<double, float><<<vec_blocks(rows32(S) * 243), VT, 0, st>>>(rows32(S) * 243, blocks,
-                                                                                   w->blocks32);
+  // mixed: FP32 blocks, or the matrix-free FP32 operator with the damped mass
+  // in FP32; x starts at 0 as in the assembled reference variant
+  if (w->mfOn && !damped) {
+    set_error("solid_solve: the matrix-free operator needs the damped mass");
+    return ESF_ERR_STATE;
+  }
+  if (w->mfOn) {
+    ESF_COUNTED convert_vec<double, float><<<vec_blocks(n), VT, 0, st>>>(n, damped, w->damped32);
+  } else {
+    ESF_COUNTED convert_vec<double, float><<<vec_blocks(rows32(S) * 243), VT, 0, st>>>(rows32(S) * 243, blocks,
+                                                                                     w->blocks32);
+  }
   ESF_CUDA(cudaMemsetAsync(x, 0, n * 8, st));
   double bnorm2 = 0;
   {

@@ -144,6 +144,8 @@ struct esf_scene {
   esf::DBuf sNode, solidF, solidMv, damped, solidV0, solidPC, solidB1, sysDiag, blocks, nbr, mask;
   esf::DBuf Ke, nf, energy;
   esf::DBuf fbCells, fbSlot;  // mixed: near-degenerate cells for the FP64 stiffness
+  esf::DBuf mfCell, mfCorner;  // mixed: per valid cell data of the matrix-free solid operator
+  long long mfCells = 0;       // valid cells they hold (0: assembled FP32 blocks)
   long long Sstep = 0;        // solid nodes of the last step's solid system
   // asynchronous frame writing (esf_write_frame_async)
   double* framePinned = nullptr;
@@ -360,7 +362,7 @@ extern "C" esf_status esf_destroy(esf_scene* s) {
   if (s->hInts) cudaFreeHost(s->hInts);
   if (s->hU64) cudaFreeHost(s->hU64);
   DBuf* bufs[] = {&s->sNode, &s->solidF, &s->solidMv, &s->damped, &s->solidV0, &s->solidPC,
-                  &s->solidB1, &s->sysDiag, &s->blocks, &s->nbr, &s->mask, &s->Ke, &s->nf, &s->fbCells, &s->fbSlot,
+                  &s->solidB1, &s->sysDiag, &s->blocks, &s->nbr, &s->mask, &s->Ke, &s->nf, &s->fbCells, &s->fbSlot, &s->mfCell, &s->mfCorner,
                   &s->energy, &s->cubTmp, &s->keys, &s->vals, &s->skeys, &s->svals, &s->bstart,
                   &s->bend, &s->mt, &s->pweights};
   for (DBuf* b : bufs) b->release();
@@ -877,6 +879,21 @@ static esf_status solid_system(esf_scene* sc, double* energyOut) {
     long long nc = d->nValid;
     sc->validCells = nc;
     sc->hInts[kFallbackCount] = 0;
+    // mixed precision, elastic: record the matrix-free operator's per-cell data
+    // (ESF_SOLID_ASSEMBLED=1 keeps the FP32 copy of the assembled blocks)
+    const bool mf = nc > 0 && sc->p.precision == ESF_MIXED && !d->d.plastic && !getenv("ESF_SOLID_ASSEMBLED");
+    d->d.mf = nullptr;
+    d->d.mfCells = 0;
+    sc->mfCells = 0;
+    if (mf) {
+      TRY(sc->mfCell.ensure((size_t)MF_PLANES * nc * 4));
+      TRY(sc->mfCorner.ensure((size_t)8 * nc * 4));
+      d->d.mf = sc->mfCell.as<float>();
+      d->d.mfCells = nc;
+      sc->mfCells = nc;
+      ESF_COUNTED k_mf_corners<<<kblocks(nc), KT, 0, st>>>(G, d->cellList.as<long long>(), nc, sc->sdof,
+                                                          sc->mfCorner.as<int>());
+    }
     TRY(sc->Ke.ensure((576 * nc + 1) * 8));
     TRY(sc->nf.ensure((24 * nc + 1) * 8));
     if (nc > 0 && d->d.plastic) {
@@ -1042,6 +1059,9 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     sc->sw = nullptr;
     TRY(solid_work_alloc(&sc->sw, S + S / 4 + 16, prec == ESF_MIXED));
   }
+  TRY(solid_work_set_matrix_free(sc->sw, G, sc->mfCells, sc->mfCells ? sc->mfCell.as<float>() : nullptr,
+                                 sc->mfCorner.as<int>(), sc->sNode.as<long long>(), sc->cellOrd,
+                                 sc->ns ? sc->s[0]->d.mu : 0.0, sc->ns ? sc->s[0]->d.lambda : 0.0, scale));
   esf_status es = ESF_OK;
   // A solve that met NaN/Inf ends the step there: nothing downstream (the
   // velocity update, particles, advection) runs on non-finite values. The
@@ -1072,7 +1092,7 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     es = solid_solve(sc->sw, S, sc->blocks.as<double>(), sc->nbr.as<int>(), sc->sysDiag.as<double>(),
                      sc->solidF.as<double>(), sc->solidV0.as<double>(), sc->p.implicit_solver_eps,
                      sc->p.cr_max_iterations, prec, sc->p.inner_eps, sc->p.max_refinements, &it[0],
-                     &rr[0], &rf[0], &cv[0], st);
+                     &rr[0], &rf[0], &cv[0], st, sc->damped.as<double>());
     if (es == ESF_ERR_NUMERIC) return numeric_stop();
     if (es) return es;
   }
@@ -1092,7 +1112,7 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     es = solid_solve(sc->sw, S, sc->blocks.as<double>(), sc->nbr.as<int>(), sc->sysDiag.as<double>(),
                      sc->solidB1.as<double>(), sc->solidPC.as<double>(), sc->p.implicit_solver_eps,
                      sc->p.cr_max_iterations, prec, sc->p.inner_eps, sc->p.max_refinements, &it[2],
-                     &rr[2], &rf[2], &cv[2], st);
+                     &rr[2], &rf[2], &cv[2], st, sc->damped.as<double>());
     if (es == ESF_ERR_NUMERIC) return numeric_stop();
     if (es) return es;
   }
