@@ -27,6 +27,7 @@ EXPORTS = [
     "esf_time_pressure_kernels", "esf_scene_footprint", "esf_server_create", "esf_server_submit",
     "esf_server_poll", "esf_server_wait", "esf_server_get_field", "esf_server_release",
     "esf_server_destroy", "esf_server_batch_stats", "esf_selftest_bounded_wait", "esf_rasterize_solid",
+    "esf_solid_load_rest_sdf", "esf_rest_sdf_query", "esf_svol_read",
 ]
 
 
@@ -72,14 +73,20 @@ def load(build_if_missing: bool = False) -> C.CDLL:
                                         C.POINTER(C.c_int), C.POINTER(C.c_double), vp, C.c_size_t,
                                         C.POINTER(C.c_double)]
     lib.esf_selftest_bounded_wait.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]
+    lib.esf_solid_load_rest_sdf.argtypes = [vp, C.c_int, C.c_char_p]
+    lib.esf_rest_sdf_query.argtypes = [vp, C.c_int, C.c_int, vp, C.c_double, vp, vp]
+    lib.esf_svol_read.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                  C.POINTER(C.c_double), C.POINTER(C.c_double), vp, vp, C.c_size_t]
     _lib = lib
     return lib
 
 
 def make_scene(desc: SceneDesc, precision: int = abi.ESF_FP64, noise: bool = True,
-          stream: int | None = None) -> CoupledIntegrator3D:
-    """GPU integrator for a synthetic scene, set up as the reference's driver does."""
-    return build_from_scene(load(), "esf_", desc, precision=precision, noise=noise, stream=stream)
+          stream: int | None = None, rest_sdf: bool = True) -> CoupledIntegrator3D:
+    """GPU integrator for a synthetic scene, set up as the reference's driver
+    does (with each solid's rest SDF when the scene has several solids)."""
+    return build_from_scene(load(), "esf_", desc, precision=precision, noise=noise, stream=stream,
+                            rest_sdf=rest_sdf)
 
 
 def last_error() -> str:

@@ -61,6 +61,7 @@ class StepReport(C.Structure):
         ("refinements", C.c_int * 3), ("fp64_iterations", C.c_int), ("prone_to_contact", C.c_int),
         ("num_particles", C.c_int), ("status", C.c_int), ("device_ms", C.c_double),
         ("phase_ms", C.c_double * 13), ("fp64_stress_cells", C.c_int), ("valid_cells", C.c_int),
+        ("solid_contacts", C.c_int),
     ]
     PHASES = ["broad_phase_cfl", "solid_forces_stiffness", "body_forces", "solid_solve_1",
               "pressure_solve", "solid_solve_2", "grid_to_particle", "particle_to_grid",
@@ -76,6 +77,7 @@ class StepReport(C.Structure):
             "num_particles": self.num_particles, "status": self.status,
             "device_ms": self.device_ms, "fp64_stress_cells": self.fp64_stress_cells,
             "valid_cells": self.valid_cells,
+            "solid_contacts": self.solid_contacts,
             "phase_ms": dict(zip(self.PHASES, list(self.phase_ms))),
         }
 

@@ -6,6 +6,8 @@ Three translation units, compiled in parallel:
                  and particle seeding keep the reference's non-FMA arithmetic
   esf_config.cpp the cfg reader
   esf_bake.cu    offline mass baking of a solid's rest mass from its mesh
+  esf_contact.cu the rest-SDF (".svol") reader and triangle hash of
+                 solid-solid contact
   esf_io.cpp     frame files (gz fields, OBJ); zlib is loaded at run time
   esf_serve.cpp  the multi-scene server (host threads, one stream per scene)
 Host code is compiled with -ffp-contract=off for the same reason (the box's
@@ -38,6 +40,7 @@ def _sources():
         "esf_solver.cu": ["-O3", "-lineinfo"],
         "esf_step.cu": ["-O3", "-lineinfo", "-fmad=false"],
         "esf_bake.cu": ["-O3", "-lineinfo"],
+        "esf_contact.cu": ["-O2"],
         "esf_config.cpp": ["-O2"],
         "esf_io.cpp": ["-O2"],
         "esf_serve.cpp": ["-O2"],
@@ -76,7 +79,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             sys.stderr.write(r.stderr)
         return obj
 
-    with cf.ThreadPoolExecutor(max_workers=5) as ex:
+    with cf.ThreadPoolExecutor(max_workers=7) as ex:
         objs = list(ex.map(one, _sources().items()))
     tmp = LIB + f".tmp{os.getpid()}"
     cmd = [nvcc, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart", "-ldl", "-lpthread"]

@@ -6,6 +6,7 @@
 #include <climits>
 
 #include "esf_common.cuh"
+#include "esf_contact.cuh"
 
 namespace esf {
 
@@ -741,10 +742,10 @@ struct ContactParams {
 };
 
 // DEFOR_SOLID_3D::gridToParticle (DEFOR_SOLID_3D.cpp:891-1034): FLIP/PIC
-// blend, wall contact impulses, then p += v dt.
+// blend, one solid-solid contact impulse (the first neighbour the particle
+// touches), one wall contact impulse, then p += v dt.
 __global__ void k_grid_to_particle(GridDev g, SolidDev s, long long np, double* part,
-                                   ContactParams cp, const double* const* otherPhi, int nOther,
-                                   int* unsupported) {
+                                   ContactParams cp, const ContactSet cs) {
   FOR_N(np, c) {
     double* P = part + 10 * c;
     double pos[3] = {P[0], P[1], P[2]};
@@ -778,9 +779,33 @@ __global__ void k_grid_to_particle(GridDev g, SolidDev s, long long np, double* 
     ci = min(max(ci, 0), g.X - 2);
     cj = min(max(cj, 0), g.Y - 2);
     ck = min(max(ck, 0), g.Z - 2);
-    for (int y = 0; y < nOther; y++) {
-      double ph = interp1(otherPhi[y], g.X, g.Y, g.Z, g.dh, g.o, pos);
-      if (!(ph > 2)) atomicOr(unsupported, 1);
+    // collision with the other solids (:967-995): B's rest SDF at the
+    // particle's position in B's rest space
+    for (int y = 0; y < cs.n; y++) {
+      const ContactNeighbor& B = cs.nb[y];
+      if (interp1(B.phi, g.X, g.Y, g.Z, g.dh, g.o, pos) > 2) continue;
+      double restPos[3], normal[3] = {0.0, 0.0, 0.0};
+      interp3(B.X, g.X, g.Y, g.Z, g.dh, g.o, pos, restPos);
+      const double sdf = sdf_contact(B.sdf, restPos, cs.thickness, normal);
+      if (sdf > cs.thickness) continue;
+      const double overlap = cs.thickness - sdf;
+      double vo[3];
+      interp3(B.vel, g.X, g.Y, g.Z, g.dh, g.o, pos, vo);
+      double vrel[3] = {pv[0] - vo[0], pv[1] - vo[1], pv[2] - vo[2]};
+      const double vn = (vrel[0] * normal[0] + vrel[1] * normal[1]) + vrel[2] * normal[2];
+      if (vn <= 0 || sdf <= 0) {
+        const double A = s.dt * cp.spring * overlap, Bv = P[9] * (0.1 * overlap / s.dt - vn);
+        const double impulse = -((Bv < A) ? Bv : A);
+        const double dvn = -impulse / P[9];
+        double vt[3];
+        for (int q = 0; q < 3; q++) vt[q] = vrel[q] - vn * normal[q];
+        const double vtn = sqrt(vt[0] * vt[0] + (vt[1] * vt[1] + vt[2] * vt[2]));  // as the wall's vt.norm()
+        double sc = 1 - cp.friction * dvn / vtn;
+        sc = (sc < 0.0) ? 0.0 : sc;  // std::max(sc, 0.0)
+        for (int q = 0; q < 3; q++) pv[q] = ((vn + dvn) * normal[q] + sc * vt[q]) + vo[q];
+        if (cs.contacts) atomicAdd(cs.contacts, 1ull);
+        break;
+      }
     }
     const double N[6][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {-1, 0, 0}, {0, -1, 0}, {0, 0, -1}};
     for (int b = 0; b < 6; b++) {
@@ -1045,6 +1070,45 @@ __global__ void k_mesh_aabb(int ntri, const int* tris, const double* verts, unsi
       atomicMin(&box[q], b);
       atomicMax(&box[3 + q], b);
     }
+  }
+}
+
+// TRIANGLE_BVH::collide (TRIANGLE_BVH.cpp:187-200) without the tree: two
+// meshes collide when a triangle of one and a triangle of the other have
+// overlapping bounding boxes (aabb::overlaps, closed intervals). A node's box
+// holds its leaves' boxes, so the tree walk reports exactly these pairs.
+__global__ void k_mesh_pair_overlap(int na, const int* ta, const double* va, int nb, const int* tb,
+                                    const double* vb, int* hit) {
+  FOR_N((long long)na * nb, t) {
+    if (*(volatile int*)hit) return;
+    const int i = (int)(t / nb), j = (int)(t % nb);
+    double amin[3], amax[3], bmin[3], bmax[3];
+    for (int k = 0; k < 3; k++) {
+      amin[k] = amax[k] = va[3 * ta[3 * i] + k];
+      bmin[k] = bmax[k] = vb[3 * tb[3 * j] + k];
+    }
+    for (int c = 1; c < 3; c++)
+      for (int k = 0; k < 3; k++) {
+        const double x = va[3 * ta[3 * i + c] + k], y = vb[3 * tb[3 * j + c] + k];
+        amin[k] = fmin(amin[k], x);
+        amax[k] = fmax(amax[k], x);
+        bmin[k] = fmin(bmin[k], y);
+        bmax[k] = fmax(bmax[k], y);
+      }
+    bool overlap = true;
+    for (int k = 0; k < 3; k++)
+      if (amin[k] > bmax[k] || amax[k] < bmin[k]) overlap = false;
+    if (overlap) atomicExch(hit, 1);
+  }
+}
+
+// SPARSE_SDF::signedDistAndCurrentNormal at given rest points (the contact
+// query alone, for checking it against the reference's).
+__global__ void k_rest_sdf_query(RestSdfDev s, int n, const double* pts, double safe, double* sd, double* normal) {
+  FOR_N(n, i) {
+    double nrm[3] = {0.0, 0.0, 0.0};
+    sd[i] = sdf_contact(s, pts + 3 * i, safe, nrm);
+    for (int k = 0; k < 3; k++) normal[3 * i + k] = nrm[k];
   }
 }
 
@@ -1689,8 +1753,24 @@ __global__ void k_advect_scalar_f32(GridDev g, const double* solidMass, const do
 // increasing index, as Eigen's setFromTriplets sums them), scaled by
 // dt^2 + beta dt, plus the damped mass on the diagonal entries; the
 // structural mask; and the stiffness force sum in the same cell order.
-__global__ void k_assemble(GridDev g, SolidDev s, const int* sdof, const long long* sNode, long long S,
-                           const int* cellOrd, const double* Ke, const double* nf, double scale,
+// The solids of a scene as the assembly sees them: each one's mass and its
+// cell -> valid-cell ordinal map; the element matrices and forces of solid i
+// start at valid cell keBase[i] of the concatenated arrays.
+struct SolidSet {
+  int n;
+  const double* mass[ESF_MAX_SOLIDS];
+  const int* ord[ESF_MAX_SOLIDS];
+  long long keBase[ESF_MAX_SOLIDS];
+};
+
+// _systemMatrix from the triplets of every solid's
+// computeStiffnessMatrixAndMaterialForce (DEFOR_SOLID_3D.cpp:697-871): a
+// solid contributes between two nodes that both carry its mass; Eigen's
+// setFromTriplets sums the duplicates in list order (solid 0's cells in
+// index order, then solid 1's), and the force vector takes each solid's
+// own sum (its local force) in turn.
+__global__ void k_assemble(GridDev g, SolidSet ss, const int* sdof, const long long* sNode, long long S,
+                           const double* Ke, const double* nf, double scale,
                            double* blocks, int* nbr, int* mask, double* force) {
   FOR_N(S * 27, t) {
     long long a = t / 27;
@@ -1705,16 +1785,17 @@ __global__ void k_assemble(GridDev g, SolidDev s, const int* sdof, const long lo
     if (mx >= 0 && mx < g.X && my >= 0 && my < g.Y && mz >= 0 && mz < g.Z) {
       long long m = nidx(g, mx, my, mz);
       mdof = sdof[m];
-      if (mdof >= 0 && s.mass[n] != 0 && s.mass[m] != 0) {
+      for (int si = 0; si < ss.n && mdof >= 0; si++) {
+        if (ss.mass[si][n] == 0 || ss.mass[si][m] == 0) continue;
         for (int ia = 7; ia >= 0; ia--) {  // cells containing n, increasing index
           int cx = nx - (ia & 1), cy = ny - ((ia >> 1) & 1), cz = nz - ((ia >> 2) & 1);
           if (cx < 0 || cy < 0 || cz < 0 || cx > g.X - 2 || cy > g.Y - 2 || cz > g.Z - 2) continue;
           int bx = mx - cx, by = my - cy, bz = mz - cz;
           if (bx < 0 || bx > 1 || by < 0 || by > 1 || bz < 0 || bz > 1) continue;
-          int ord = cellOrd[cidx(g, cx, cy, cz)];
+          int ord = ss.ord[si][cidx(g, cx, cy, cz)];
           if (ord < 0) continue;
           int ib = bx + 2 * by + 4 * bz;
-          const double* K = Ke + 576LL * ord;
+          const double* K = Ke + 576LL * (ss.keBase[si] + ord);
           for (int r = 0; r < 3; r++)
             for (int q = 0; q < 3; q++) blk[r * 3 + q] += K[(ia * 3 + r) * 24 + ib * 3 + q];
           present = true;
@@ -1724,14 +1805,18 @@ __global__ void k_assemble(GridDev g, SolidDev s, const int* sdof, const long lo
     for (int e = 0; e < 9; e++) blocks[blk_at(a, 9 * j + e)] = present ? blk[e] * scale : 0.0;
     if (j == 13) {
       present = true;  // coeffRef(i, i) creates the diagonal entries
-      // force: cells containing n in increasing index, corner ia
+      // force: per solid, cells containing n in increasing index, corner ia
       double f[3] = {0, 0, 0};
-      for (int ia = 7; ia >= 0; ia--) {
-        int cx = nx - (ia & 1), cy = ny - ((ia >> 1) & 1), cz = nz - ((ia >> 2) & 1);
-        if (cx < 0 || cy < 0 || cz < 0 || cx > g.X - 2 || cy > g.Y - 2 || cz > g.Z - 2) continue;
-        int ord = cellOrd[cidx(g, cx, cy, cz)];
-        if (ord < 0) continue;
-        for (int r = 0; r < 3; r++) f[r] += nf[24LL * ord + r * 8 + ia];
+      for (int si = 0; si < ss.n; si++) {
+        double fs[3] = {0, 0, 0};
+        for (int ia = 7; ia >= 0; ia--) {
+          int cx = nx - (ia & 1), cy = ny - ((ia >> 1) & 1), cz = nz - ((ia >> 2) & 1);
+          if (cx < 0 || cy < 0 || cz < 0 || cx > g.X - 2 || cy > g.Y - 2 || cz > g.Z - 2) continue;
+          int ord = ss.ord[si][cidx(g, cx, cy, cz)];
+          if (ord < 0) continue;
+          for (int r = 0; r < 3; r++) fs[r] += nf[24LL * (ss.keBase[si] + ord) + r * 8 + ia];
+        }
+        for (int r = 0; r < 3; r++) f[r] = si == 0 ? fs[r] : f[r] + fs[r];
       }
       for (int r = 0; r < 3; r++) force[3 * a + r] = f[r];
     }

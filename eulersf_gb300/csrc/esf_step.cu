@@ -17,6 +17,7 @@
 #include <string>
 #include <vector>
 
+#include "esf_contact_host.h"
 #include "esf_io.h"
 #include "esf_kernels.cuh"
 
@@ -116,6 +117,13 @@ struct Solid {
   long long pn = 0;
   long long np = 0, nValid = 0;
   double pmass = 0;
+  // rest SDF of solid-solid contact (esf_solid_load_rest_sdf): lattice
+  // values and codes, per-point triangle lists
+  DBuf sdfVal, sdfCode, sdfOff, sdfIds;
+  RestSdfDev sdf{};
+  bool hasSdf = false;
+  // cell -> valid-cell ordinal of this solid (scenes with several solids)
+  DBuf ord;
 };
 
 }  // namespace esf
@@ -154,6 +162,7 @@ struct esf_scene {
   std::thread frameThread;
   int frameStatus = 0;
   long long validCells = 0;
+  esf::DBuf contactCount;  // particles that took a solid-solid impulse this step
   // scratch
   esf::DBuf cubTmp, keys, vals, skeys, svals, bstart, bend, mt, pweights;
   long long mtLen = 0;
@@ -342,6 +351,7 @@ static void free_solid(Solid* d) {
   cudaFree(d->dRot); cudaFree(d->dVerts); cudaFree(d->dRest); cudaFree(d->dRestMass); cudaFree(d->dTris);
   d->part.release(); d->cellList.release(); d->cellFlag.release(); d->cellScan.release();
   d->fp.release(); d->fpUpd.release(); d->fpVal.release(); d->fpWin.release();
+  d->sdfVal.release(); d->sdfCode.release(); d->sdfOff.release(); d->sdfIds.release(); d->ord.release();
   delete d;
 }
 
@@ -364,7 +374,7 @@ extern "C" esf_status esf_destroy(esf_scene* s) {
   DBuf* bufs[] = {&s->sNode, &s->solidF, &s->solidMv, &s->damped, &s->solidV0, &s->solidPC,
                   &s->solidB1, &s->sysDiag, &s->blocks, &s->nbr, &s->mask, &s->Ke, &s->nf, &s->fbCells, &s->fbSlot, &s->mfCell, &s->mfCorner,
                   &s->energy, &s->cubTmp, &s->keys, &s->vals, &s->skeys, &s->svals, &s->bstart,
-                  &s->bend, &s->mt, &s->pweights};
+                  &s->bend, &s->mt, &s->pweights, &s->contactCount};
   for (DBuf* b : bufs) b->release();
   pressure_work_free(s->pw);
   solid_work_free(s->sw);
@@ -513,6 +523,87 @@ extern "C" esf_status esf_add_solid(esf_scene* sc, const esf_solid_desc* dd) {
   return ESF_OK;
 }
 
+// DEFOR_SOLID_3D::loadRestSDF (DEFOR_SOLID_3D.cpp:210-214): the solid's
+// rest SDF from a ".svol" file and the triangle lists of its band points,
+// hashed from the rest-pose mesh, on the device.
+extern "C" esf_status esf_solid_load_rest_sdf(esf_scene* sc, int solid, const char* path) {
+  if (!sc || !path || solid < 0 || solid >= sc->ns) {
+    set_error("esf_solid_load_rest_sdf: no such solid or null path");
+    return ESF_ERR_INVALID_ARG;
+  }
+  cudaSetDevice(sc->device);
+  Solid* d = sc->s[solid];
+  SvolLattice L;
+  TRY(svol_read(path, &L));
+  std::vector<int> off, ids;
+  svol_hash_triangles(L, d->restPose.data(), d->ntri, d->tris.data(), &off, &ids);
+  TRY(d->sdfVal.ensure(L.val.size() * 4));
+  TRY(d->sdfCode.ensure(L.code.size()));
+  TRY(d->sdfOff.ensure(off.size() * 4));
+  TRY(d->sdfIds.ensure(ids.size() * 4));
+  ESF_CUDA(cudaStreamSynchronize(sc->stream));
+  ESF_CUDA(cudaMemcpy(d->sdfVal.p, L.val.data(), L.val.size() * 4, cudaMemcpyHostToDevice));
+  ESF_CUDA(cudaMemcpy(d->sdfCode.p, L.code.data(), L.code.size(), cudaMemcpyHostToDevice));
+  ESF_CUDA(cudaMemcpy(d->sdfOff.p, off.data(), off.size() * 4, cudaMemcpyHostToDevice));
+  ESF_CUDA(cudaMemcpy(d->sdfIds.p, ids.data(), ids.size() * 4, cudaMemcpyHostToDevice));
+  RestSdfDev& r = d->sdf;
+  r.val = d->sdfVal.as<float>();
+  r.code = d->sdfCode.as<signed char>();
+  r.triOff = d->sdfOff.as<int>();
+  r.triIds = d->sdfIds.as<int>();
+  for (int k = 0; k < 3; k++) {
+    r.lo[k] = L.lo[k];
+    r.n[k] = L.n[k];
+  }
+  r.nxy = (long long)L.n[0] * L.n[1];
+  r.dx = L.dx;
+  r.inv = 1.0 / L.dx;
+  for (int k = 0; k < 3; k++) r.off[k] = (-L.t[k]) * r.inv;
+  r.inC = L.inC;
+  r.outC = L.outC;
+  r.rest = d->dRest;
+  r.cur = d->dVerts;
+  r.tris = d->dTris;
+  d->hasSdf = true;
+  return ESF_OK;
+}
+
+// SPARSE_SDF::signedDistAndCurrentNormal of solid `solid` at n rest-space
+// points (host arrays), with the solid's current mesh as the step left it.
+extern "C" esf_status esf_rest_sdf_query(esf_scene* sc, int solid, int n, const double* points, double safe_dist,
+                                         double* sd, double* normals) {
+  if (!sc || solid < 0 || solid >= sc->ns || n < 0 || (n > 0 && (!points || !sd || !normals))) {
+    set_error("esf_rest_sdf_query: invalid argument");
+    return ESF_ERR_INVALID_ARG;
+  }
+  Solid* d = sc->s[solid];
+  if (!d->hasSdf) {
+    set_error("esf_rest_sdf_query: solid %d has no rest SDF", solid);
+    return ESF_ERR_STATE;
+  }
+  if (n == 0) return ESF_OK;
+  cudaSetDevice(sc->device);
+  double *dp = nullptr, *dsd = nullptr, *dn = nullptr;
+  esf_status e = dalloc((void**)&dp, (size_t)n * 24);
+  if (!e) e = dalloc((void**)&dsd, (size_t)n * 8);
+  if (!e) e = dalloc((void**)&dn, (size_t)n * 24);
+  cudaStream_t st = sc->stream;
+  if (!e && cudaMemcpyAsync(dp, points, (size_t)n * 24, cudaMemcpyHostToDevice, st) != cudaSuccess) e = ESF_ERR_CUDA;
+  if (!e) {
+    ESF_COUNTED k_rest_sdf_query<<<kblocks(n), KT, 0, st>>>(d->sdf, n, dp, safe_dist, dsd, dn);
+    if (cudaGetLastError() != cudaSuccess) e = ESF_ERR_CUDA;
+  }
+  if (!e && (cudaMemcpyAsync(sd, dsd, (size_t)n * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+             cudaMemcpyAsync(normals, dn, (size_t)n * 24, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+             cudaStreamSynchronize(st) != cudaSuccess))
+    e = ESF_ERR_CUDA;
+  if (e == ESF_ERR_CUDA) set_error("esf_rest_sdf_query: %s", cudaGetErrorString(cudaGetLastError()));
+  cudaFree(dp);
+  cudaFree(dsd);
+  cudaFree(dn);
+  return e;
+}
+
 extern "C" esf_status esf_set_fluid(esf_scene* s, double density, double viscosity) {
   if (!s) return ESF_ERR_INVALID_ARG;
   (void)viscosity;  // stored but unused by the reference (COUPLED_INTEGRATOR_3D.cpp:46)
@@ -574,7 +665,8 @@ static esf_status compute_solid_mass(esf_scene* sc, Solid* d, int usesdf) {
 // grid barrier timed out raises the scene's sweep error word (dInts[42]),
 // checked when the step or init ends.
 constexpr int kSweepBar = 40, kSweepErr = 42;
-constexpr int kFallbackCount = 44;  // mixed: cells of the FP32 stiffness evaluated again in FP64
+constexpr int kFallbackCount = 44;  // mixed: cells of the FP32 stiffness evaluated again in FP64 (one per solid)
+constexpr int kOverlap = 52;        // broad phase: two solids' meshes overlap
 template <bool VEC>
 static esf_status sweep_pass(esf_scene* sc, Solid* d, const Sweep& w, const unsigned long long* ranks) {
   cudaStream_t st = sc->stream;
@@ -841,6 +933,14 @@ static double u64_to_double(unsigned long long b) {
   return d;
 }
 
+// cell -> valid-cell ordinal map of solid i (solid 0 uses the scene's)
+static int* solid_ord(esf_scene* sc, int i) {
+  if (i == 0) return sc->cellOrd;
+  Solid* d = sc->s[i];
+  if (d->ord.ensure((size_t)sc->g.R * 4) != ESF_OK) return nullptr;
+  return d->ord.as<int>();
+}
+
 // stiffness + computeMV + assembly (DEFOR_SOLID_3D.cpp:697-889;
 // COUPLED_INTEGRATOR_3D.cpp:432-437, 609-620 for the assembly)
 static esf_status solid_system(esf_scene* sc, double* energyOut) {
@@ -863,28 +963,36 @@ static esf_status solid_system(esf_scene* sc, double* energyOut) {
   ESF_CUDA(cudaMemsetAsync(sc->damped.p, 0, 3 * S * 8 + 8, st));
   ESF_CUDA(cudaMemsetAsync(sc->mask.p, 0, S * 4 + 4, st));
   const int EB = 4096;
-  // energy partials: stiffness, mass-weighted velocity, body forces, FP64
-  // fallback cells of the mixed path's FP32 stiffness
-  TRY(sc->energy.ensure(EB * 4 * 8));
-  ESF_CUDA(cudaMemsetAsync(sc->energy.p, 0, EB * 4 * 8, st));
-  double* ePart = sc->energy.as<double>();
-  // one solid: its valid-cell list is the one the particles were seeded from
-  if (sc->ns != 1 && S > 0) {
-    set_error("solid_system: scenes with more than one solid are not supported yet");
-    return ESF_ERR_UNSUPPORTED;
-  }
+  // energy partials, 4 x EB per solid: stiffness, mass-weighted velocity,
+  // body forces (solid 0's region only), FP64 fallback cells of the mixed
+  // path's FP32 stiffness
+  TRY(sc->energy.ensure((size_t)EB * 4 * 8 * (sc->ns > 0 ? sc->ns : 1)));
+  ESF_CUDA(cudaMemsetAsync(sc->energy.p, 0, (size_t)EB * 4 * 8 * (sc->ns > 0 ? sc->ns : 1), st));
+  // element matrices and forces of all solids, concatenated in solid order
+  long long totalCells = 0;
+  for (int i = 0; i < sc->ns; i++) totalCells += sc->s[i]->nValid;
+  TRY(sc->Ke.ensure((576 * totalCells + 1) * 8));
+  TRY(sc->nf.ensure((24 * totalCells + 1) * 8));
+  sc->validCells = totalCells;
+  sc->mfCells = 0;
+  long long keBase = 0;
   for (int i = 0; i < sc->ns; i++) {
     Solid* d = sc->s[i];
-    ESF_CUDA(cudaMemsetAsync(sc->cellOrd, 0xff, G.R * 4, st));
-    long long nc = d->nValid;
-    sc->validCells = nc;
-    sc->hInts[kFallbackCount] = 0;
-    // mixed precision, elastic: record the matrix-free operator's per-cell data
-    // (ESF_SOLID_ASSEMBLED=1 keeps the FP32 copy of the assembled blocks)
-    const bool mf = nc > 0 && sc->p.precision == ESF_MIXED && !d->d.plastic && !getenv("ESF_SOLID_ASSEMBLED");
+    double* ePart = sc->energy.as<double>() + (size_t)4 * EB * i;
+    int* ord = solid_ord(sc, i);
+    if (!ord) return ESF_ERR_OOM;
+    ESF_CUDA(cudaMemsetAsync(ord, 0xff, G.R * 4, st));
+    const long long nc = d->nValid;
+    sc->hInts[kFallbackCount + i] = 0;
+    double* Ke = sc->Ke.as<double>() + 576 * keBase;
+    double* nf = sc->nf.as<double>() + 24 * keBase;
+    // mixed precision, elastic, one solid: record the matrix-free operator's
+    // per-cell data (ESF_SOLID_ASSEMBLED=1 keeps the FP32 copy of the
+    // assembled blocks, as scenes with several solids do)
+    const bool mf = sc->ns == 1 && nc > 0 && sc->p.precision == ESF_MIXED && !d->d.plastic &&
+                    !getenv("ESF_SOLID_ASSEMBLED");
     d->d.mf = nullptr;
     d->d.mfCells = 0;
-    sc->mfCells = 0;
     if (mf) {
       TRY(sc->mfCell.ensure((size_t)MF_PLANES * nc * 4));
       TRY(sc->mfCorner.ensure((size_t)8 * nc * 4));
@@ -894,8 +1002,6 @@ static esf_status solid_system(esf_scene* sc, double* energyOut) {
       ESF_COUNTED k_mf_corners<<<kblocks(nc), KT, 0, st>>>(G, d->cellList.as<long long>(), nc, sc->sdof,
                                                           sc->mfCorner.as<int>());
     }
-    TRY(sc->Ke.ensure((576 * nc + 1) * 8));
-    TRY(sc->nf.ensure((24 * nc + 1) * 8));
     if (nc > 0 && d->d.plastic) {
       TRY(d->fpUpd.ensure(nc * 4));
       TRY(d->fpVal.ensure(nc * 72));
@@ -909,16 +1015,14 @@ static esf_status solid_system(esf_scene* sc, double* energyOut) {
       ESF_CUDA(cudaMemsetAsync(sc->dInts + kFallbackCount, 0, sizeof(int), st));
       unsigned* fbCount = reinterpret_cast<unsigned*>(sc->dInts + kFallbackCount);
       ESF_COUNTED k_element_stiffness_f32<<<kblocks(nc, 128), 128, 0, st>>>(
-          G, d->d, d->cellList.as<long long>(), nc, sc->Ke.as<double>(), sc->nf.as<double>(), ePart,
-          sc->fbCells.as<long long>(), sc->fbSlot.as<long long>(), fbCount);
-      ESF_COUNTED k_element_stiffness<<<kblocks(nc, 128), 128, 0, st>>>(
-          G, d->d, sc->fbCells.as<long long>(), nc, sc->Ke.as<double>(), sc->nf.as<double>(), ePart + 3 * EB,
+          G, d->d, d->cellList.as<long long>(), nc, Ke, nf, ePart, sc->fbCells.as<long long>(),
           sc->fbSlot.as<long long>(), fbCount);
-      ESF_CUDA(cudaMemcpyAsync(&sc->hInts[kFallbackCount], fbCount, sizeof(int), cudaMemcpyDeviceToHost, st));
+      ESF_COUNTED k_element_stiffness<<<kblocks(nc, 128), 128, 0, st>>>(
+          G, d->d, sc->fbCells.as<long long>(), nc, Ke, nf, ePart + 3 * EB, sc->fbSlot.as<long long>(), fbCount);
+      ESF_CUDA(cudaMemcpyAsync(&sc->hInts[kFallbackCount + i], fbCount, sizeof(int), cudaMemcpyDeviceToHost, st));
     } else if (nc > 0) {
       ESF_COUNTED k_element_stiffness<<<kblocks(nc, 128), 128, 0, st>>>(G, d->d, d->cellList.as<long long>(), nc,
-                                                             sc->Ke.as<double>(), sc->nf.as<double>(),
-                                                             ePart, nullptr, nullptr);
+                                                             Ke, nf, ePart, nullptr, nullptr);
     }
     if (nc > 0) {
       if (d->d.plastic) {
@@ -928,13 +1032,14 @@ static esf_status solid_system(esf_scene* sc, double* energyOut) {
                                                            d->d.FpInv);
       }
       // cell -> ordinal in the valid list
-      ESF_COUNTED k_cell_ord_fill<<<kblocks(nc), KT, 0, st>>>(G, d->cellList.as<long long>(), nc, sc->cellOrd);
+      ESF_COUNTED k_cell_ord_fill<<<kblocks(nc), KT, 0, st>>>(G, d->cellList.as<long long>(), nc, ord);
     }
     Box b = mkbox(d->ex[0], d->ex[1], d->ex[2], d->ex[3] - 1, d->ex[4] - 1, d->ex[5] - 1);
     if (boxn(b) > 0 && S > 0)
       ESF_COUNTED k_compute_mv<<<std::min(kblocks(boxn(b)), EB), KT, 0, st>>>(G, d->d, b, sc->sdof,
                                                                   sc->solidMv.as<double>(), ePart + EB);
     ESF_LAUNCH_CHECK();
+    keBase += nc;
   }
   *energyOut = 0;
   return ESF_OK;
@@ -960,6 +1065,12 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     set_error("esf_step: a solve of an earlier step met NaN/Inf; restore a state with esf_read_frame first");
     return ESF_ERR_STATE;
   }
+  for (int i = 0; i < sc->ns && sc->ns > 1; i++)
+    if (!sc->s[i]->hasSdf) {
+      set_error("esf_step: solid %d has no rest SDF; scenes with several solids need one per solid for "
+                "solid-solid contact (esf_solid_load_rest_sdf)", i);
+      return ESF_ERR_STATE;
+    }
   cudaSetDevice(sc->device);
   const GridDev& G = sc->g;
   cudaStream_t st = sc->stream;
@@ -988,10 +1099,21 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
         inside = false;
     if (!inside) prone = 1;
   }
-  if (!prone && sc->ns > 1) {
-    set_error("esf_step: solid-solid broad phase is not supported yet");
-    return ESF_ERR_UNSUPPORTED;
-  }
+  // solids close to one another (:394-404): the first pair whose meshes'
+  // triangle boxes overlap
+  for (int i = 0; i + 1 < sc->ns && !prone; i++)
+    for (int j = i + 1; j < sc->ns && !prone; j++) {
+      Solid *a = sc->s[i], *b = sc->s[j];
+      int* hit = sc->dInts + kOverlap;
+      ESF_CUDA(cudaMemsetAsync(hit, 0, sizeof(int), st));
+      const long long pairs = (long long)a->ntri * b->ntri;
+      ESF_COUNTED k_mesh_pair_overlap<<<kblocks(pairs), KT, 0, st>>>(a->ntri, a->dTris, a->dVerts, b->ntri,
+                                                                     b->dTris, b->dVerts, hit);
+      ESF_LAUNCH_CHECK();
+      ESF_CUDA(cudaMemcpyAsync(&sc->hInts[kOverlap], hit, sizeof(int), cudaMemcpyDeviceToHost, st));
+      ESF_CUDA(cudaStreamSynchronize(st));
+      if (sc->hInts[kOverlap]) prone = 1;
+    }
   // CFL (:88-102)
   sc->hU64[0] = 0;
   ESF_CUDA(cudaMemcpyAsync(sc->dU64, sc->hU64, 8, cudaMemcpyHostToDevice, st));
@@ -1034,8 +1156,18 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
   const double scale = dt * dt + sc->p.rayleigh_beta * dt;
   if (S > 0) {
     // forces + blocks (diagonal mass added in a second pass, below)
-    ESF_COUNTED k_assemble<<<kblocks(S * 27), KT, 0, st>>>(G, sc->s[0]->d, sc->sdof, sc->sNode.as<long long>(), S,
-                                                sc->cellOrd, sc->Ke.as<double>(), sc->nf.as<double>(), scale,
+    SolidSet ss;
+    memset(&ss, 0, sizeof ss);
+    ss.n = sc->ns;
+    long long base = 0;
+    for (int i = 0; i < sc->ns; i++) {
+      ss.mass[i] = sc->s[i]->d.mass;
+      ss.ord[i] = solid_ord(sc, i);
+      ss.keBase[i] = base;
+      base += sc->s[i]->nValid;
+    }
+    ESF_COUNTED k_assemble<<<kblocks(S * 27), KT, 0, st>>>(G, ss, sc->sdof, sc->sNode.as<long long>(), S,
+                                                sc->Ke.as<double>(), sc->nf.as<double>(), scale,
                                                 sc->blocks.as<double>(),
                                                 sc->nbr.as<int>(), sc->mask.as<int>(), sc->solidF.as<double>());
   }
@@ -1049,7 +1181,7 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
                                           sc->sysDiag.as<double>());
     ESF_LAUNCH_CHECK();
   }
-  double energy = sum_partials(sc, 4 * EB);
+  double energy = sum_partials(sc, 4 * EB * (sc->ns > 0 ? sc->ns : 1));
   // ---- pcrImplicitSolve (:662-764)
   int it[3] = {0, 0, 0}, cv[3] = {0, 0, 0}, rf[3] = {0, 0, 0}, it64 = 0;
   double rr[3] = {0, 0, 0};
@@ -1138,11 +1270,30 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     if (boxn(ex) > 0) ESF_COUNTED k_copy_grid_velocity<<<kblocks(boxn(ex)), KT, 0, st>>>(G, d->d, ex, sc->vel);
     d->d.dt = dt;
   }
-  for (int i = 0; i < sc->ns; i++) {  // gridToParticle
+  TRY(sc->contactCount.ensure(8));
+  ESF_CUDA(cudaMemsetAsync(sc->contactCount.p, 0, 8, st));
+  for (int i = 0; i < sc->ns; i++) {  // gridToParticle, with the other solids as contact neighbours
     Solid* d = sc->s[i];
+    ContactSet cs;
+    memset(&cs, 0, sizeof cs);
+    cs.thickness = sc->p.contact_safe_distance;
+    cs.contacts = sc->contactCount.as<unsigned long long>();
+    for (int j = 0; j < sc->ns; j++) {
+      if (j == i) continue;
+      Solid* o = sc->s[j];
+      if (!o->hasSdf) {
+        set_error("esf_step: solid %d has no rest SDF; scenes with several solids need one per solid "
+                  "(esf_solid_load_rest_sdf)", j);
+        return ESF_ERR_STATE;
+      }
+      ContactNeighbor& nb = cs.nb[cs.n++];
+      nb.phi = o->d.phi;
+      nb.X = o->d.X;
+      nb.vel = o->d.vel;
+      nb.sdf = o->sdf;
+    }
     if (d->np > 0)
-      ESF_COUNTED k_grid_to_particle<<<kblocks(d->np), KT, 0, st>>>(G, d->d, d->np, d->part.as<double>(), cp, nullptr, 0,
-                                                        sc->dInts + 32);
+      ESF_COUNTED k_grid_to_particle<<<kblocks(d->np), KT, 0, st>>>(G, d->d, d->np, d->part.as<double>(), cp, cs);
   }
   ESF_CUDA(cudaEventRecord(sc->ph[7], st));
   for (int i = 0; i < sc->ns; i++) {  // particleToGrid
@@ -1283,8 +1434,13 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     }
     rep->prone_to_contact = prone;
     rep->fp64_iterations = it64;
-    rep->fp64_stress_cells = prec == ESF_MIXED ? sc->hInts[kFallbackCount] : (int)sc->validCells;
+    int fb = 0;
+    for (int i = 0; i < sc->ns; i++) fb += sc->hInts[kFallbackCount + i];
+    rep->fp64_stress_cells = prec == ESF_MIXED ? fb : (int)sc->validCells;
     rep->valid_cells = (int)sc->validCells;
+    unsigned long long contacts = 0;
+    ESF_CUDA(cudaMemcpy(&contacts, sc->contactCount.p, 8, cudaMemcpyDeviceToHost));
+    rep->solid_contacts = (int)contacts;
     long long np = 0;
     for (int i = 0; i < sc->ns; i++) np += sc->s[i]->np;
     rep->num_particles = (int)np;

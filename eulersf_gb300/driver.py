@@ -78,6 +78,9 @@ def run(cfg_path, frames=None, precision=abi.ESF_FP64, out=sys.stdout):
         d.num_triangles, d.triangles = len(tris), t.ctypes.data_as(C.POINTER(C.c_int))
         d.plastic_yield = float(cfg.get(f"solid plastic yield {i}", -1))
         I.addSolid(d, keep=(rest, v, t))
+        # main.cpp:146-148; a rest SDF is only read by solid-solid contact
+        if n.value > 1:
+            I.loadRestSDF(i, base + ".svol")
     I.setFluidDensity(float(cfg.get("fluid density", 1)))
     I.setFluidViscocity(float(cfg.get("fluid viscocity", 0)))
     I.init()

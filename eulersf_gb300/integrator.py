@@ -10,6 +10,7 @@ oracle's Python wrapper drives its own library through the same class.
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -84,6 +85,21 @@ class CoupledIntegrator3D:
     def addSolid(self, desc: abi.SolidDesc, keep=()):
         self._keep.extend(keep)
         self._call("add_solid", self._h, C.byref(desc))
+
+    def loadRestSDF(self, solid: int, path: str):
+        """DEFOR_SOLID_3D::loadRestSDF (DEFOR_SOLID_3D.cpp:210-214) of solid i."""
+        self._call("solid_load_rest_sdf", self._h, int(solid), path.encode())
+
+    def restSdfQuery(self, solid: int, points, safe_dist: float):
+        """SPARSE_SDF::signedDistAndCurrentNormal of solid i at rest points
+        (n x 3): (distances, normals n x 3)."""
+        pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))
+        n = len(pts)
+        sd = np.zeros(n)
+        nrm = np.zeros((n, 3))
+        self._call("rest_sdf_query", self._h, int(solid), n, pts.ctypes.data, C.c_double(safe_dist),
+                   sd.ctypes.data, nrm.ctypes.data)
+        return sd, nrm
 
     def setFluidDensity(self, d):
         self._fluid = (d, getattr(self, "_fluid", (1.0, 0.0))[1])
@@ -182,6 +198,24 @@ def make_solid_desc(radius, center, density, E, nu, velocity=(0, 0, 0), plastic_
     return d, (rest, v, t)
 
 
+_SVOL_DIR = None
+
+
+def sphere_svol_path(radius: float) -> str:
+    """A ".svol" rest SDF of the synthetic sphere of this radius, written
+    once per process into a private temporary directory."""
+    global _SVOL_DIR
+    import tempfile
+    from .svol import sphere_svol
+    if _SVOL_DIR is None:
+        _SVOL_DIR = tempfile.mkdtemp(prefix="esf_svol_")
+    path = os.path.join(_SVOL_DIR, f"sphere_{float(radius)!r}.svol")
+    if not os.path.exists(path):
+        sphere_svol(path + ".tmp", radius)
+        os.replace(path + ".tmp", path)
+    return path
+
+
 def params_from_desc(desc: SceneDesc, precision: int = abi.ESF_FP64) -> abi.Params:
     dh = desc.dh
     p = abi.Params()
@@ -212,17 +246,19 @@ def params_from_desc(desc: SceneDesc, precision: int = abi.ESF_FP64) -> abi.Para
 
 
 def build_from_scene(lib, prefix, desc: SceneDesc, precision=abi.ESF_FP64, noise=True,
-                     stream=None) -> CoupledIntegrator3D:
+                     stream=None, rest_sdf=True) -> CoupledIntegrator3D:
     """APPLICATION::init (main.cpp:63-97) for a synthetic scene: integrator,
     solids, fluid density, init(), smoke carpet, then the seeded fluid noise
     added at nodes without solid mass."""
     res = desc.res
     I = CoupledIntegrator3D(lib, prefix, res, res, res, desc.dh, (0.0, 0.0, 0.0),
                             params_from_desc(desc, precision), stream=stream)
-    for s in desc.solids:
+    for i, s in enumerate(desc.solids):
         d, keep = make_solid_desc(s.radius, s.center, s.density, s.E, s.nu, s.velocity,
                                   s.plastic_yield, s.rotation, s.scaling, s.rotation_matrix)
         I.addSolid(d, keep)
+        if len(desc.solids) > 1 and rest_sdf:
+            I.loadRestSDF(i, sphere_svol_path(s.radius))
     I.setFluidDensity(desc.fluid_density)
     I.setFluidViscocity(0.0)
     I.init()

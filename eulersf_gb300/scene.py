@@ -21,6 +21,9 @@ Inputs that stand in for the reference's shipped assets (meshes/sphere/*):
 * ``solid scaling`` defaults to 1: the reference treats it as a deformation
   of the rest shape (X = R^T (x - T) / s, DEFOR_SOLID_3D.cpp:126-152), so a
   scaled ball starts stretched (F = s I);
+* rest SDF (scenes with more than one solid, for solid-solid contact): the
+  exact distance of the sphere on a DT-Grid narrow band (svol.py) in place of
+  the shipped ``sphere.svol``;
 * fluid noise: U(-a, a) per component at interior nodes from a counter-based
   splitmix64 stream keyed by (seed, node, component), so that C, CUDA and
   numpy produce the same values.
@@ -33,6 +36,8 @@ import struct
 from dataclasses import dataclass, field
 
 import numpy as np
+
+from .svol import sphere_svol
 
 REST_RADIUS = 0.1
 REST_MASS_DH = 0.001
@@ -292,6 +297,8 @@ def write_scene(desc: SceneDesc, directory: str, name: str = "sphere") -> str:
         (res, mdh, morig, mdata), verts, faces = solid_assets(s.radius)
         write_field_gz(os.path.join(directory, f"{name}{i}.mass"), res, mdh, morig, mdata)
         write_obj(os.path.join(directory, f"{name}{i}.obj"), verts, faces)
+        if len(desc.solids) > 1:  # rest SDF for solid-solid contact (main.cpp:146-148)
+            sphere_svol(os.path.join(directory, f"{name}{i}.svol"), s.radius)
     noise = noise_field(desc.res, desc.noise_seed, desc.noise_amplitude)
     noise.astype("<f8").tofile(os.path.join(directory, "noise.f64"))
     return cfg_path

@@ -129,6 +129,8 @@ typedef struct esf_step_report {
   int fp64_stress_cells;      /* mixed: valid cells whose stress was evaluated in FP64
                                  (cond(F) > 1e3); the others use FP32 */
   int valid_cells;            /* valid solid cells of the step's stiffness sweep */
+  int solid_contacts;         /* particles that took a solid-solid contact impulse
+                                 (DEFOR_SOLID_3D.cpp:967-995) */
 } esf_step_report;
 
 /* Field identifiers for esf_get_field / esf_set_field / esf_field_info. */
@@ -201,6 +203,30 @@ esf_status esf_destroy(esf_scene* scene);
 /* new DEFOR_SOLID_3D + setters + COUPLED_INTEGRATOR_3D::addSolid
  * (main.cpp:99-160; COUPLED_INTEGRATOR_3D.h:44). Copies all inputs. */
 esf_status esf_add_solid(esf_scene* scene, const esf_solid_desc* solid);
+/* DEFOR_SOLID_3D::loadRestSDF (DEFOR_SOLID_3D.cpp:210-214; main.cpp:146-148):
+ * the rest-pose signed distance of solid `solid` from a DT-Grid ".svol" file
+ * ("DTG v1.0", SvolLoader_DTTop1.0.h), for solid-solid contact in the
+ * particle update. Scenes with more than one solid need it for every solid
+ * before their first step (esf_step returns ESF_ERR_STATE otherwise).
+ * ESF_ERR_IO on a missing or malformed file, ESF_ERR_UNSUPPORTED for a
+ * rotated volume. */
+esf_status esf_solid_load_rest_sdf(esf_scene* scene, int solid, const char* svol_path);
+/* SPARSE_SDF::signedDistAndCurrentNormal (SPARSE_SDF.cpp:98-117) of a solid
+ * at n rest-space points (host arrays, 3 per point): the signed distance, or
+ * 1 when the point is farther than safe_dist or its surface point lies under
+ * no hashed triangle, and the current unit normal of that triangle (zero
+ * when the distance is 1). The contact test of the particle update alone. */
+esf_status esf_rest_sdf_query(esf_scene* scene, int solid, int n, const double* points,
+                              double safe_dist, double* signed_dist, double* normals);
+/* The dense lattice of a ".svol" rest SDF, on the host (no device needed):
+ * point (x, y, z) for lo <= (x, y, z) < lo + n at
+ * (x - lo[0]) + (y - lo[1]) n[0] + (z - lo[2]) n[0] n[1]; values holds the
+ * band values, codes 1 for band points, -1 where the DT-Grid returns its
+ * inside constant and 0 where it returns the outside constant (constants[0],
+ * constants[1]). Lattice coordinate of a rest point p: (p - translation)/dx.
+ * values and codes NULL: size query. */
+esf_status esf_svol_read(const char* path, int lo[3], int n[3], double* dx, double translation[3],
+                         double constants[2], float* values, signed char* codes, size_t capacity);
 /* COUPLED_INTEGRATOR_3D::setFluidDensity / setFluidViscocity (h:45-46). */
 esf_status esf_set_fluid(esf_scene* scene, double density, double viscosity);
 /* COUPLED_INTEGRATOR_3D::init (COUPLED_INTEGRATOR_3D.cpp:104-135). */

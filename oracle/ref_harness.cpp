@@ -299,7 +299,8 @@ int main(int argc, char** argv) {
   std::string noiseFile;
   int dumpEvery = 1, fullEvery = 1;
   bool noDump = false;
-  std::string restartDir;
+  std::string restartDir, sdfQueryFile;
+  double sdfQuerySafe = 0;
   for (int a = 4; a < argc; a++) {
     std::string s = argv[a];
     if (s == "--noise" && a + 1 < argc) noiseFile = argv[++a];
@@ -307,6 +308,10 @@ int main(int argc, char** argv) {
     else if (s == "--full-every" && a + 1 < argc) fullEvery = atoi(argv[++a]);
     else if (s == "--no-dump") noDump = true;
     else if (s == "--frame-restart" && a + 1 < argc) restartDir = argv[++a];
+    else if (s == "--sdf-query" && a + 2 < argc) {
+      sdfQueryFile = argv[++a];
+      sdfQuerySafe = atof(argv[++a]);
+    }
   }
   mkdir(outdir.c_str(), 0755);
   Eigen::initParallel();
@@ -344,6 +349,33 @@ int main(int argc, char** argv) {
         for (int d = 0; d < 3; d++) integrator->_velocity[i][d] += buf[i * 3 + d];
   }
   double tInit = now_s() - t0;
+
+  // SPARSE_SDF::signedDistAndCurrentNormal of every solid with a rest SDF at
+  // the rest points of the file (raw doubles, 3 per point), after init:
+  // sdfq.solid<s>.npy holds n x 4 (distance, normal)
+  if (!sdfQueryFile.empty()) {
+    FILE* f = fopen(sdfQueryFile.c_str(), "rb");
+    if (!f) return 4;
+    std::vector<double> pts;
+    double buf[3];
+    while (fread(buf, 8, 3, f) == 3) pts.insert(pts.end(), buf, buf + 3);
+    fclose(f);
+    long n = (long)pts.size() / 3;
+    Dumper dq;
+    dq.dir = outdir;
+    dq.prefix = "sdfq.";
+    for (size_t si = 0; si < integrator->_solids.size(); si++) {
+      SPARSE_SDF* sdf = integrator->_solids[si]->_restSDF;
+      if (!sdf) continue;
+      std::vector<double> res(n * 4);
+      for (long i = 0; i < n; i++) {
+        VEC3F p(pts[i * 3], pts[i * 3 + 1], pts[i * 3 + 2]), normal(0, 0, 0);
+        res[i * 4] = sdf->signedDistAndCurrentNormal(p, normal, sdfQuerySafe);
+        for (int k = 0; k < 3; k++) res[i * 4 + 1 + k] = normal[k];
+      }
+      dq.f64(("solid" + std::to_string(si)).c_str(), res.data(), res.size(), {n, 4});
+    }
+  }
 
   Dumper d;
   d.dir = outdir;

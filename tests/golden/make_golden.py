@@ -24,6 +24,10 @@ and its offline mass baking of the shipped sphere (``run_mass``,
     python tests/golden/make_golden.py --frame
     python tests/golden/make_golden.py --mass
 
+and a two-ball scene with solid-solid contact (``run_contact``):
+
+    python tests/golden/make_golden.py --contact
+
 ``--keep DIR`` keeps the harness's raw dumps there and reuses a completed run.
 """
 from __future__ import annotations
@@ -164,6 +168,71 @@ def run_frame(out_dir):
             "N": desc.N, "mass_sample_dh": desc.mass_sample_dh, "vorticity_eps": desc.vorticity_eps,
             "buoyancy": desc.buoyancy, "noise_seed": desc.noise_seed, "frames": frames,
             "flow_rate": desc.flow_rate, "solids": solids}))
+        np.savez_compressed(os.path.join(out_dir, name + ".npz"), **arrays)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+
+
+# Solid-solid contact: two balls moving towards each other, one grid cell
+# apart, so that particles of each come within the contact distance of the
+# other's rest SDF (the scene writer's ".svol" files, read by the reference
+# through SPARSE_SDF) in the first steps. The fixture holds the state of both
+# solids, the system matrix the two assemble together, and the contact query
+# SPARSE_SDF::signedDistAndCurrentNormal alone at seeded rest points around
+# each surface (after init).
+CONTACT_SCENE = ("contact20", SceneDesc(
+    N=20, mass_sample_dh=(1 / 20) / 4, noise_seed=8,
+    solids=[SolidDesc(center=(0.335, 0.5, 0.5), radius=0.15, velocity=(0.8, 0.0, 0.0)),
+            SolidDesc(center=(0.665, 0.52, 0.5), radius=0.15, velocity=(-0.8, 0.0, 0.0))]), 3)
+CONTACT_STEP_FIELDS = ["gridIdxToSolidIdx", "velocity", "lambda1", "solidMass", "solidUnitForce",
+                       "dampedSolidMassVec", "solidVelocityAtDt0", "systemMatrix.indptr",
+                       "systemMatrix.indices", "systemMatrix.data"]
+CONTACT_SOLID_FIELDS = ["valid", "boxes", "mass", "phi", "u", "velocity", "meshVertices"]
+
+
+def contact_query_points(radius, count=4096, seed=5):
+    """Rest points around a sphere's surface: seeded directions at distances
+    within +-0.2 radius of it, the contact band and beyond."""
+    rng = np.random.default_rng(seed)
+    d = rng.standard_normal((count, 3))
+    d /= np.linalg.norm(d, axis=1)[:, None]
+    r = radius * (1 + rng.uniform(-0.2, 0.2, count))
+    return d * r[:, None]
+
+
+def run_contact(out_dir):
+    name, desc, frames = CONTACT_SCENE
+    tmp = tempfile.mkdtemp(prefix="esf_golden_")
+    try:
+        cfg = write_scene(desc, os.path.join(tmp, "scene"))
+        dump = os.path.join(tmp, "dump")
+        pts = contact_query_points(desc.solids[0].radius)
+        qfile = os.path.join(tmp, "query.f64")
+        pts.astype("<f8").tofile(qfile)
+        safe = 0.5 * desc.dh  # "contact safe distance" default
+        subprocess.run([HARNESS, cfg, dump, str(frames), "--noise", os.path.join(tmp, "scene", "noise.f64"),
+                        "--sdf-query", qfile, repr(safe)], check=True,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        arrays = {"sdfq.points": pts, "sdfq.safe": np.array(safe)}
+        for i in range(len(desc.solids)):
+            arrays[f"sdfq.solid{i}"] = np.load(os.path.join(dump, f"sdfq.solid{i}.npy"))
+        log = [json.loads(l) for l in open(os.path.join(dump, "log.jsonl"))][1:]
+        solids = [f"solid{i}." for i in range(len(desc.solids))]
+        for k in range(0, len(log) + 1):
+            step_fields = [f for f in CONTACT_STEP_FIELDS if k == 1 or not f.startswith("systemMatrix")]
+            fields = (INIT_FIELDS if k == 0 else step_fields) + \
+                [sp + f for sp in solids for f in CONTACT_SOLID_FIELDS + (["particles"] if k in (0, len(log)) else [])]
+            for f in fields:
+                p = os.path.join(dump, f"s{k}.{f}.npy")
+                if os.path.exists(p):
+                    arrays[f"s{k}.{f}"] = np.load(p)
+        for l in log:
+            l.pop("seconds", None)
+        arrays["log"] = np.array(json.dumps(log))
+        arrays["scene"] = np.array(json.dumps({
+            "N": desc.N, "mass_sample_dh": desc.mass_sample_dh, "vorticity_eps": desc.vorticity_eps,
+            "buoyancy": desc.buoyancy, "noise_seed": desc.noise_seed, "frames": frames,
+            "flow_rate": desc.flow_rate, "solids": [dict(sd.__dict__) for sd in desc.solids]}))
         np.savez_compressed(os.path.join(out_dir, name + ".npz"), **arrays)
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
@@ -313,6 +382,10 @@ def run_big(name, desc, steps, stored, sample, out_dir, keep=None):
 
 def main():
     args = sys.argv[1:]
+    if args and args[0] == "--contact":
+        run_contact(HERE)
+        print(CONTACT_SCENE[0], os.path.getsize(os.path.join(HERE, CONTACT_SCENE[0] + ".npz")), "bytes")
+        return
     if args and args[0] == "--big":
         keep = None
         if "--keep" in args:
