@@ -63,6 +63,10 @@ class CoupledIntegrator3D {
   const double* origin() const { return grid_.origin; }
 
   void addSolid(const esf_solid_desc& solid) { check(esf_add_solid(scene_, &solid), "esf_add_solid"); }
+  // DEFOR_SOLID_3D::loadRestSDF of solid i (needed by scenes with several solids)
+  void loadRestSDF(int solid, const std::string& svolPath) {
+    check(esf_solid_load_rest_sdf(scene_, solid, svolPath.c_str()), "esf_solid_load_rest_sdf");
+  }
   void setFluidDensity(double d) {
     density_ = d;
     check(esf_set_fluid(scene_, density_, viscosity_), "esf_set_fluid");
