@@ -15,7 +15,7 @@ import os
 import numpy as np
 
 from . import abi
-from .scene import SceneDesc, lame, noise_field, solid_assets
+from .scene import SceneDesc, assets_of, lame, noise_field, solid_assets
 
 
 class CoupledIntegrator3D:
@@ -170,11 +170,13 @@ class CoupledIntegrator3D:
 
 
 def make_solid_desc(radius, center, density, E, nu, velocity=(0, 0, 0), plastic_yield=-1.0,
-                    rotation=(0.0, 0.0, 0.0), scaling=(1.0, 1.0, 1.0), rotation_matrix=None):
-    """Solid descriptor for the synthetic sphere (rest assets from scene.py);
-    `rotation` in the cfg's units (angles / pi), or an exact `rotation_matrix`."""
+                    rotation=(0.0, 0.0, 0.0), scaling=(1.0, 1.0, 1.0), rotation_matrix=None,
+                    assets=None):
+    """Solid descriptor for the synthetic sphere (rest assets from scene.py,
+    or the given (mass field, vertices, triangles)); `rotation` in the cfg's
+    units (angles / pi), or an exact `rotation_matrix`."""
     from .scene import rotation_matrix as _rot
-    (res, mdh, morig, mdata), verts, faces = solid_assets(radius)
+    (res, mdh, morig, mdata), verts, faces = assets if assets is not None else solid_assets(radius)
     lam, mu = lame(E, nu)
     rest = np.ascontiguousarray(mdata.reshape(-1), dtype=np.float64)
     v = np.ascontiguousarray(verts, dtype=np.float64).reshape(-1)
@@ -255,7 +257,8 @@ def build_from_scene(lib, prefix, desc: SceneDesc, precision=abi.ESF_FP64, noise
                             params_from_desc(desc, precision), stream=stream)
     for i, s in enumerate(desc.solids):
         d, keep = make_solid_desc(s.radius, s.center, s.density, s.E, s.nu, s.velocity,
-                                  s.plastic_yield, s.rotation, s.scaling, s.rotation_matrix)
+                                  s.plastic_yield, s.rotation, s.scaling, s.rotation_matrix,
+                                  assets=assets_of(s))
         I.addSolid(d, keep)
         if len(desc.solids) > 1 and rest_sdf:
             I.loadRestSDF(i, sphere_svol_path(s.radius))

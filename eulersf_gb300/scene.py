@@ -75,6 +75,9 @@ class SolidDesc:
     # the 3x3 rotation (row-major) the reference built from `rotation`, when
     # known exactly (golden fixtures); otherwise computed by rotation_matrix()
     rotation_matrix: tuple | None = None
+    # registered rest assets (register_assets) in place of the synthetic
+    # sphere of `radius`, e.g. the reference's shipped mesh and baked mass
+    asset: str = ""
 
 
 @dataclass
@@ -285,6 +288,25 @@ def solid_assets(radius: float):
     return _CACHE[key]
 
 
+_ASSETS = {}
+
+
+def register_assets(name: str, mass_field, verts, faces) -> None:
+    """Rest assets for solids whose ``asset`` names them: the rest mass grid
+    (res, dh, origin, data[z, y, x]) and the closed surface mesh."""
+    _ASSETS[name] = (mass_field, np.asarray(verts, dtype=np.float64),
+                     np.asarray(faces, dtype=np.int32))
+
+
+def assets_of(s: SolidDesc):
+    """(rest mass field, mesh vertices, mesh triangles) of a solid."""
+    if s.asset:
+        if s.asset not in _ASSETS:
+            raise KeyError(f"rest assets {s.asset!r} are not registered")
+        return _ASSETS[s.asset]
+    return solid_assets(s.radius)
+
+
 def write_scene(desc: SceneDesc, directory: str, name: str = "sphere") -> str:
     """Write cfg + assets + noise into ``directory``; returns the cfg path.
     Solid i's assets are ``<name><i>.mass`` and ``<name><i>.obj``."""
@@ -294,7 +316,7 @@ def write_scene(desc: SceneDesc, directory: str, name: str = "sphere") -> str:
     cfg_path = os.path.join(directory, "scene.cfg")
     write_cfg(cfg_path, cfg)
     for i, s in enumerate(desc.solids):
-        (res, mdh, morig, mdata), verts, faces = solid_assets(s.radius)
+        (res, mdh, morig, mdata), verts, faces = assets_of(s)
         write_field_gz(os.path.join(directory, f"{name}{i}.mass"), res, mdh, morig, mdata)
         write_obj(os.path.join(directory, f"{name}{i}.obj"), verts, faces)
         if len(desc.solids) > 1:  # rest SDF for solid-solid contact (main.cpp:146-148)

@@ -15,7 +15,20 @@ for p in (ROOT, os.path.join(ROOT, "oracle")):
 
 from eulersf_gb300.scene import SceneDesc, SolidDesc  # noqa: E402
 
-GOLDEN_SCENES = ["ball16", "ball20_vort", "wall20", "plastic20", "rot20"]
+GOLDEN_SCENES = ["ball16", "ball20_vort", "wall20", "plastic20", "rot20", "shipped20"]
+
+
+def register_shipped_sphere():
+    """The reference's shipped sphere mesh with the rest mass its own
+    rasterizeSolid tool baked (tests/golden/sphere_mass.npz) as the rest
+    assets "shipped_sphere"."""
+    from eulersf_gb300.scene import register_assets
+    z = np.load(os.path.join(GOLDEN, "sphere_mass.npz"))
+    res = [int(v) for v in z["res"]]
+    n = res[0] * res[1] * res[2]
+    data = np.unpackbits(z["solid"])[:n].astype(np.float64) * float(z["density"])
+    register_assets("shipped_sphere", (res, float(z["dh"]), z["origin"].astype(np.float64),
+                                       data.reshape(res[2], res[1], res[0])), z["vertices"], z["triangles"])
 
 # bit-exact integer/flag fields (the reference's DOF maps, cell flags, boxes)
 EXACT = ["gridIdxToSolutionIdx", "gridIdxToSolidIdx", "solid0.valid", "solid0.boxes"]
@@ -39,7 +52,10 @@ def load_golden(name):
                         plastic_yield=s.get("plastic_yield", -1.0),
                         rotation=tuple(s.get("rotation", (0.0, 0.0, 0.0))),
                         scaling=tuple(s.get("scaling", (1.0, 1.0, 1.0))),
-                        rotation_matrix=s.get("rotation_matrix")) for s in meta["solids"]]
+                        rotation_matrix=s.get("rotation_matrix"),
+                        asset=s.get("asset", "")) for s in meta["solids"]]
+    if any(s.asset == "shipped_sphere" for s in solids):
+        register_shipped_sphere()
     desc = SceneDesc(N=meta["N"], mass_sample_dh=meta["mass_sample_dh"],
                      vorticity_eps=meta["vorticity_eps"], buoyancy=meta["buoyancy"],
                      noise_seed=meta["noise_seed"], flow_rate=meta.get("flow_rate", 0.5),

@@ -72,7 +72,24 @@ def scenes():
                               solids=[SolidDesc(center=(0.5, 0.55, 0.5), radius=0.12,
                                                 rotation=(0.1, 0.25, 0.4),
                                                 scaling=(1.05, 0.95, 1.0))]), 2)
+    # the reference's shipped sphere (meshes/sphere/sphere.obj) with the rest
+    # mass its own rasterizeSolid tool baked (sphere_mass.npz, made by --mass)
+    out["shipped20"] = (SceneDesc(N=20, mass_sample_dh=(1 / 20) / 4, noise_seed=2,
+                                  solids=[SolidDesc(center=(0.5, 0.6, 0.5), radius=0.0995,
+                                                    asset="shipped_sphere")]), 2)
     return out
+
+
+def register_shipped_sphere():
+    """The shipped sphere's mesh and tool-baked mass (sphere_mass.npz) as the
+    rest assets "shipped_sphere"."""
+    from eulersf_gb300.scene import register_assets
+    z = np.load(os.path.join(HERE, "sphere_mass.npz"))
+    res = [int(v) for v in z["res"]]
+    n = res[0] * res[1] * res[2]
+    data = np.unpackbits(z["solid"])[:n].astype(np.float64) * float(z["density"])
+    register_assets("shipped_sphere", (res, float(z["dh"]), z["origin"].astype(np.float64),
+                                       data.reshape(res[2], res[1], res[0])), z["vertices"], z["triangles"])
 
 
 INIT_FIELDS = ["gridIdxToSolutionIdx", "gridIdxToSolidIdx", "velocity", "intensity", "solidMass",
@@ -382,6 +399,7 @@ def run_big(name, desc, steps, stored, sample, out_dir, keep=None):
 
 def main():
     args = sys.argv[1:]
+    register_shipped_sphere()
     if args and args[0] == "--contact":
         run_contact(HERE)
         print(CONTACT_SCENE[0], os.path.getsize(os.path.join(HERE, CONTACT_SCENE[0] + ".npz")), "bytes")
