@@ -302,11 +302,12 @@ esf_status esf_pressure_solve_batch(int n, const esf_grid* grids, const double* 
  * allocated, freed or created (no stream, event or graph). The first call on
  * each device, and the first after that device's context has been re-created
  * (cudaDeviceReset), looks up the array's device address with
- * cudaGetSymbolAddress, which can load the module's device code: that first
- * call should come before any stream capture. One scratch per device: calls
+ * cudaGetSymbolAddress, which can load the module's device code. One
+ * scratch per device: calls
  * that overlap on the same device, from two host threads or two streams, race
  * on it and must be serialised by the caller; each call clears what it needs
- * zeroed. Returns when the solve has finished on `stream`. */
+ * zeroed. The call synchronises `stream` and returns when the solve has
+ * finished on it. */
 #define ESF_STATIC_SOLVE_MAX_CELLS (64 * 64 * 64)
 #define ESF_STATIC_SOLVE_MAX_DEVICES 64
 esf_status esf_pressure_solve_static(const esf_grid* grid, const double* mass_inv_node,
