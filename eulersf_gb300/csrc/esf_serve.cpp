@@ -19,6 +19,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -45,6 +46,7 @@ struct SolidCopy {
   esf_solid_desc d;
   std::vector<double> rest, verts;
   std::vector<int> tris;
+  std::string sdfPath;  // rest SDF of solid-solid contact, or empty
 };
 
 struct Request {
@@ -114,8 +116,12 @@ struct esf_server {
     esf_status e = esf_create(&r->grid, &r->params, nullptr, &r->scene);
     if (e) return e;
     if (batcher && (e = esf::scene_set_batcher(r->scene, batcher))) return e;
-    for (auto& s : r->solids)
-      if ((e = esf_add_solid(r->scene, &s->d))) return e;
+    for (size_t i = 0; i < r->solids.size(); i++) {
+      if ((e = esf_add_solid(r->scene, &r->solids[i]->d))) return e;
+      if (!r->solids[i]->sdfPath.empty() &&
+          (e = esf_solid_load_rest_sdf(r->scene, (int)i, r->solids[i]->sdfPath.c_str())))
+        return e;
+    }
     if ((e = esf_set_fluid(r->scene, r->density, r->viscosity))) return e;
     if ((e = esf_init(r->scene))) return e;
     const int X = r->grid.xRes, Y = r->grid.yRes, Z = r->grid.zRes;
@@ -265,6 +271,11 @@ extern "C" esf_status esf_server_submit(esf_server* s, const esf_request* q, uin
     c->d.rest_mass = c->rest.data();
     c->d.vertices = c->verts.data();
     c->d.triangles = c->tris.data();
+    if (q->rest_sdf_paths && q->rest_sdf_paths[i]) c->sdfPath = q->rest_sdf_paths[i];
+    if (q->num_solids > 1 && c->sdfPath.empty()) {
+      esf::set_error("esf_server_submit: solid %d of a scene with several solids has no rest SDF path", i);
+      return ESF_ERR_INVALID_ARG;
+    }
     r->solids.push_back(std::move(c));
   }
   r->footprint = esf_scene_footprint(&q->grid, &q->params, q->num_solids, q->solids);

@@ -44,7 +44,8 @@ class Request(C.Structure):
     _fields_ = [("grid", abi.Grid), ("params", abi.Params), ("num_solids", C.c_int),
                 ("solids", C.POINTER(abi.SolidDesc)), ("fluid_density", C.c_double),
                 ("fluid_viscosity", C.c_double), ("smoke_carpet", C.c_double),
-                ("noise_seed", C.c_ulonglong), ("noise_amplitude", C.c_double), ("steps", C.c_int)]
+                ("noise_seed", C.c_ulonglong), ("noise_amplitude", C.c_double), ("steps", C.c_int),
+                ("rest_sdf_paths", C.POINTER(C.c_char_p))]
 
 
 class RequestStatus(C.Structure):
@@ -79,10 +80,12 @@ def request_for(desc, steps: int, precision: int = abi.ESF_MIXED):
     integrator.build_from_scene: the same params, solids, carpet and noise.
     Returns (request, keep-alive objects)."""
     from .integrator import make_solid_desc, params_from_desc
+    from .scene import assets_of
     descs, keep = [], []
     for s in desc.solids:
         d, k = make_solid_desc(s.radius, s.center, s.density, s.E, s.nu, s.velocity,
-                               s.plastic_yield, s.rotation, s.scaling, s.rotation_matrix)
+                               s.plastic_yield, s.rotation, s.scaling, s.rotation_matrix,
+                               assets=assets_of(s))
         descs.append(d)
         keep.extend(k)
     arr = (abi.SolidDesc * len(descs))(*descs)
@@ -98,6 +101,11 @@ def request_for(desc, steps: int, precision: int = abi.ESF_MIXED):
     q.noise_seed = desc.noise_seed
     q.noise_amplitude = desc.noise_amplitude
     q.steps = steps
+    if len(desc.solids) > 1:  # rest SDFs for solid-solid contact
+        from .integrator import sphere_svol_path
+        paths = (C.c_char_p * len(desc.solids))(*[sphere_svol_path(s.radius).encode() for s in desc.solids])
+        q.rest_sdf_paths = C.cast(paths, C.POINTER(C.c_char_p))
+        keep.append(paths)
     return q, (arr, keep)
 
 

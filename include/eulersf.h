@@ -370,6 +370,9 @@ typedef struct esf_request {
   unsigned long long noise_seed; /* fluid noise U(-a, a) per component at interior nodes */
   double noise_amplitude;        /* without solid mass, added after init; 0: none */
   int steps;                     /* stepImplicit calls */
+  const char* const* rest_sdf_paths; /* per solid, a ".svol" rest SDF (esf_solid_load_rest_sdf):
+                                        the paths are copied at submit and the files read when
+                                        the scene starts; required when num_solids > 1, else NULL */
 } esf_request;
 typedef enum esf_request_state {
   ESF_REQ_QUEUED = 0,

@@ -87,3 +87,30 @@ def test_batched_and_unbatched_serving_agree(gpu_lib):
     for (va, ia), (vb, ib) in zip(out[True], out[False]):
         assert ia == ib
         assert np.array_equal(va, vb)
+
+
+def test_two_solid_request_equals_solo_run(gpu_lib):
+    """A served scene with two solids (each with its rest SDF path in the
+    request) gives the same bits as the same scene stepped alone; a
+    two-solid request without rest SDF paths is refused at submit."""
+    import eulersf_gb300 as E
+    from common import load_golden
+    from eulersf_gb300.serve import ESF_REQ_DONE, Server, request_for
+    desc, _, _ = load_golden("contact20")
+    steps = 2
+    with Server(max_active=2) as srv:
+        t = srv.submit(desc, steps, abi.ESF_FP64)
+        st = srv.wait(t)
+        assert st["state"] == ESF_REQ_DONE and st["steps_done"] == steps, st
+        vel = srv.get(t, "velocity", desc.res ** 3 * 3)
+        srv.release(t)
+        q, keep = request_for(desc, steps, abi.ESF_FP64)
+        q.rest_sdf_paths = None
+        tk = C.c_uint64()
+        assert srv._lib.esf_server_submit(srv._h, C.byref(q), C.byref(tk)) == 1  # ESF_ERR_INVALID_ARG
+        del keep
+    G = E.make_scene(desc)
+    for _ in range(steps):
+        G.stepImplicit()
+    assert np.array_equal(vel, G.get("velocity"))
+    G.close()
