@@ -98,6 +98,17 @@ bool swap_for(const std::string& endian) {
   return (endian == "LittleEndian") != host_little_endian();
 }
 
+// bytes left in the stream (a malformed count must not size an allocation
+// beyond the file)
+long long remaining(std::istream& is) {
+  const std::streampos here = is.tellg();
+  if (here < 0) return 0;
+  is.seekg(0, std::ios_base::end);
+  const std::streampos end = is.tellg();
+  is.seekg(here);
+  return end < here ? 0 : (long long)(end - here);
+}
+
 // running run-length sums: aa[j] = values before run j
 std::vector<long long> build_aa(const std::vector<long long>& idx) {
   std::vector<long long> aa(idx.size() / 2 + 1);
@@ -151,12 +162,14 @@ esf_status svol_read(const char* path, SvolLattice* L) {
   long long numVa3D = 0;
   for (int lev = 0; lev < 3 && ok; lev++) {
     long long num = 0;
-    ok = read_uints(is, intSize, swap, &num, 1) && num >= 0 && num < (1LL << 31) && num % 2 == 0;
+    ok = read_uints(is, intSize, swap, &num, 1) && num >= 0 && num < (1LL << 31) && num % 2 == 0 &&
+         num * indexSize <= remaining(is);
     if (!ok) break;
     idx[lev].resize((size_t)num);
     ok = read_ints(is, indexSize, swap, idx[lev].data(), (size_t)num);
     long long nva = 0;
-    ok = ok && read_uints(is, intSize, swap, &nva, 1) && nva >= 0 && nva < (1LL << 31);
+    ok = ok && read_uints(is, intSize, swap, &nva, 1) && nva >= 0 && nva < (1LL << 31) &&
+         (lev == 2 || nva * intSize <= remaining(is));
     if (!ok) break;
     if (lev < 2) {
       va[lev].resize((size_t)nva);
@@ -204,6 +217,10 @@ esf_status svol_read(const char* path, SvolLattice* L) {
     if (name == "insideConstant") inC = v;
     if (name == "outsideConstant") outC = v;
     std::getline(is, line);
+  }
+  if (!is || (dataSize != 4 && dataSize != 8) || numVa3D * dataSize > remaining(is)) {
+    set_error("svol_read: %s: truncated values", path);
+    return ESF_ERR_IO;
   }
   std::vector<double> values((size_t)numVa3D);
   if (!is || !read_reals(is, dataSize, swap_for(endian2), values.data(), values.size()) || !(dx > 0)) {
@@ -307,7 +324,7 @@ void svol_to_grid(const SvolLattice& L, const double* p, double* g) {
 // rest bounding box (TRIANGLE::boundingBox) in lattice indices, grown by one
 // (DTGrid::boundingBoxIndices: floor - 1 .. ceil + 1); band points in it
 // list the triangle.
-void svol_hash_triangles(const SvolLattice& L, const double* rest, int ntri, const int* tris,
+bool svol_hash_triangles(const SvolLattice& L, const double* rest, int ntri, const int* tris,
                          std::vector<int>* off, std::vector<int>* ids) {
   const long long nxy = (long long)L.n[0] * L.n[1];
   const long long total = nxy * L.n[2];
@@ -339,12 +356,19 @@ void svol_hash_triangles(const SvolLattice& L, const double* rest, int ntri, con
           if (L.code[(size_t)q] == 1) fn(q);
         }
   };
-  for (int t = 0; t < ntri; t++) for_points(t, [&](long long q) { count[(size_t)q + 1]++; });
+  long long entries = 0;
+  for (int t = 0; t < ntri; t++)
+    for_points(t, [&](long long q) {
+      count[(size_t)q + 1]++;
+      entries++;
+    });
+  if (entries >= (1LL << 31) - 1) return false;  // offsets are 32-bit
   off->assign((size_t)total + 1, 0);
   for (long long q = 0; q < total; q++) (*off)[(size_t)q + 1] = (*off)[(size_t)q] + count[(size_t)q + 1];
   ids->assign((size_t)(*off)[(size_t)total] + 1, 0);
   std::vector<int> fill(off->begin(), off->end() - 1);
   for (int t = 0; t < ntri; t++) for_points(t, [&](long long q) { (*ids)[(size_t)fill[(size_t)q]++] = t; });
+  return true;
 }
 
 }  // namespace esf

@@ -21,8 +21,9 @@ esf_status svol_read(const char* path, SvolLattice* L);
 // lattice coordinates of a rest-space point (DTGrid worldToGrid)
 void svol_to_grid(const SvolLattice& L, const double* p, double* g);
 // per lattice point, the triangles whose rest bounding box covers it, in
-// triangle order: CSR offsets (points + 1) and ids
-void svol_hash_triangles(const SvolLattice& L, const double* rest, int ntri, const int* tris,
+// triangle order: CSR offsets (points + 1) and ids; false when the lists
+// would hold 2^31 entries or more
+bool svol_hash_triangles(const SvolLattice& L, const double* rest, int ntri, const int* tris,
                          std::vector<int>* off, std::vector<int>* ids);
 
 }  // namespace esf

@@ -198,6 +198,10 @@ extern "C" size_t esf_scene_footprint(const esf_grid* g, const esf_params* p, in
   // (estimate / measured = 1.07, 1.00, 0.99 for a 0.2-radius ball), plus
   // the one-pass FP32 iteration's second set of r, t, q (12 bytes a row)
   double bytes = T * (520.0 + 240.0 * ns) + R * 192.0;
+  // scenes with several solids: each further solid's cell -> valid-cell map,
+  // and every solid's rest-SDF lattice with its triangle lists (~21 MB for
+  // the shipped sphere's volume)
+  if (ns > 1) bytes += R * 4.0 * (ns - 1) + ns * 24.0e6;
   for (int i = 0; i < ns && solids; i++) {
     // solid nodes and particles from the scaled mesh's bounding box
     const esf_solid_desc& d = solids[i];

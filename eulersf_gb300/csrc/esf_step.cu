@@ -536,7 +536,10 @@ extern "C" esf_status esf_solid_load_rest_sdf(esf_scene* sc, int solid, const ch
   SvolLattice L;
   TRY(svol_read(path, &L));
   std::vector<int> off, ids;
-  svol_hash_triangles(L, d->restPose.data(), d->ntri, d->tris.data(), &off, &ids);
+  if (!svol_hash_triangles(L, d->restPose.data(), d->ntri, d->tris.data(), &off, &ids)) {
+    set_error("esf_solid_load_rest_sdf: %s: the mesh's triangle lists on this lattice exceed 2^31 entries", path);
+    return ESF_ERR_UNSUPPORTED;
+  }
   TRY(d->sdfVal.ensure(L.val.size() * 4));
   TRY(d->sdfCode.ensure(L.code.size()));
   TRY(d->sdfOff.ensure(off.size() * 4));
