@@ -112,12 +112,6 @@ struct PcrState {
   int cap;           // inner mode: iterations between replacements (0 = none)
   int pp;            // one-pass FP32 iteration: which buffer set holds r, t, q
   unsigned int ticket[4];
-  // one-pass iteration with the two-level preconditioner: the pass leaves
-  // (s', t_D'), (s', q) and whether it was the set-up pass; the coarse
-  // kernel adds (s', Z F Z^T s') and forms alpha, omega = (Ap, M^-1 Ap)
-  double muD, nu, omega;
-  int wasSetup;
-  unsigned int coTicket;  // last-block ticket of the coarse kernel
 };
 
 // Solid system layout ("sliced"): the 27 neighbour 3x3 blocks of solid node a,

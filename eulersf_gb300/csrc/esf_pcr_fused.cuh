@@ -59,8 +59,7 @@ constexpr int FU_OFF_A = FU_OFF_SQ + TW_PP * HY * 4;
 constexpr int FU_OFF_B = FU_OFF_A + TW_NP * NYN * 4;
 constexpr int FU_OFF_C = FU_OFF_B + TW_NP * NYN * 4;
 constexpr int FU_OFF_RED = (FU_OFF_C + TW_NP * NYN * 4 + 15) / 16 * 16;
-constexpr int FU_OFF_H = FU_OFF_RED + 32 * 8;  // two-level: per warp, half-warp pattern sums
-constexpr int FU_SMEM = FU_OFF_H + (NT / 32) * 2 * 8 * 4;  // about 48 KB: four blocks per SM
+constexpr int FU_SMEM = FU_OFF_RED + 32 * 8;  // about 47 KB: four blocks per SM
 constexpr int FU_SUMS = 4;                    // delta, mu, nu, omega
 
 // Scalars after a fused pass: totals of (r', s'), (s', t'), (s', q), (Ap, q).
@@ -97,49 +96,13 @@ __device__ __forceinline__ void finish_fused(PcrState* st, double dl, double mu,
   }
 }
 
-// Scalars after a pass of the two-level variant: as finish_fused, but alpha
-// (which needs the coarse part of (s', M^-1 s')) is left to the coarse kernel.
-__device__ __forceinline__ void finish_fused_coarse(PcrState* st, double dl, double mu, double nu) {
-  st->wasSetup = st->setup;
-  if (st->setup) {
-    st->delta = dl;
-    st->delta0 = dl;
-    st->beta = 0.0;
-    st->setup = 0;
-    st->iter0 = st->iter;
-    if (!(dl > 0.0)) {
-      st->converged = 1;
-      st->done = 1;
-    }
-  } else {
-    st->beta = dl / st->delta;
-    st->delta = dl;
-    st->iter++;
-    if (dl <= st->eps * st->eps * st->delta0 || (st->cap > 0 && st->iter - st->iter0 >= st->cap)) {
-      st->converged = 1;
-      st->done = 1;
-    }
-  }
-  st->muD = mu;
-  st->nu = nu;
-  st->pp ^= 1;
-  if (!(dl == dl) || !(mu == mu) || !(nu == nu)) {
-    st->status = ESF_ERR_NUMERIC;
-    st->done = 1;
-  }
-}
-
 // One block's share of a pass: the 64 x 8-cell column (bx, by) over the cell
 // layers bz*cz .. bz*cz+cz-1 of the scene (g, tm, p, partial, st), whose
 // pass has nb blocks; bid is this block's place among them (the order in
-// which the last block folds the partial sums). CO: the two-level
-// preconditioner (esf_coarse.cuh): t is read as s/diag + (Z c)(cell), s' is
-// summed against the block patterns, and alpha is left to the coarse kernel.
-template <bool CO>
+// which the last block folds the partial sums).
 __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm, const FusedPtrs& p,
                                            double* partial, PcrState* st, int cz, int bx, int by,
-                                           int bz, int nb, int bid, unsigned char* smem,
-                                           const CoarseArgs& co) {
+                                           int bz, int nb, int bid, unsigned char* smem) {
   unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem + FU_OFF_BAR);
   float* sP = reinterpret_cast<float*>(smem + FU_OFF_P);
   float* sQ = reinterpret_cast<float*>(smem + FU_OFF_SQ);
@@ -224,39 +187,6 @@ __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm
   float prev0 = 0, prev1 = 0, prevE = 0, vOwn0 = 0, vOwn1 = 0;
   float qCur0 = 0, qCur1 = 0, ivCur0 = 0, ivCur1 = 0;
   float mpx0 = 0, mpy0 = 0, mpz0 = 0, mpx1 = 0, mpy1 = 0, mpz1 = 0, mpxE = 0, mpyE = 0, mpzE = 0;
-  // two-level: the coarse factors of the thread's own pair and ring cell for
-  // the current z-block, and its pattern sums of s' for the current z-block
-  const int bs = CO ? co.bs : 1;
-  const float syOwn = (cgy & 1) ? -1.0f : 1.0f;
-  const int xe = x0 - 1 + eh, ye = y0 - 1 + ey;
-  const bool eIn = hasE && xe >= 0 && xe < g.cX && ye >= 0 && ye < g.cY;
-  const float syE = (ye & 1) ? -1.0f : 1.0f, sxE = (xe & 1) ? -1.0f : 1.0f;
-  int zbOwn = -1, zbE = -1;
-  float fo0 = 0, fo1 = 0, fo2 = 0, fo3 = 0, fe0 = 0, fe1 = 0, fe2 = 0, fe3 = 0;
-  float hP = 0, hQ = 0, hPz = 0, hQz = 0;
-  const int zbFirst = z0 / bs;
-  float* sH = reinterpret_cast<float*>(smem + FU_OFF_H);
-  // the block's pattern sums of z-block zb, half-warp (32 cells) by half-warp
-  auto co_flush = [&](int zb) {
-    float v[8] = {hP, hQ, syOwn * hP, syOwn * hQ, hPz, hQz, syOwn * hPz, syOwn * hQz};
-#pragma unroll
-    for (int k = 0; k < 8; k++)
-#pragma unroll
-      for (int o = 8; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-    if ((lane & 15) == 0) {
-#pragma unroll
-      for (int k = 0; k < 8; k++) sH[((w << 1) + (lane >> 4)) * 8 + k] = v[k];
-    }
-    __syncthreads();
-    if (tid < 16) {
-      const int half = tid >> 3, k = tid & 7;
-      float a = 0.0f;
-      for (int ww = 0; ww < NT / 32; ww++) a += sH[((ww << 1) + half) * 8 + k];
-      co.hpart[(long long)bid * CO_PART + (zb - zbFirst) * 16 + half * 8 + k] = a;
-    }
-    __syncthreads();
-    hP = hQ = hPz = hQz = 0.0f;
-  };
   bool ok = true;
   int landed = 0;
   int issued = TMA_STAGES < nsteps ? TMA_STAGES : nsteps;
@@ -275,19 +205,8 @@ __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm
     // (a) r' = r - alpha (t + beta q) at the tile and halo cells of layer kk
     {
       const float2 r2 = *reinterpret_cast<const float2*>(R + bM);
-      float2 t2 = *reinterpret_cast<const float2*>(Tt + bM);
+      const float2 t2 = *reinterpret_cast<const float2*>(Tt + bM);
       const float2 q2 = *reinterpret_cast<const float2*>(Qq + bM);
-      if (CO && cin && kk >= 0 && kk < g.cZ) {  // t = s/diag + (Z c) at the pair (sx = +1, -1)
-        const int zb = kk / bs;
-        if (zb != zbOwn) {
-          coarse_factors(co, cgx / bs, cgy / bs, zb, syOwn, fo0, fo1, fo2, fo3);
-          zbOwn = zb;
-        }
-        const float sz = (kk & 1) ? -1.0f : 1.0f;
-        const float A = __fmaf_rn(sz, fo1, fo0), B = __fmaf_rn(sz, fo3, fo2);
-        t2.x += A + B;
-        t2.y += A - B;
-      }
       const float qn0 = __fmaf_rn(beta, q2.x, t2.x), qn1 = __fmaf_rn(beta, q2.y, t2.y);
       const float v0 = __fmaf_rn(-alpha, qn0, r2.x), v1 = __fmaf_rn(-alpha, qn1, r2.y);
       *reinterpret_cast<float2*>(sP + pM) = make_float2(prev0 + v0, prev1 + v1);
@@ -308,11 +227,9 @@ __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm
         *reinterpret_cast<float2*>(rOut + o) = make_float2(v0, v1);
         *reinterpret_cast<float2*>(qOut + o) = make_float2(qn0, qn1);
         // (Ap, q) = (q diag, q); an approximate quotient is plenty for a sum
-        // that only sets the step length (two-level: omega by recurrence)
-        if (!CO) {
-          if (iv.x > 0.0f) sOm += __fdividef(qn0 * qn0, iv.x);
-          if (iv.y > 0.0f) sOm += __fdividef(qn1 * qn1, iv.y);
-        }
+        // that only sets the step length
+        if (iv.x > 0.0f) sOm += __fdividef(qn0 * qn0, iv.x);
+        if (iv.y > 0.0f) sOm += __fdividef(qn1 * qn1, iv.y);
         qCur0 = qn0;
         qCur1 = qn1;
         ivCur0 = iv.x;
@@ -320,17 +237,7 @@ __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm
       }
     }
     if (hasE) {
-      float te = Tt[bE];
-      if (CO && eIn && kk >= 0 && kk < g.cZ) {
-        const int zb = kk / bs;
-        if (zb != zbE) {
-          coarse_factors(co, xe / bs, ye / bs, zb, syE, fe0, fe1, fe2, fe3);
-          zbE = zb;
-        }
-        const float sz = (kk & 1) ? -1.0f : 1.0f;
-        te += __fmaf_rn(sxE, __fmaf_rn(sz, fe3, fe2), __fmaf_rn(sz, fe1, fe0));
-      }
-      const float v = __fmaf_rn(-alpha, __fmaf_rn(beta, Qq[bE], te), R[bE]);
+      const float v = __fmaf_rn(-alpha, __fmaf_rn(beta, Qq[bE], Tt[bE]), R[bE]);
       sP[pE] = prevE + v;
       sQ[pE] = prevE - v;
       prevE = v;
@@ -383,7 +290,6 @@ __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm
       issued = i + TMA_STAGES + 1;
     }
     // (c) s' and t' = s'/diag at the tile's cells of layer kk-1
-    if (CO && kk >= z0 + 2 && (kk - 1) % bs == 0) co_flush((kk - 1) / bs - 1);  // a z-block is complete
     if (kk >= z0 + 1 && cin) {
       const float2 A01 = *reinterpret_cast<const float2*>(sA + aN);
       const float A2 = sA[aN + 2];
@@ -410,14 +316,6 @@ __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm
       sDl += vOwn0 * o0 + vOwn1 * o1;
       sMu += o0 * t0 + o1 * t1;
       sNu += o0 * qPrev0 + o1 * qPrev1;
-      if (CO) {
-        const float P = o0 + o1, Q = o0 - o1;
-        const bool odd = ((kk - 1) & 1) != 0;
-        hP += P;
-        hQ += Q;
-        hPz += odd ? -P : P;
-        hQz += odd ? -Q : Q;
-      }
     }
   }
   if (__syncthreads_or(!ok)) {
@@ -429,7 +327,6 @@ __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm
     }
     return;
   }
-  if (CO) co_flush((z1 - 1) / bs);
   // the four sums: block partials, folded in block order by the last block
   const double pDl = block_sum<NT>((double)sDl, sred);
   const double pMu = block_sum<NT>((double)sMu, sred);
@@ -455,19 +352,17 @@ __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm
   const double tDl = fold(0), tMu = fold(1), tNu = fold(2), tOm = fold(3);
   if (tid == 0) {
     st->ticket[1] = 0;
-    if (CO) finish_fused_coarse(st, tDl, tMu, tNu);
-    else finish_fused(st, tDl, tMu, tNu, tOm);
+    finish_fused(st, tDl, tMu, tNu, tOm);
   }
 }
 
-template <bool CO>
 __global__ void __launch_bounds__(NT, 4) pcr_iteration_fused(GridDev g, const __grid_constant__ FusedMaps tm,
                                                              FusedPtrs p, double* partial, PcrState* st,
-                                                             int cz, CoarseArgs co) {
+                                                             int cz) {
   extern __shared__ __align__(128) unsigned char smem[];
-  fused_pass<CO>(g, tm, p, partial, st, cz, blockIdx.x, blockIdx.y, blockIdx.z,
-                 gridDim.x * gridDim.y * gridDim.z,
-                 blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z), smem, co);
+  fused_pass(g, tm, p, partial, st, cz, blockIdx.x, blockIdx.y, blockIdx.z,
+             gridDim.x * gridDim.y * gridDim.z,
+             blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z), smem);
 }
 
 // ---- several scenes' inner solves in one launch (continuous batching).
@@ -510,8 +405,7 @@ __global__ void __launch_bounds__(NT, 4) pcr_iteration_fused_batch(const FusedTa
   const int nb = t.gx * t.gy * t.gz;
   if (local >= nb) return;
   const int bx = local % t.gx, by = (local / t.gx) % t.gy, bz = local / (t.gx * t.gy);
-  const CoarseArgs none{};
-  fused_pass<false>(t.g, t.tm, t.p, t.partial, t.st, t.cz, bx, by, bz, nb, local, smem, none);
+  fused_pass(t.g, t.tm, t.p, t.partial, t.st, t.cz, bx, by, bz, nb, local, smem);
 }
 
 // The states of a batch's tasks, in list order, for one copy to the host.

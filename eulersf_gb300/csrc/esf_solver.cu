@@ -8,11 +8,8 @@
 //    every 5th iteration, with all scalars kept on the device and the
 //    iteration chunks replayed as CUDA graphs;
 //  * FP32 inner solves inside FP64 iterative refinement (ESF_MIXED), one
-//    TMA-staged kernel per inner iteration (esf_pcr_fused.cuh), with a
-//    two-level preconditioner on the grid's sign-pattern modes
-//    (esf_coarse.cuh);
+//    TMA-staged kernel per inner iteration (esf_pcr_fused.cuh);
 //  * the solid system (M + dt^2 K) in 27-neighbour 3x3 block rows.
-#include <dlfcn.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -353,81 +350,7 @@ __global__ void __launch_bounds__(NT) pressure_stencil(GridDev g, StencilArgs<T>
 }
 
 #include "esf_tma.cuh"
-#include "esf_coarse.cuh"
 #include "esf_pcr_fused.cuh"
-
-// ---- two-level preconditioner: host side
-// cuSOLVER's dense Cholesky, loaded at run time (libcusolver.so.12); without
-// it the inner solves keep the Jacobi preconditioner alone.
-struct CusolverApi {
-  int (*create)(void**);
-  int (*setStream)(void*, cudaStream_t);
-  int (*potrfSize)(void*, int, int, double*, int, int*);
-  int (*potrf)(void*, int, int, double*, int, double*, int, int*);
-  int (*potriSize)(void*, int, int, double*, int, int*);
-  int (*potri)(void*, int, int, double*, int, double*, int, int*);
-  int (*destroy)(void*);
-  bool ok;
-};
-static const CusolverApi& cusolver_api() {
-  static const CusolverApi api = [] {
-    CusolverApi a;
-    memset(&a, 0, sizeof a);
-    void* lib = dlopen("libcusolver.so.12", RTLD_NOW | RTLD_LOCAL);
-    if (!lib) lib = dlopen("libcusolver.so", RTLD_NOW | RTLD_LOCAL);
-    if (!lib) return a;
-    a.create = reinterpret_cast<int (*)(void**)>(dlsym(lib, "cusolverDnCreate"));
-    a.setStream = reinterpret_cast<int (*)(void*, cudaStream_t)>(dlsym(lib, "cusolverDnSetStream"));
-    a.potrfSize = reinterpret_cast<int (*)(void*, int, int, double*, int, int*)>(
-        dlsym(lib, "cusolverDnDpotrf_bufferSize"));
-    a.potrf = reinterpret_cast<int (*)(void*, int, int, double*, int, double*, int, int*)>(
-        dlsym(lib, "cusolverDnDpotrf"));
-    a.potriSize = reinterpret_cast<int (*)(void*, int, int, double*, int, int*)>(
-        dlsym(lib, "cusolverDnDpotri_bufferSize"));
-    a.potri = reinterpret_cast<int (*)(void*, int, int, double*, int, double*, int, int*)>(
-        dlsym(lib, "cusolverDnDpotri"));
-    a.destroy = reinterpret_cast<int (*)(void*)>(dlsym(lib, "cusolverDnDestroy"));
-    a.ok = a.create && a.setStream && a.potrfSize && a.potrf && a.potriSize && a.potri && a.destroy;
-    return a;
-  }();
-  return api;
-}
-constexpr int CUBLAS_LOWER = 0;  // cublasFillMode_t CUBLAS_FILL_MODE_LOWER
-
-struct CoarseWork {
-  CoarseArgs a;        // ct points at c, hpart at hpart
-  int K = 0;
-  long long R = 0;
-  float *F = nullptr, *c = nullptr, *h = nullptr, *hpart = nullptr, *c0 = nullptr, *h0 = nullptr;
-  float *v = nullptr, *y = nullptr;
-  unsigned long long* Eint = nullptr;
-  double *E64 = nullptr, *work = nullptr, *partial = nullptr;
-  unsigned long long* dmax = nullptr;
-  unsigned* fmax = nullptr;
-  int* info = nullptr;
-  int lwork = 0;
-  long long hpartBlocks = 0;
-  void* solver = nullptr;
-};
-
-static void coarse_free(CoarseWork* c) {
-  if (!c) return;
-  if (c->solver) cusolver_api().destroy(c->solver);
-  for (void* p : {(void*)c->F, (void*)c->c, (void*)c->h, (void*)c->hpart, (void*)c->c0, (void*)c->h0,
-                  (void*)c->v, (void*)c->y, (void*)c->Eint, (void*)c->E64, (void*)c->work,
-                  (void*)c->partial, (void*)c->dmax, (void*)c->fmax, (void*)c->info})
-    cudaFree(p);
-  delete c;
-}
-
-// Block size: the smallest multiple of 32 cells whose blocks give at most
-// 4096 coarse unknowns (8 patterns a block).
-static int coarse_block(const GridDev& g) {
-  for (int bs = 32;; bs += 32) {
-    const long long k = 8LL * ((g.cX + bs - 1) / bs) * ((g.cY + bs - 1) / bs) * ((g.cZ + bs - 1) / bs);
-    if (k <= 4096) return bs;
-  }
-}
 
 // ------------------------------------------------------- vector kernels
 constexpr int VT = 256;
@@ -608,7 +531,7 @@ struct PressureWork {
   GridDev g;
   bool graphsFor64, graphsFor32;
   const void* keyA[8];  // pointers the captured graphs were built for
-  const void* keyB[10];
+  const void* keyB[8];
   cudaStream_t capStream;
   cudaEvent_t ev[4];
   unsigned long long kFirst, kChunk, kFirst32, kChunk32;  // kernels per graph
@@ -627,8 +550,6 @@ struct PressureWork {
   // inner solves handed to a batcher shared with other scenes or systems
   InnerBatcher* batcher;
   cudaEvent_t batchReady, batchDone;
-  // two-level preconditioner of the one-pass inner solves (esf_coarse.cuh)
-  struct CoarseWork* co;
 };
 
 // ---- FP32 vectors of the inner solves in compressible memory. They are
@@ -763,7 +684,7 @@ static int fused_cz(const GridDev& g) {
     int dev = 0, sms = 152, per = 4;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pcr_iteration_fused<false>, NT, FU_SMEM) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pcr_iteration_fused, NT, FU_SMEM) !=
             cudaSuccess ||
         per < 1)
       per = 4;
@@ -866,7 +787,6 @@ void pressure_work_free(PressureWork* w) {
   if (w->batcher) pressure_work_set_batcher(w, nullptr);
   if (w->batchReady) cudaEventDestroy(w->batchReady);
   if (w->batchDone) cudaEventDestroy(w->batchDone);
-  coarse_free(w->co);
   delete w;
 }
 
@@ -955,7 +875,7 @@ static esf_status prepare_tma(PressureWork* w, const GridDev& g, const double* m
   if (!path || !fits || (pick && strcmp(pick, "tma") == 0)) return ESF_OK;
   if (!w->fusedOk) {
     static const cudaError_t attr = cudaFuncSetAttribute(
-        pcr_iteration_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, FU_SMEM);
+        pcr_iteration_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, FU_SMEM);
     if (attr != cudaSuccess) {
       set_error("pcr_iteration_fused: %d bytes of shared memory refused: %s", FU_SMEM,
                 cudaGetErrorString(attr));
@@ -989,19 +909,9 @@ struct FusedKernels {
   FusedPtrs p;
   double* partial;
   PcrState* st;
-  const CoarseWork* co = nullptr;  // two-level preconditioner, or none
   void iteration(cudaStream_t cs) const {
     const int cz = fused_cz(g);
-    const dim3 gr = tma_grid(g, cz);
-    if (!co) {
-      ESF_COUNTED pcr_iteration_fused<false><<<gr, NT, FU_SMEM, cs>>>(g, *tm, p, partial, st, cz, CoarseArgs{});
-      return;
-    }
-    // the pass, Z^T s' folded, c' = F Z^T s' and alpha
-    ESF_COUNTED pcr_iteration_fused<true><<<gr, NT, FU_SMEM, cs>>>(g, *tm, p, partial, st, cz, co->a);
-    ESF_COUNTED k_coarse_fold<<<(co->K + 255) / 256, 256, 0, cs>>>(co->a, g.cX, gr.x, gr.y, gr.z, cz, co->h, st);
-    ESF_COUNTED k_coarse_matvec<<<std::min((co->K + 7) / 8, 608), 256, 0, cs>>>(co->F, co->h, co->c, co->K,
-                                                                             co->partial, st);
+    ESF_COUNTED pcr_iteration_fused<<<tma_grid(g, cz), NT, FU_SMEM, cs>>>(g, *tm, p, partial, st, cz);
   }
   // graph capture interface of PressureKernels (inner solves only)
   void setup_warm(cudaStream_t) const {}
@@ -1010,10 +920,8 @@ struct FusedKernels {
     for (int k = 0; k < n; k++) iteration(cs);
   }
 };
-static FusedKernels fused_kernels(PressureWork* w, const GridDev& g, PcrState* st,
-                                  const CoarseWork* co = nullptr) {
+static FusedKernels fused_kernels(PressureWork* w, const GridDev& g, PcrState* st) {
   FusedKernels k;
-  k.co = co;
   k.g = g;
   k.tm = &w->fmaps;
   k.p.r[0] = w->r32; k.p.r[1] = w->r32b;
@@ -1164,108 +1072,6 @@ static esf_status init_state(PcrState* d, double eps, int maxIt, cudaStream_t st
 static esf_status batched_inner_solve(PressureWork* w, const GridDev& g, cudaStream_t st, PcrState* out);
 static bool batching_pays(PressureWork* w);
 
-// ESF_COARSE=1 turns the two-level preconditioner of the one-pass inner
-// solves on.
-static bool coarse_enabled() {
-  const char* e = getenv("ESF_COARSE");
-  return e && e[0] == '1';
-}
-
-// Coarse operator E = Z^T A Z of this solve's A (minv32 set), regularised and
-// inverted into F; *ok false (Jacobi alone) when cuSOLVER is missing, the
-// pass's z-chunks span more than three z-blocks or the factorisation fails.
-static esf_status coarse_prepare(PressureWork* w, const GridDev& g, int cz, cudaStream_t st, bool* ok) {
-  *ok = false;
-  const CusolverApi& api = cusolver_api();
-  if (!api.ok) return ESF_OK;
-  const int bs = coarse_block(g);
-  if (cz > 2 * bs) return ESF_OK;
-  const int nbx = (g.cX + bs - 1) / bs, nby = (g.cY + bs - 1) / bs, nbz = (g.cZ + bs - 1) / bs;
-  const int K = 8 * nbx * nby * nbz;
-  const dim3 gr = tma_grid(g, cz);
-  const long long nblk = (long long)gr.x * gr.y * gr.z;
-  CoarseWork*& c = w->co;
-  if (!c || c->K != K || c->R != g.R || c->hpartBlocks < nblk) {
-    coarse_free(c);
-    c = new CoarseWork();
-    c->K = K;
-    c->R = g.R;
-    c->hpartBlocks = nblk;
-    const size_t KK = (size_t)K * K;
-    ESF_CUDA(cudaMalloc(&c->F, KK * 4));
-    ESF_CUDA(cudaMalloc(&c->Eint, KK * 8));
-    ESF_CUDA(cudaMalloc(&c->E64, KK * 8));
-    for (float** v : {&c->c, &c->h, &c->c0, &c->h0}) ESF_CUDA(cudaMalloc(v, (size_t)K * 4));
-    ESF_CUDA(cudaMalloc(&c->hpart, (size_t)nblk * CO_PART * 4));
-    ESF_CUDA(cudaMalloc(&c->v, (size_t)g.R * 4));
-    ESF_CUDA(cudaMalloc(&c->y, (size_t)g.R * 4));
-    ESF_CUDA(cudaMalloc(&c->partial, 1024 * 8));
-    ESF_CUDA(cudaMalloc(&c->dmax, 8));
-    ESF_CUDA(cudaMalloc(&c->fmax, 4));
-    ESF_CUDA(cudaMalloc(&c->info, 4));
-    if (api.create(&c->solver) != 0) {
-      c->solver = nullptr;
-      return ESF_OK;
-    }
-    int l1 = 0, l2 = 0;
-    api.setStream(c->solver, st);
-    if (api.potrfSize(c->solver, CUBLAS_LOWER, K, c->E64, K, &l1) != 0 ||
-        api.potriSize(c->solver, CUBLAS_LOWER, K, c->E64, K, &l2) != 0)
-      return ESF_OK;
-    c->lwork = std::max(l1, l2);
-    ESF_CUDA(cudaMalloc(&c->work, (size_t)std::max(c->lwork, 1) * 8));
-    static const cudaError_t attr = cudaFuncSetAttribute(
-        pcr_iteration_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, FU_SMEM);
-    if (attr != cudaSuccess) return ESF_OK;
-  }
-  if (!c->solver || !c->work) return ESF_OK;
-  c->a.bs = bs;
-  c->a.nbx = nbx;
-  c->a.nby = nby;
-  c->a.nbz = nbz;
-  c->a.ct = c->c;
-  c->a.hpart = c->hpart;
-  // fixed-point scale: |y| <= 27 x 24 max m^-1 for |v| <= 1 (27 neighbours,
-  // 8 shared nodes x 3 components each), and an entry sums bs^3 of them
-  ESF_CUDA(cudaMemsetAsync(c->fmax, 0, 4, st));
-  ESF_COUNTED k_max_float<<<vec_blocks(g.T), 256, 0, st>>>(w->minv32, g.T, c->fmax);
-  unsigned mbits = 0;
-  ESF_CUDA(cudaMemcpyAsync(&mbits, c->fmax, 4, cudaMemcpyDeviceToHost, st));
-  ESF_CUDA(cudaStreamSynchronize(st));
-  float maxm;
-  memcpy(&maxm, &mbits, 4);
-  if (!(maxm > 0.0f)) return ESF_OK;
-  const double bound = (double)bs * bs * bs * 648.0 * maxm;
-  const double scale = ldexp(1.0, 61 - (int)ceil(log2(bound)));
-  ESF_CUDA(cudaMemsetAsync(c->Eint, 0, (size_t)K * K * 8, st));
-  for (int chi = 0; chi < 8; chi++)
-    for (int p = 0; p < 8; p++) {
-      ESF_COUNTED k_coarse_colour<<<vec_blocks(g.R), 256, 0, st>>>(g, c->a, chi, p, c->v);
-      esf_status e = pressure_apply<float>(g, w->minv32, c->v, c->y, st);
-      if (e) return e;
-      ESF_COUNTED k_coarse_gather<<<vec_blocks(g.R), 256, 0, st>>>(g, c->a, chi, p, c->y, c->Eint, scale);
-    }
-  ESF_CUDA(cudaMemsetAsync(c->dmax, 0, 8, st));
-  ESF_COUNTED k_coarse_finish_E<<<vec_blocks((long long)K * K), 256, 0, st>>>(c->Eint, K, 1.0 / scale, c->E64,
-                                                                             c->dmax);
-  ESF_COUNTED k_coarse_regularise<<<(K + 255) / 256, 256, 0, st>>>(c->E64, K, c->dmax, 1e-4);
-  ESF_LAUNCH_CHECK();
-  api.setStream(c->solver, st);
-  int info = 0;
-  if (api.potrf(c->solver, CUBLAS_LOWER, K, c->E64, K, c->work, c->lwork, c->info) != 0) return ESF_OK;
-  ESF_CUDA(cudaMemcpyAsync(&info, c->info, 4, cudaMemcpyDeviceToHost, st));
-  ESF_CUDA(cudaStreamSynchronize(st));
-  if (info != 0) return ESF_OK;
-  if (api.potri(c->solver, CUBLAS_LOWER, K, c->E64, K, c->work, c->lwork, c->info) != 0) return ESF_OK;
-  ESF_CUDA(cudaMemcpyAsync(&info, c->info, 4, cudaMemcpyDeviceToHost, st));
-  ESF_CUDA(cudaStreamSynchronize(st));
-  if (info != 0) return ESF_OK;
-  ESF_COUNTED k_coarse_F<<<vec_blocks((long long)K * K), 256, 0, st>>>(c->E64, K, c->F);
-  ESF_LAUNCH_CHECK();
-  *ok = true;
-  return ESF_OK;
-}
-
 esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv64,
                           const double* diag64, const double* b, double* x, double eps, int maxIt,
                           int precision, double innerEps, int maxRefine, int* iters,
@@ -1330,18 +1136,10 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
                              w->s32, w->partial, w->st32};
   k32.tma = tma;
   const bool fused = path == P32_FUSED;
-  // two-level preconditioner (one-pass path, scenes that run their own inner solves)
-  bool useCo = false;
-  if (fused && coarse_enabled() && !batching_pays(w)) {
-    esf_status e = coarse_prepare(w, g, fused_cz(g), st, &useCo);
-    if (e) return e;
-  }
-  const CoarseWork* co = useCo ? w->co : nullptr;
-  const FusedKernels kf = fused_kernels(w, g, w->st32, co);
-  const void* key[10] = {w->minv32, w->invd32, w->b32, w->x32, tma, &w->fmaps,
-                         reinterpret_cast<const void*>(static_cast<uintptr_t>(path + 1)),
-                         reinterpret_cast<const void*>(static_cast<uintptr_t>(fused_cz(g))),
-                         co, co ? co->F : nullptr};
+  const FusedKernels kf = fused_kernels(w, g, w->st32);
+  const void* key[8] = {w->minv32, w->invd32, w->b32, w->x32, tma, &w->fmaps,
+                        reinterpret_cast<const void*>(static_cast<uintptr_t>(path + 1)),
+                        reinterpret_cast<const void*>(static_cast<uintptr_t>(fused_cz(g)))};
   if (!w->graphsFor32 || memcmp(key, w->keyB, sizeof key) != 0) {
     esf_status e = fused ? capture(w->capStream, kf, false, false, &w->gChunk32, &w->kChunk32)
                          : capture(w->capStream, k32, false, false, &w->gChunk32, &w->kChunk32);
@@ -1352,16 +1150,6 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
   // start of an inner solve: zero directions (and, one-pass, t of the first
   // buffer set, which the set-up pass reads), then the set-up pass s = A r
   auto inner_setup = [&]() -> esf_status {
-    if (co) {
-      // r = M^-1 res: add Z F Z^T res (res in FP64 from the residual kernel)
-      ESF_COUNTED k_coarse_reduce<<<dim3(co->a.nbx, co->a.nby, co->a.nbz), 256, 0, st>>>(g, co->a, w->r, co->h0);
-      ESF_COUNTED k_coarse_matvec<<<std::min((co->K + 7) / 8, 608), 256, 0, st>>>(co->F, co->h0, co->c0, co->K,
-                                                                               nullptr, nullptr);
-      CoarseArgs a0 = co->a;
-      a0.ct = co->c0;
-      ESF_COUNTED k_coarse_add<<<vec_blocks(g.R), 256, 0, st>>>(g, a0, w->r32);
-      ESF_CUDA(cudaMemsetAsync(co->c, 0, (size_t)co->K * 4, st));
-    }
     ESF_CUDA(cudaMemsetAsync(w->d32, 0, g.R * 4, st));
     ESF_CUDA(cudaMemsetAsync(w->Ap32, 0, g.R * 4, st));
     if (fused) {
@@ -1475,7 +1263,6 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
       hi.setup = 1;
       hi.eps = trigger(resid2);
       memset(hi.ticket, 0, sizeof hi.ticket);
-      hi.coTicket = 0;
       ESF_CUDA(cudaMemcpyAsync(w->st32, &hi, sizeof hi, cudaMemcpyHostToDevice, st));
       ESF_CUDA(cudaStreamSynchronize(st));
       e = inner_setup();
