@@ -756,13 +756,18 @@ __global__ void k_grid_to_particle(GridDev g, SolidDev s, long long np, double* 
     int bb[3];
     double wt[12];
     stencil_weights(g, pos, bb, wt);
-    for (int r = k; r < k + 4; r++)
-      for (int t = j; t < j + 4; t++)
-        for (int sx = i; sx < i + 4; sx++) {
+    // (offsets as compile-time indices keep the weights in registers)
+#pragma unroll
+    for (int dr = 0; dr < 4; dr++)
+#pragma unroll
+      for (int dt = 0; dt < 4; dt++)
+#pragma unroll
+        for (int ds = 0; ds < 4; ds++) {
+          const int r = k + dr, t = j + dt, sx = i + ds;
           if (sx < 0 || t < 0 || r < 0 || sx > g.X - 1 || t > g.Y - 1 || r > g.Z - 1) continue;
           long long n = nidx(g, sx, t, r);
           if (s.mass[n] == 0) continue;
-          double w = wt[sx - i] * wt[4 + t - j] * wt[8 + r - k];
+          double w = wt[ds] * wt[4 + dt] * wt[8 + dr];
           for (int q = 0; q < 3; q++) {
             double v = s.vel[3 * n + q];
             pic[q] += v * w;
@@ -807,8 +812,11 @@ __global__ void k_grid_to_particle(GridDev g, SolidDev s, long long np, double* 
         break;
       }
     }
-    const double N[6][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {-1, 0, 0}, {0, -1, 0}, {0, 0, -1}};
     for (int b = 0; b < 6; b++) {
+      // wall normal b: +x, +y, +z, -x, -y, -z (the values, not a table, so
+      // nothing is indexed at run time)
+      double N[3];
+      for (int q = 0; q < 3; q++) N[q] = (q == b % 3) ? (b < 3 ? 1.0 : -1.0) : 0.0;
       double dist = fabs(pos[b % 3] - cp.bnd[b]);
       if (dist < cp.wallThickness) {
         double overlap = cp.wallThickness - dist;
@@ -821,17 +829,17 @@ __global__ void k_grid_to_particle(GridDev g, SolidDev s, long long np, double* 
         else if (b == 5) zi = g.Z - 1;
         const double* vo = s.vel + 3 * nidx(g, xi, yi, zi);
         double vrel[3] = {pv[0] - vo[0], pv[1] - vo[1], pv[2] - vo[2]};
-        double vn = (vrel[0] * N[b][0] + vrel[1] * N[b][1]) + vrel[2] * N[b][2];
+        double vn = (vrel[0] * N[0] + vrel[1] * N[1]) + vrel[2] * N[2];
         if (vn <= 0) {
           double A = s.dt * cp.spring * overlap, B = P[9] * (0.1 * overlap / s.dt - vn);
           double impulse = -((B < A) ? B : A);
           double dvn = -impulse / P[9];
           double vt[3];
-          for (int q = 0; q < 3; q++) vt[q] = vrel[q] - vn * N[b][q];
+          for (int q = 0; q < 3; q++) vt[q] = vrel[q] - vn * N[q];
           double vtn = sqrt(vt[0] * vt[0] + (vt[1] * vt[1] + vt[2] * vt[2]));
           double sc = 0.1 - cp.friction * dvn / vtn;
           sc = (sc < 0.0) ? 0.0 : sc;
-          for (int q = 0; q < 3; q++) pv[q] = ((vn + dvn) * N[b][q] + sc * vt[q]) + vo[q];
+          for (int q = 0; q < 3; q++) pv[q] = ((vn + dvn) * N[q] + sc * vt[q]) + vo[q];
           break;
         }
       }
