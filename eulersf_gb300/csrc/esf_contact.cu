@@ -383,7 +383,13 @@ extern "C" esf_status esf_svol_read(const char* path, int lo[3], int n[3], doubl
     return ESF_ERR_INVALID_ARG;
   }
   esf::SvolLattice L;
-  esf_status e = esf::svol_read(path, &L);
+  esf_status e;
+  try {
+    e = esf::svol_read(path, &L);
+  } catch (...) {  // host allocation of a very large lattice
+    esf::set_error("esf_svol_read: out of host memory for %s", path);
+    return ESF_ERR_OOM;
+  }
   if (e) return e;
   for (int k = 0; k < 3; k++) {
     lo[k] = L.lo[k];

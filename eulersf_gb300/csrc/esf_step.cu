@@ -534,11 +534,17 @@ extern "C" esf_status esf_solid_load_rest_sdf(esf_scene* sc, int solid, const ch
   cudaSetDevice(sc->device);
   Solid* d = sc->s[solid];
   SvolLattice L;
-  TRY(svol_read(path, &L));
   std::vector<int> off, ids;
-  if (!svol_hash_triangles(L, d->restPose.data(), d->ntri, d->tris.data(), &off, &ids)) {
-    set_error("esf_solid_load_rest_sdf: %s: the mesh's triangle lists on this lattice exceed 2^31 entries", path);
-    return ESF_ERR_UNSUPPORTED;
+  try {  // host allocations of the lattice and the triangle lists
+    TRY(svol_read(path, &L));
+    if (!svol_hash_triangles(L, d->restPose.data(), d->ntri, d->tris.data(), &off, &ids)) {
+      set_error("esf_solid_load_rest_sdf: %s: the mesh's triangle lists on this lattice exceed 2^31 entries",
+                path);
+      return ESF_ERR_UNSUPPORTED;
+    }
+  } catch (...) {
+    set_error("esf_solid_load_rest_sdf: out of host memory for %s", path);
+    return ESF_ERR_OOM;
   }
   TRY(d->sdfVal.ensure(L.val.size() * 4));
   TRY(d->sdfCode.ensure(L.code.size()));
