@@ -12,6 +12,11 @@ device time per launch as a fraction of the measured HBM copy bandwidth
 (the roofline of the step: 64-88% of it is the pressure solve).
 
     python -m eulersf_gb300.two_sphere_bench [--size 384] [--steps 10] [--seed 7]
+    python -m eulersf_gb300.two_sphere_bench --collide      # the same balls, touching and approaching
+
+--collide places the two balls side by side at (0.38, 0.7, 0.5) and
+(0.62, 0.7, 0.5), 0.24 apart centre to centre, moving towards each other at
+0.5 m/s, so that solid-solid contact acts from the first step.
 """
 from __future__ import annotations
 
@@ -27,9 +32,13 @@ from .scene import SceneDesc, SolidDesc
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def scene(size: int = 384, seed: int = 7) -> SceneDesc:
-    balls = [SolidDesc(center=c, radius=0.12, density=1100.0, E=3e5, nu=0.45)
-             for c in ((0.35, 0.7, 0.5), (0.65, 0.8, 0.5))]
+def scene(size: int = 384, seed: int = 7, collide: bool = False) -> SceneDesc:
+    if collide:
+        balls = [SolidDesc(center=c, radius=0.12, density=1100.0, E=3e5, nu=0.45, velocity=v)
+                 for c, v in (((0.38, 0.7, 0.5), (0.5, 0.0, 0.0)), ((0.62, 0.7, 0.5), (-0.5, 0.0, 0.0)))]
+    else:
+        balls = [SolidDesc(center=c, radius=0.12, density=1100.0, E=3e5, nu=0.45)
+                 for c in ((0.35, 0.7, 0.5), (0.65, 0.8, 0.5))]
     return SceneDesc(N=size, noise_seed=seed, fluid_height=0.3, solids=balls)
 
 
@@ -41,8 +50,8 @@ def hbm_peak():
     return 6800.0, "fallback"
 
 
-def run(size=384, steps=10, seed=7, out=print):
-    desc = scene(size, seed)
+def run(size=384, steps=10, seed=7, out=print, collide=False):
+    desc = scene(size, seed, collide)
     t0 = time.perf_counter()
     I = make_scene(desc, precision=abi.ESF_MIXED)
     setup_s = time.perf_counter() - t0
@@ -67,7 +76,8 @@ def run(size=384, steps=10, seed=7, out=print):
     peak, kind = hbm_peak()
     words = 17  # per row of a whole iteration but its residual check, 4-byte words
     achieved = words * 4 * R / (upd.value * 1e-3) / 1e9 if st == 0 and upd.value > 0 else None
-    summary = {"summary": True, "scene": "two spheres, radius 0.12, fluid height 0.3", "size": size,
+    summary = {"summary": True, "scene": "two spheres, radius 0.12, fluid height 0.3"
+               + (", touching and approaching" if collide else ""), "size": size,
                "steps": steps, "seed": seed, "precision": "mixed", "setup_s": setup_s,
                "steps_per_s": steps / t, "cells_per_s": R * steps / t,
                "pressure_iters_per_s": piters / t, "pressure_iters_per_step": piters / steps,
@@ -89,8 +99,9 @@ def main(argv=None):
     ap.add_argument("--size", type=int, default=384)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--collide", action="store_true", help="balls touching and approaching")
     a = ap.parse_args(argv)
-    run(a.size, a.steps, a.seed)
+    run(a.size, a.steps, a.seed, collide=a.collide)
     return 0
 
 
