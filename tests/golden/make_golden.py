@@ -209,11 +209,13 @@ CONTACT_SOLID_FIELDS = ["valid", "boxes", "mass", "phi", "u", "velocity", "meshV
 
 def contact_query_points(radius, count=4096, seed=5):
     """Rest points around a sphere's surface: seeded directions at distances
-    within +-0.2 radius of it, the contact band and beyond."""
+    within +-0.2 radius of it (the contact band and beyond), then 64 deep
+    inside (below the band) and 64 far outside (beyond the volume's box)."""
     rng = np.random.default_rng(seed)
-    d = rng.standard_normal((count, 3))
+    d = rng.standard_normal((count + 128, 3))
     d /= np.linalg.norm(d, axis=1)[:, None]
-    r = radius * (1 + rng.uniform(-0.2, 0.2, count))
+    r = np.concatenate([radius * (1 + rng.uniform(-0.2, 0.2, count)),
+                        radius * rng.uniform(0.0, 0.5, 64), radius * rng.uniform(2.0, 3.0, 64)])
     return d * r[:, None]
 
 
