@@ -253,6 +253,9 @@ def build_from_scene(lib, prefix, desc: SceneDesc, precision=abi.ESF_FP64, noise
     solids, fluid density, init(), smoke carpet, then the seeded fluid noise
     added at nodes without solid mass."""
     res = desc.res
+    if len(desc.solids) > 1 and rest_sdf and not hasattr(lib, prefix + "solid_load_rest_sdf"):
+        raise NotImplementedError(f"{prefix}: scenes with several solids need solid-solid contact, "
+                                  "which this library does not provide")
     I = CoupledIntegrator3D(lib, prefix, res, res, res, desc.dh, (0.0, 0.0, 0.0),
                             params_from_desc(desc, precision), stream=stream)
     for i, s in enumerate(desc.solids):
