@@ -21,6 +21,9 @@ the ratio of the two paths' steps/s on those steps, each path's pressure
 iterations, and the L-inf differences of velocity and pressure between them
 after each compared step; and it re-checks the final mixed pressure solve's
 relative residual with the CPU oracle's operator (outside the timed region).
+It then runs the same steps once more with precision ESF_MIXED_X64 (the
+pressure solve's iterate and direction in FP64, one Krylov run per solve:
+`mixed_x64`, --no-x64 to skip), outside the timed region of `value`.
 """
 from __future__ import annotations
 
@@ -363,6 +366,7 @@ def ours(args):
                         "the same duration"}
     # ---- the plain FP64 GPU path on the same scene, steps 1..F
     fp64 = None
+    fsnaps = {}
     if F > 0:
         I.close()  # the mixed scene's memory is not needed any more
         I = None
@@ -372,6 +376,7 @@ def ours(args):
             r = D.stepImplicit()
             if k == 0:
                 continue
+            fsnaps[k] = (D.get("velocity"), D.get("lambda1"), r["device_ms"])
             vm, lm = snaps[k]
             rows.append({"step": k, "fp64_ms": r["device_ms"], "mixed_ms": warm_reports[k]["device_ms"],
                          "fp64_pressure_iters": r["iterations"][1],
@@ -397,6 +402,48 @@ def ours(args):
                 "what": "both paths from the same initial state, steps 1..F (step 0 untimed on both: "
                         "first-step set-up); device time of each step (CUDA events in esf_step); "
                         "L-inf = max |mixed - fp64| / max |fp64| of the field after the step"}
+    # ---- the same workload with the pressure solve's iterate and direction
+    # in FP64 (ESF_MIXED_X64: one FP32 Krylov run per solve, no restarts),
+    # over the same warm-up and timed steps; device time from the step reports
+    x64 = None
+    if compare and not args.no_x64:
+        if I is not None:
+            I.close()
+            I = None
+        X = E.make_scene(desc, precision=abi.ESF_MIXED_X64, stream=stream.cuda_stream)
+        xr, lv, lp, t64s, txs = [], [], [], 0.0, 0.0
+        for k in range(args.warmup + args.steps):
+            r = X.stepImplicit()
+            xr.append(r)
+            if k in fsnaps:
+                vf, lf, ms64 = fsnaps[k]
+                lv.append(_linf(X.get("velocity"), vf))
+                lp.append(_linf(X.get("lambda1"), lf))
+                t64s += ms64 * 1e-3
+                txs += r["device_ms"] * 1e-3
+        timed = xr[args.warmup:]
+        tx = sum(r["device_ms"] for r in timed) * 1e-3
+        xu, xa = C.c_double(), C.c_double()
+        stx = lib.esf_time_pressure_kernels(X._h, 20, C.byref(xu), C.byref(xa))
+        X.close()
+        moved_x = 16 * 4 * R
+        x_gbs = moved_x / (xu.value * 1e-3) / 1e9 if stx == 0 and xu.value > 0 else None
+        x64 = {"steps_per_s": args.steps / tx, "over_mixed": (args.steps / tx) / value,
+               "over_fp64_same_steps": (t64s / txs) if txs > 0 else None,
+               "pressure_iters_each_step": [r["iterations"][1] for r in timed],
+               "pressure_iters_per_step": sum(r["iterations"][1] for r in timed) / args.steps,
+               "fp64_checks_each_step": [r["refinements"][1] for r in timed],
+               "rel_residual_max": max(max(r["rel_residual"]) for r in xr),
+               "all_converged": all(all(r["converged"]) for r in xr),
+               "l_inf_velocity_each_step": lv, "l_inf_pressure_each_step": lp,
+               "kernel": "pcr_iteration_fused_x64", "kernel_ms": xu.value if stx == 0 else None,
+               "moved_words_per_row": 16, "frac_of_moved": (x_gbs / peak) if x_gbs else None,
+               "what": "precision ESF_MIXED_X64 on the same scene and steps: FP32 operator, residual "
+                       "vectors and stencil; the pressure solve's iterate and search direction in "
+                       "FP64; one Krylov run per solve to the 1e-8 FP64 residual, checked in FP64 "
+                       "(no inner tolerance, no restarts). Not the configured refinement (FP32 inner "
+                       "solves to 1e-4), which `value` measures. L-inf against the FP64 path after "
+                       "steps 1..F; over_fp64_same_steps on those steps"}
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -434,6 +481,7 @@ def ours(args):
             "fp64_gpu_steps_per_s": fp64["fp64_gpu_steps_per_s"] if fp64 else None,
             "l_inf_velocity": max(fp64["l_inf_velocity_each_step"]) if fp64 else None,
             "l_inf_pressure": max(fp64["l_inf_pressure_each_step"]) if fp64 else None,
+            "mixed_x64": x64,
             "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
         }
         print(json.dumps(line), flush=True)
@@ -457,6 +505,8 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=3,
                     help="FP64 GPU comparison over steps 1..F (bounded by --warmup - 1)")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-x64", action="store_true",
+                    help="skip the ESF_MIXED_X64 run of the same steps (mixed_x64)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)

@@ -12,7 +12,7 @@ STATUS = {
     4: "ESF_ERR_OOM", 5: "ESF_ERR_IO", 6: "ESF_ERR_NUMERIC", 7: "ESF_ERR_NO_DEVICE",
     8: "ESF_ERR_UNSUPPORTED",
 }
-ESF_FP64, ESF_MIXED = 0, 1
+ESF_FP64, ESF_MIXED, ESF_MIXED_X64 = 0, 1, 2
 
 
 class EsfError(RuntimeError):

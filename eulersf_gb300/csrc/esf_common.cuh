@@ -112,6 +112,7 @@ struct PcrState {
   int cap;           // inner mode: iterations between replacements (0 = none)
   int pp;            // one-pass FP32 iteration: which buffer set holds r, t, q
   unsigned int ticket[4];
+  double deltaPrev;  // one-pass double-float run: r.s of the iterate before the current one
 };
 
 // Solid system layout ("sliced"): the 27 neighbour 3x3 blocks of solid node a,

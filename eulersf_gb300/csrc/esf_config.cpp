@@ -106,7 +106,10 @@ extern "C" esf_status esf_parse_config(const char* path, esf_grid* grid, esf_par
   p->friction = c.f("friction", 0.5);
   p->flip_cutoff = c.i("flip cutoff", 3);
   p->flow_rate = c.f("flow rate", 0);
-  p->precision = c.s("precision", "fp64") == "mixed" ? ESF_MIXED : ESF_FP64;
+  {
+    const std::string prec = c.s("precision", "fp64");
+    p->precision = prec == "mixed" ? ESF_MIXED : prec == "mixed x64" ? ESF_MIXED_X64 : ESF_FP64;
+  }
   p->inner_eps = c.f("inner solver eps", 1e-4);
   int n = c.i("number of solids", 1);
   if (num_solids) *num_solids = n;

@@ -65,7 +65,25 @@ constexpr int FU_SUMS = 4;                    // delta, mu, nu, omega
 // Scalars after a fused pass: totals of (r', s'), (s', t'), (s', q), (Ap, q).
 __device__ __forceinline__ void finish_fused(PcrState* st, double dl, double mu, double nu,
                                              double om) {
-  if (st->setup) {
+  if (st->rebase) {
+    // (double-float run) r was replaced by the FP64 residual (b - A x)/diag
+    // and this pass kept q, d and e: the scalars of the pass that produced
+    // the old r, recomputed for the new one
+    const double beta = (st->deltaPrev > 0.0) ? dl / st->deltaPrev : 0.0;
+    double den = mu + 2.0 * beta * nu + beta * beta * om;
+    if (!(den > 0.0)) den = mu;
+    st->beta = beta;
+    st->alpha = (den > 0.0) ? dl / den : 0.0;
+    st->delta = dl;
+    st->delta0 = dl;
+    st->rebase = 0;
+    st->iter++;
+    st->iter0 = st->iter;
+    if (!(dl > 0.0)) {
+      st->converged = 1;
+      st->done = 1;
+    }
+  } else if (st->setup) {
     st->delta = dl;
     st->delta0 = dl;
     st->beta = 0.0;
@@ -82,6 +100,7 @@ __device__ __forceinline__ void finish_fused(PcrState* st, double dl, double mu,
     if (!(den > 0.0)) den = mu;  // rounding guard; (Ap, Ap/diag) is positive
     st->beta = beta;
     st->alpha = (den > 0.0) ? dl / den : 0.0;
+    st->deltaPrev = st->delta;
     st->delta = dl;
     st->iter++;
     if (dl <= st->eps * st->eps * st->delta0 || (st->cap > 0 && st->iter - st->iter0 >= st->cap)) {
@@ -96,13 +115,57 @@ __device__ __forceinline__ void finish_fused(PcrState* st, double dl, double mu,
   }
 }
 
+// Double-float ("df") arithmetic on FP32 pairs (hi, lo), value hi + lo with
+// |lo| <= ulp(hi)/2: a 48-bit significand from FP32 instructions only, by
+// the error-free transformations of Knuth (TwoSum) and Dekker (the product
+// error of an FMA). Explicit _rn intrinsics keep the compiler from
+// contracting or reordering them.
+__device__ __forceinline__ float2 df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float v = __fsub_rn(s, a);
+  return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v)));
+}
+// y + a x (x df; y, a FP32)
+__device__ __forceinline__ float2 df_axpy(float a, float2 x, float y) {
+  const float ph = __fmul_rn(a, x.x);
+  const float pl = __fmaf_rn(a, x.x, -ph);
+  const float2 s = df_two_sum(y, ph);
+  const float t = __fadd_rn(__fmaf_rn(a, x.y, pl), s.y);
+  return df_two_sum(s.x, t);
+}
+// e + a d (e, d df; a FP32)
+__device__ __forceinline__ float2 df_add_scaled(float2 e, float a, float2 d) {
+  const float ph = __fmul_rn(a, d.x);
+  const float pl = __fmaf_rn(a, d.x, -ph);
+  const float2 s = df_two_sum(e.x, ph);
+  const float t = __fadd_rn(__fadd_rn(__fmaf_rn(a, d.y, pl), e.y), s.y);
+  return df_two_sum(s.x, t);
+}
+
 // One block's share of a pass: the 64 x 8-cell column (bx, by) over the cell
 // layers bz*cz .. bz*cz+cz-1 of the scene (g, tm, p, partial, st), whose
 // pass has nb blocks; bid is this block's place among them (the order in
 // which the last block folds the partial sums).
+//
+// X64: the correction e (since the last FP64 check, which folds it into
+// the FP64 solution) and the direction d are double-float pairs (edf, ddf:
+// (hi, lo) per cell, interleaved) and move by plain 16-byte loads and
+// stores of each thread's two cells, prefetched one layer ahead, instead of
+// the TMA own-cell boxes; r, t, q and the stencil stay FP32. An FP32 iterate
+// cannot hold the corrections of the operator's slowest modes: its rounding
+// (relative 2^-24 per cell) reaches the residual amplified by up to kappa
+// (about 5e7 at 256^3 cells), and an FP32 direction lets x and the recursive
+// residual drift apart by as much. With both at a 48-bit significand one
+// FP32 Krylov run reaches the FP64 tolerance in about the FP64 solver's
+// iteration count, without the restarts of iterative refinement. (FP64
+// arithmetic for the two updates kept the FP64 pipe 67% busy at half the
+// DRAM bandwidth; the df updates are about 33 FP32 instructions a cell.)
+// Both updates use the FP32 alpha and beta that update r and q.
+template <bool X64>
 __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm, const FusedPtrs& p,
-                                           double* partial, PcrState* st, int cz, int bx, int by,
-                                           int bz, int nb, int bid, unsigned char* smem) {
+                                           float* edf, float* ddf, double* partial, PcrState* st,
+                                           int cz, int bx, int by, int bz, int nb, int bid,
+                                           unsigned char* smem) {
   unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem + FU_OFF_BAR);
   float* sP = reinterpret_cast<float*>(smem + FU_OFF_P);
   float* sQ = reinterpret_cast<float*>(smem + FU_OFF_SQ);
@@ -117,7 +180,9 @@ __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm
     return;
   }
   const int pin = st->pp & 1, pout = pin ^ 1;
-  const float alpha = (float)st->alpha, beta = (float)st->beta;
+  // rebase pass (X64 only): alpha 0, q and d carried over unchanged
+  const bool rb = X64 && st->rebase;
+  const float alpha = rb ? 0.0f : (float)st->alpha, beta = (float)st->beta;
   const int tid = threadIdx.x;
   const int x0 = bx * TXW, y0 = by * TY, z0 = bz * cz;
   const int z1 = min(z0 + cz, g.cZ);
@@ -133,14 +198,17 @@ __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm
     unsigned long long* b = &bar[i % TMA_STAGES];
     const bool own = kk >= z0 && kk < z1;
     const bool node = kk >= z0;
-    mbar_expect_tx(b, 3 * TMA_HALO_BYTES + (own ? 3 * TMA_OWN_BYTES : 0) + (node ? TMA_NODE_BYTES : 0));
+    mbar_expect_tx(b, 3 * TMA_HALO_BYTES + (own ? (X64 ? 1 : 3) * TMA_OWN_BYTES : 0) +
+                          (node ? TMA_NODE_BYTES : 0));
     tma_load_3d(s + FU_OFF_R, mR, x0 - 4, y0 - 1, kk, b);
     tma_load_3d(s + FU_OFF_T, mT, x0 - 4, y0 - 1, kk, b);
     tma_load_3d(s + FU_OFF_Q, mQ, x0 - 4, y0 - 1, kk, b);
     if (own) {
       tma_load_3d(s + FU_OFF_IV, &tm.iv, x0, y0, kk, b);
-      tma_load_3d(s + FU_OFF_X, &tm.x, x0, y0, kk, b);
-      tma_load_3d(s + FU_OFF_D, &tm.d, x0, y0, kk, b);
+      if (!X64) {
+        tma_load_3d(s + FU_OFF_X, &tm.x, x0, y0, kk, b);
+        tma_load_3d(s + FU_OFF_D, &tm.d, x0, y0, kk, b);
+      }
     }
     if (node) tma_load_3d(s + FU_OFF_M, &tm.m, x0, y0, kk, b);
   };
@@ -187,6 +255,12 @@ __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm
   float prev0 = 0, prev1 = 0, prevE = 0, vOwn0 = 0, vOwn1 = 0;
   float qCur0 = 0, qCur1 = 0, ivCur0 = 0, ivCur1 = 0;
   float mpx0 = 0, mpy0 = 0, mpz0 = 0, mpx1 = 0, mpy1 = 0, mpz1 = 0, mpxE = 0, mpyE = 0, mpzE = 0;
+  float4 eNext = make_float4(0.f, 0.f, 0.f, 0.f), dNext = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (X64 && cin && z0 < z1) {
+    const long long o = ccol + (long long)z0 * g.cslab;
+    eNext = *reinterpret_cast<const float4*>(edf + 2 * o);
+    dNext = *reinterpret_cast<const float4*>(ddf + 2 * o);
+  }
   bool ok = true;
   int landed = 0;
   int issued = TMA_STAGES < nsteps ? TMA_STAGES : nsteps;
@@ -207,7 +281,7 @@ __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm
       const float2 r2 = *reinterpret_cast<const float2*>(R + bM);
       const float2 t2 = *reinterpret_cast<const float2*>(Tt + bM);
       const float2 q2 = *reinterpret_cast<const float2*>(Qq + bM);
-      const float qn0 = __fmaf_rn(beta, q2.x, t2.x), qn1 = __fmaf_rn(beta, q2.y, t2.y);
+      const float qn0 = rb ? q2.x : __fmaf_rn(beta, q2.x, t2.x), qn1 = rb ? q2.y : __fmaf_rn(beta, q2.y, t2.y);
       const float v0 = __fmaf_rn(-alpha, qn0, r2.x), v1 = __fmaf_rn(-alpha, qn1, r2.y);
       *reinterpret_cast<float2*>(sP + pM) = make_float2(prev0 + v0, prev1 + v1);
       *reinterpret_cast<float2*>(sQ + pM) = make_float2(prev0 - v0, prev1 - v1);
@@ -217,13 +291,27 @@ __device__ __forceinline__ void fused_pass(const GridDev& g, const FusedMaps& tm
       prev1 = v1;
       if (kk >= z0 && kk < z1 && cin) {
         const float2 iv = *reinterpret_cast<const float2*>(s + FU_OFF_IV + 4 * oM);
-        const float2 xv = *reinterpret_cast<const float2*>(s + FU_OFF_X + 4 * oM);
-        const float2 dv = *reinterpret_cast<const float2*>(s + FU_OFF_D + 4 * oM);
-        const float dn0 = __fmaf_rn(beta, dv.x, r2.x), dn1 = __fmaf_rn(beta, dv.y, r2.y);
         const long long o = ccol + (long long)kk * g.cslab;
-        *reinterpret_cast<float2*>(p.d + o) = make_float2(dn0, dn1);
-        *reinterpret_cast<float2*>(p.x + o) =
-            make_float2(__fmaf_rn(alpha, dn0, xv.x), __fmaf_rn(alpha, dn1, xv.y));
+        if constexpr (X64) {
+          const float4 ev = eNext, dv = dNext;
+          if (kk + 1 < z1) {  // the next layer's e and d, in flight during this one
+            eNext = *reinterpret_cast<const float4*>(edf + 2 * (o + g.cslab));
+            dNext = *reinterpret_cast<const float4*>(ddf + 2 * (o + g.cslab));
+          }
+          const float2 dn0 = rb ? make_float2(dv.x, dv.y) : df_axpy(beta, make_float2(dv.x, dv.y), r2.x);
+          const float2 dn1 = rb ? make_float2(dv.z, dv.w) : df_axpy(beta, make_float2(dv.z, dv.w), r2.y);
+          const float2 en0 = df_add_scaled(make_float2(ev.x, ev.y), alpha, dn0);
+          const float2 en1 = df_add_scaled(make_float2(ev.z, ev.w), alpha, dn1);
+          *reinterpret_cast<float4*>(ddf + 2 * o) = make_float4(dn0.x, dn0.y, dn1.x, dn1.y);
+          *reinterpret_cast<float4*>(edf + 2 * o) = make_float4(en0.x, en0.y, en1.x, en1.y);
+        } else {
+          const float2 xv = *reinterpret_cast<const float2*>(s + FU_OFF_X + 4 * oM);
+          const float2 dv = *reinterpret_cast<const float2*>(s + FU_OFF_D + 4 * oM);
+          const float dn0 = __fmaf_rn(beta, dv.x, r2.x), dn1 = __fmaf_rn(beta, dv.y, r2.y);
+          *reinterpret_cast<float2*>(p.d + o) = make_float2(dn0, dn1);
+          *reinterpret_cast<float2*>(p.x + o) =
+              make_float2(__fmaf_rn(alpha, dn0, xv.x), __fmaf_rn(alpha, dn1, xv.y));
+        }
         *reinterpret_cast<float2*>(rOut + o) = make_float2(v0, v1);
         *reinterpret_cast<float2*>(qOut + o) = make_float2(qn0, qn1);
         // (Ap, q) = (q diag, q); an approximate quotient is plenty for a sum
@@ -360,9 +448,20 @@ __global__ void __launch_bounds__(NT, 4) pcr_iteration_fused(GridDev g, const __
                                                              FusedPtrs p, double* partial, PcrState* st,
                                                              int cz) {
   extern __shared__ __align__(128) unsigned char smem[];
-  fused_pass(g, tm, p, partial, st, cz, blockIdx.x, blockIdx.y, blockIdx.z,
-             gridDim.x * gridDim.y * gridDim.z,
-             blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z), smem);
+  fused_pass<false>(g, tm, p, nullptr, nullptr, partial, st, cz, blockIdx.x, blockIdx.y, blockIdx.z,
+                    gridDim.x * gridDim.y * gridDim.z,
+                    blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z), smem);
+}
+
+// The same pass with the correction and direction in double-float
+// (ESF_MIXED_X64).
+__global__ void __launch_bounds__(NT, 4) pcr_iteration_fused_x64(GridDev g, const __grid_constant__ FusedMaps tm,
+                                                                 FusedPtrs p, float* edf, float* ddf,
+                                                                 double* partial, PcrState* st, int cz) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  fused_pass<true>(g, tm, p, edf, ddf, partial, st, cz, blockIdx.x, blockIdx.y, blockIdx.z,
+                   gridDim.x * gridDim.y * gridDim.z,
+                   blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z), smem);
 }
 
 // ---- several scenes' inner solves in one launch (continuous batching).
@@ -405,7 +504,7 @@ __global__ void __launch_bounds__(NT, 4) pcr_iteration_fused_batch(const FusedTa
   const int nb = t.gx * t.gy * t.gz;
   if (local >= nb) return;
   const int bx = local % t.gx, by = (local / t.gx) % t.gy, bz = local / (t.gx * t.gy);
-  fused_pass(t.g, t.tm, t.p, t.partial, t.st, t.cz, bx, by, bz, nb, local, smem);
+  fused_pass<false>(t.g, t.tm, t.p, nullptr, nullptr, t.partial, t.st, t.cz, bx, by, bz, nb, local, smem);
 }
 
 // The states of a batch's tasks, in list order, for one copy to the host.

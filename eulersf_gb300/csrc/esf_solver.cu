@@ -546,6 +546,13 @@ struct PressureWork {
   float *r32b, *s32b, *Ap32b;
   FusedMaps fmaps;
   bool fusedOk;
+  // ESF_MIXED_X64: the double-float correction and search direction
+  // (allocated on first use) and the graph of its iteration chunk
+  float *edf, *ddf;
+  cudaGraphExec_t gChunkX;
+  unsigned long long kChunkX;
+  const void* keyX[8];
+  bool graphsForX;
   MappedSet mapped;  // FP32 vectors mapped by vec_alloc
   // inner solves handed to a batcher shared with other scenes or systems
   InnerBatcher* batcher;
@@ -775,8 +782,11 @@ void pressure_work_free(PressureWork* w) {
                    w->Ap32b, w->minv32p})
     vec_free(&w->mapped, v);
   cudaFree(w->minv32);
+  cudaFree(w->edf);
+  cudaFree(w->ddf);
   cudaFree(w->partial); cudaFree(w->st); cudaFree(w->st32); cudaFree(w->stT);
   if (w->hst) cudaFreeHost(w->hst);
+  if (w->gChunkX) cudaGraphExecDestroy(w->gChunkX);
   if (w->gFirst) cudaGraphExecDestroy(w->gFirst);
   if (w->gChunk) cudaGraphExecDestroy(w->gChunk);
   if (w->gFirst32) cudaGraphExecDestroy(w->gFirst32);
@@ -874,8 +884,13 @@ static esf_status prepare_tma(PressureWork* w, const GridDev& g, const double* m
   const bool fits = (long long)gr.x * gr.y * gr.z * FU_SUMS <= ESF_MAX_PARTIALS / 2;
   if (!path || !fits || (pick && strcmp(pick, "tma") == 0)) return ESF_OK;
   if (!w->fusedOk) {
-    static const cudaError_t attr = cudaFuncSetAttribute(
-        pcr_iteration_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, FU_SMEM);
+    static const cudaError_t attr = [] {
+      cudaError_t a = cudaFuncSetAttribute(pcr_iteration_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           FU_SMEM);
+      if (a != cudaSuccess) return a;
+      return cudaFuncSetAttribute(pcr_iteration_fused_x64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  FU_SMEM);
+    }();
     if (attr != cudaSuccess) {
       set_error("pcr_iteration_fused: %d bytes of shared memory refused: %s", FU_SMEM,
                 cudaGetErrorString(attr));
@@ -909,8 +924,15 @@ struct FusedKernels {
   FusedPtrs p;
   double* partial;
   PcrState* st;
+  float* edf = nullptr;  // set: ESF_MIXED_X64, the double-float correction
+  float* ddf = nullptr;  // and direction ((hi, lo) per cell)
   void iteration(cudaStream_t cs) const {
     const int cz = fused_cz(g);
+    if (edf) {
+      ESF_COUNTED pcr_iteration_fused_x64<<<tma_grid(g, cz), NT, FU_SMEM, cs>>>(g, *tm, p, edf, ddf, partial,
+                                                                                st, cz);
+      return;
+    }
     ESF_COUNTED pcr_iteration_fused<<<tma_grid(g, cz), NT, FU_SMEM, cs>>>(g, *tm, p, partial, st, cz);
   }
   // graph capture interface of PressureKernels (inner solves only)
@@ -1071,6 +1093,17 @@ static esf_status init_state(PcrState* d, double eps, int maxIt, cudaStream_t st
 
 static esf_status batched_inner_solve(PressureWork* w, const GridDev& g, cudaStream_t st, PcrState* out);
 static bool batching_pays(PressureWork* w);
+static esf_status df_buffers(PressureWork* w, const GridDev& g);
+
+// x += e_hi + e_lo (exact in FP64, then rounded into x), e = 0: the
+// double-float correction of an ESF_MIXED_X64 run folded into the solution
+__global__ void __launch_bounds__(VT) fold_df(long long n, float2* e, double* x) {
+  for (long long i = blockIdx.x * (long long)VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT) {
+    const float2 v = e[i];
+    x[i] += (double)v.x + (double)v.y;
+    e[i] = make_float2(0.0f, 0.0f);
+  }
+}
 
 esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv64,
                           const double* diag64, const double* b, double* x, double eps, int maxIt,
@@ -1203,6 +1236,102 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
     status = ESF_ERR_NUMERIC;
   } else if (sqrt(resid2) < eps * bnorm) {
     conv = 1;
+  } else if (precision == ESF_MIXED_X64 && fused) {
+    // One FP32 Krylov run with its correction e and direction d in
+    // double-float (pcr_iteration_fused_x64). The run pauses for an
+    // FP64 check of ||b - A x|| whenever r.Ar has fallen by 0.1^2 since the
+    // last check, or by the ratio that predicts the tolerance if that is
+    // larger, or after kX64CheckEvery iterations; it then continues (q, d, x
+    // kept; e folded into x) from the checked residual until a check
+    // passes. The recursive
+    // FP32 residual drifts from b - A x by the rounding of q (2^-24 of each
+    // step), so it is replaced at every check; checking every 10x keeps that
+    // drift small against the residual it replaces (replacing a residual
+    // that drifted far stalls the run: the recomputed beta swamps the new
+    // direction with the old). `refinements` counts the checks.
+    constexpr int kX64CheckEvery = 1000;
+    {
+      esf_status e = df_buffers(w, g);
+      if (e) return e;
+    }
+    FusedKernels kx = kf;
+    kx.edf = w->edf;
+    kx.ddf = w->ddf;
+    const void* keyx[8] = {w->minv32, w->invd32, w->edf, w->ddf, tma, &w->fmaps,
+                           reinterpret_cast<const void*>(static_cast<uintptr_t>(fused_cz(g))), nullptr};
+    if (!w->graphsForX || memcmp(keyx, w->keyX, sizeof keyx) != 0) {
+      esf_status e = capture(w->capStream, kx, false, false, &w->gChunkX, &w->kChunkX);
+      if (e) return e;
+      memcpy(w->keyX, keyx, sizeof keyx);
+      w->graphsForX = true;
+    }
+    auto predicted = [&](double r2) {
+      double t = (r2 > 0) ? 0.5 * eps * bnorm / sqrt(r2) : 0.0;
+      t = t > 0.1 ? t : 0.1;
+      return t < 0.5 ? t : 0.5;
+    };
+    ESF_CUDA(cudaMemsetAsync(w->edf, 0, g.R * 8, st));
+    ESF_CUDA(cudaMemsetAsync(w->ddf, 0, g.R * 8, st));
+    ESF_CUDA(cudaMemsetAsync(w->Ap32, 0, g.R * 4, st));
+    ESF_CUDA(cudaMemsetAsync(w->s32, 0, g.R * 4, st));
+    PcrState h;
+    memset(&h, 0, sizeof h);
+    h.eps = predicted(resid2);
+    h.maxIt = maxIt;
+    h.setup = 1;
+    h.inner = 1;
+    h.cap = kX64CheckEvery;
+    ESF_CUDA(cudaMemcpyAsync(w->st32, &h, sizeof h, cudaMemcpyHostToDevice, st));
+    ESF_CUDA(cudaStreamSynchronize(st));
+    kx.iteration(st);  // set-up pass: s = A r, delta; d = r; e unchanged (alpha 0)
+    ESF_LAUNCH_CHECK();
+    for (;;) {
+      PcrState hi;
+      esf_status e = run_graph_solve(w->hst, w->ev, w->st32, nullptr, w->gChunkX, 0, w->kChunkX, maxIt,
+                                     st, &hi);
+      if (e) return e;
+      total = hi.iter;
+      if (hi.status) {
+        status = (esf_status)hi.status;
+        break;
+      }
+      // x += e; FP64 residual b - A x, written as (b - A x)/diag into the
+      // live r buffer (the recursive FP32 r drifts from it by the rounding
+      // of q, 2^-24 of each step); a rebase pass then recomputes t and the
+      // scalars from it, keeping q and d
+      ESF_COUNTED fold_df<<<vec_blocks(g.R), VT, 0, st>>>(g.R, reinterpret_cast<float2*>(w->edf), x);
+      ESF_LAUNCH_CHECK();
+      StencilArgs<double> a;
+      memset(&a, 0, sizeof a);
+      a.in = x; a.b = b; a.r = w->r; a.out32 = (hi.pp & 1) ? w->r32b : w->r32; a.invd = w->invd;
+      a.minv = minv64; a.partial = w->partial; a.st = w->st;
+      ESF_COUNTED pressure_stencil<double, S_RESID64><<<stencil_grid<double>(g), NT, 0, st>>>(g, a, stencil_cz(g));
+      ESF_LAUNCH_CHECK();
+      PcrState ho;
+      ESF_CUDA(cudaMemcpyAsync(&ho, w->st, sizeof ho, cudaMemcpyDeviceToHost, st));
+      ESF_CUDA(cudaStreamSynchronize(st));
+      resid2 = ho.resid2;
+      ref++;
+      rel = bnorm > 0 ? sqrt(resid2) / bnorm : sqrt(resid2);
+      if (!(resid2 == resid2)) {
+        status = ESF_ERR_NUMERIC;
+        break;
+      }
+      if (sqrt(resid2) < eps * bnorm) {
+        conv = 1;
+        break;
+      }
+      if (total >= maxIt) break;
+      hi.done = 0;
+      hi.converged = 0;
+      hi.rebase = 1;
+      hi.eps = predicted(resid2);
+      memset(hi.ticket, 0, sizeof hi.ticket);
+      ESF_CUDA(cudaMemcpyAsync(w->st32, &hi, sizeof hi, cudaMemcpyHostToDevice, st));
+      ESF_CUDA(cudaStreamSynchronize(st));
+      kx.iteration(st);  // rebase pass
+      ESF_LAUNCH_CHECK();
+    }
   } else {
     ESF_CUDA(cudaMemsetAsync(w->x32, 0, g.R * 4, st));
     {
@@ -1340,9 +1469,22 @@ static esf_status time_kernels_t(PressureWork* w, const GridDev& g, const T* min
 // The one-pass iteration timed on an inner solve of A e = b from e = 0 (the
 // set-up pass and one iteration untimed, then `reps` iterations; the
 // tolerance is 0, so every launch does a full iteration).
+static esf_status df_buffers(PressureWork* w, const GridDev& g) {
+  if (!w->edf) ESF_CUDA(cudaMalloc(&w->edf, g.R * 8));
+  if (!w->ddf) ESF_CUDA(cudaMalloc(&w->ddf, g.R * 8));
+  return ESF_OK;
+}
+
 static esf_status time_fused(PressureWork* w, const GridDev& g, int reps, double* ms,
-                             cudaStream_t st) {
+                             cudaStream_t st, bool x64) {
   const long long R = g.R;
+  // x64 (ESF_MIXED_X64): the double-float iteration on zeroed e and d
+  if (x64) {
+    esf_status e = df_buffers(w, g);
+    if (e) return e;
+    ESF_CUDA(cudaMemsetAsync(w->edf, 0, R * 8, st));
+    ESF_CUDA(cudaMemsetAsync(w->ddf, 0, R * 8, st));
+  }
   // r = b/diag in the first buffer set, x = d = q = 0
   ESF_COUNTED pcr_zero_start<float><<<vec_blocks(R), VT, 0, st>>>(R, w->b32, w->invd32, w->x32, w->r32,
                                                                w->d32, w->Ap32, w->partial, w->stT);
@@ -1354,7 +1496,11 @@ static esf_status time_fused(PressureWork* w, const GridDev& g, int reps, double
   h.inner = 1;
   ESF_CUDA(cudaMemcpyAsync(w->stT, &h, sizeof h, cudaMemcpyHostToDevice, st));
   ESF_CUDA(cudaStreamSynchronize(st));
-  const FusedKernels k = fused_kernels(w, g, w->stT);
+  FusedKernels k = fused_kernels(w, g, w->stT);
+  if (x64) {
+    k.edf = w->edf;
+    k.ddf = w->ddf;
+  }
   k.iteration(st);
   k.iteration(st);
   cudaEvent_t e0, e1;
@@ -1383,7 +1529,7 @@ esf_status pressure_time_kernels(PressureWork* w, const GridDev& g, const double
                                  cudaStream_t st) {
   (void)x;
   ESF_COUNTED inv_vec<<<vec_blocks(g.R), VT, 0, st>>>(g.R, diag64, w->invd, w->invd32);
-  if (precision == ESF_MIXED) {
+  if (precision == ESF_MIXED || precision == ESF_MIXED_X64) {
     if (!w->x32) return ESF_ERR_STATE;
     ESF_COUNTED convert_vec<double, float><<<vec_blocks(g.T), VT, 0, st>>>(g.T, minv64, w->minv32);
     ESF_COUNTED convert_vec<double, float><<<vec_blocks(g.R), VT, 0, st>>>(g.R, b, w->b32);
@@ -1394,7 +1540,7 @@ esf_status pressure_time_kernels(PressureWork* w, const GridDev& g, const double
     if (e) return e;
     if (path == P32_FUSED) {
       *axpy_ms = 0.0;
-      return time_fused(w, g, reps, update_ms, st);
+      return time_fused(w, g, reps, update_ms, st, precision == ESF_MIXED_X64);
     }
     return time_kernels_t<float>(w, g, w->minv32, w->invd32, w->b32, w->x32, w->r32, w->d32,
                                  w->Ap32, w->s32, reps, update_ms, axpy_ms, st, tma);

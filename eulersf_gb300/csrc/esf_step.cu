@@ -329,7 +329,7 @@ extern "C" esf_status esf_create(const esf_grid* g, const esf_params* p, void* s
     cudaMemsetAsync(s->jdiag, 0, R * 8, s->stream);
     cudaMemsetAsync(s->rhs, 0, R * 8, s->stream);
     cudaMemsetAsync(s->b1, 0, R * 8, s->stream);
-    e = pressure_work_alloc(&s->pw, G, p->precision == ESF_MIXED);
+    e = pressure_work_alloc(&s->pw, G, p->precision != ESF_FP64);
   }
   if (!e && cudaEventCreate(&s->e0) != cudaSuccess) e = ESF_ERR_CUDA;
   if (!e && cudaEventCreate(&s->e1) != cudaSuccess) e = ESF_ERR_CUDA;
@@ -998,7 +998,7 @@ static esf_status solid_system(esf_scene* sc, double* energyOut) {
     // mixed precision, elastic, one solid: record the matrix-free operator's
     // per-cell data (ESF_SOLID_ASSEMBLED=1 keeps the FP32 copy of the
     // assembled blocks, as scenes with several solids do)
-    const bool mf = sc->ns == 1 && nc > 0 && sc->p.precision == ESF_MIXED && !d->d.plastic &&
+    const bool mf = sc->ns == 1 && nc > 0 && sc->p.precision != ESF_FP64 && !d->d.plastic &&
                     !getenv("ESF_SOLID_ASSEMBLED");
     d->d.mf = nullptr;
     d->d.mfCells = 0;
@@ -1017,7 +1017,7 @@ static esf_status solid_system(esf_scene* sc, double* energyOut) {
       d->d.updIdx = d->fpUpd.as<int>();
       d->d.updVal = d->fpVal.as<double>();
     }
-    if (nc > 0 && sc->p.precision == ESF_MIXED && !d->d.plastic) {
+    if (nc > 0 && sc->p.precision != ESF_FP64 && !d->d.plastic) {
       // stress and stiffness in FP32; near-degenerate cells again in FP64
       TRY(sc->fbCells.ensure(nc * 8));
       TRY(sc->fbSlot.ensure(nc * 8));
@@ -1198,7 +1198,7 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
   if (!sc->sw || solid_work_capacity(sc->sw) < S) {
     solid_work_free(sc->sw);
     sc->sw = nullptr;
-    TRY(solid_work_alloc(&sc->sw, S + S / 4 + 16, prec == ESF_MIXED));
+    TRY(solid_work_alloc(&sc->sw, S + S / 4 + 16, prec != ESF_FP64));
   }
   TRY(solid_work_set_matrix_free(sc->sw, G, sc->mfCells, sc->mfCells ? sc->mfCell.as<float>() : nullptr,
                                  sc->mfCorner.as<int>(), sc->sNode.as<long long>(), sc->cellOrd,
@@ -1414,7 +1414,7 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
   ESF_CUDA(cudaEventRecord(sc->ph[12], st));
   // fluid velocity and intensity: FP32 arithmetic in mixed precision (the
   // solid's material coordinates, which decide its cell flags, stay FP64)
-  if (prec == ESF_MIXED) {
+  if (prec != ESF_FP64) {
     ESF_COUNTED k_advect_velocity_f32<<<kblocks(G.T), KT, 0, st>>>(G, sc->solidMass, sc->vel, sc->vws, dt);
     std::swap(sc->vel, sc->vws);
     ESF_COUNTED k_advect_scalar_f32<<<kblocks(G.T), KT, 0, st>>>(G, sc->solidMass, sc->vel, sc->intensity, sc->ws, dt);
@@ -1445,7 +1445,7 @@ extern "C" esf_status esf_step(esf_scene* sc, esf_step_report* rep) {
     rep->fp64_iterations = it64;
     int fb = 0;
     for (int i = 0; i < sc->ns; i++) fb += sc->hInts[kFallbackCount + i];
-    rep->fp64_stress_cells = prec == ESF_MIXED ? fb : (int)sc->validCells;
+    rep->fp64_stress_cells = prec != ESF_FP64 ? fb : (int)sc->validCells;
     rep->valid_cells = (int)sc->validCells;
     unsigned long long contacts = 0;
     ESF_CUDA(cudaMemcpy(&contacts, sc->contactCount.p, 8, cudaMemcpyDeviceToHost));
@@ -1662,13 +1662,13 @@ extern "C" esf_status esf_pressure_solve(const esf_grid* g, const double* minv, 
                                          const double* b, double* x, double eps, int maxIt,
                                          int precision, int* iters, double* relres, void* stream) {
   if (!g || !minv || !diag || !b || !x || g->xRes < 3 || g->yRes < 3 || g->zRes < 3 || maxIt < 0 ||
-      (precision != ESF_FP64 && precision != ESF_MIXED)) {
+      (precision != ESF_FP64 && precision != ESF_MIXED && precision != ESF_MIXED_X64)) {
     set_error("esf_pressure_solve: invalid argument");
     return ESF_ERR_INVALID_ARG;
   }
   GridDev G = grid_dev(g);
   PressureWork* w = nullptr;
-  TRY(pressure_work_alloc(&w, G, precision == ESF_MIXED));
+  TRY(pressure_work_alloc(&w, G, precision != ESF_FP64));
   int it = 0, rf = 0, cv = 0;
   double rr = 0;
   esf_status e = pressure_solve(w, G, minv, diag, b, x, eps, maxIt, precision, 1e-4, 50, &it, &rr, &rf,
@@ -1695,7 +1695,7 @@ extern "C" esf_status esf_pressure_solve_batch(int n, const esf_grid* grids, con
                                                int autotune, int* iters, double* relres,
                                                esf_batch_stats* stats, void* stream) {
   if (n < 1 || !grids || !minv || !diag || !b || !x || maxIt < 0 ||
-      (precision != ESF_FP64 && precision != ESF_MIXED)) {
+      (precision != ESF_FP64 && precision != ESF_MIXED && precision != ESF_MIXED_X64)) {
     set_error("esf_pressure_solve_batch: invalid argument");
     return ESF_ERR_INVALID_ARG;
   }
@@ -1727,7 +1727,7 @@ extern "C" esf_status esf_pressure_solve_batch(int n, const esf_grid* grids, con
       e = ESF_ERR_CUDA;
       break;
     }
-    e = pressure_work_alloc(&works[i], grid_dev(&grids[i]), precision == ESF_MIXED);
+    e = pressure_work_alloc(&works[i], grid_dev(&grids[i]), precision != ESF_FP64);
     if (!e && batcher) e = pressure_work_set_batcher(works[i], batcher);
   }
   if (!e) {

@@ -8,7 +8,11 @@ prints one JSON line per substep. With "save data = true" it writes each
 frame's files under "data path" (main.cpp:198-199); a "start frame" above 0
 resumes from the previous frame's files (main.cpp:95).
 
-    python -m eulersf_gb300.driver scene.cfg [frames] [--mixed]
+    python -m eulersf_gb300.driver scene.cfg [frames] [--mixed | --mixed-x64]
+
+--mixed: FP32 inner solves in FP64 iterative refinement; --mixed-x64: one
+FP32 Krylov run per pressure solve with its iterate and direction in FP64
+(ESF_MIXED_X64). Without either, the plain FP64 method.
 """
 from __future__ import annotations
 
@@ -117,13 +121,14 @@ def run(cfg_path, frames=None, precision=abi.ESF_FP64, out=sys.stdout):
 
 def main(argv=None):
     argv = list(sys.argv[1:] if argv is None else argv)
-    mixed = "--mixed" in argv
-    argv = [a for a in argv if a != "--mixed"]
+    prec = (abi.ESF_MIXED_X64 if "--mixed-x64" in argv else
+            abi.ESF_MIXED if "--mixed" in argv else abi.ESF_FP64)
+    argv = [a for a in argv if a not in ("--mixed", "--mixed-x64")]
     if not argv:
         print(__doc__)
         return 2
     frames = int(argv[1]) if len(argv) > 1 else None
-    run(argv[0], frames, abi.ESF_MIXED if mixed else abi.ESF_FP64)
+    run(argv[0], frames, prec)
     return 0
 
 

@@ -5,7 +5,7 @@ iterations per second ("CG iters/s") on a pressure system of the rubber-ball
 scene's size, device-resident inputs, timed with CUDA events on the stream
 the solve runs on.
 
-    python -m eulersf_gb300.solver_bench [--size 256] [--precision mixed|fp64]
+    python -m eulersf_gb300.solver_bench [--size 256] [--precision mixed|mixed-x64|fp64]
                                          [--iters 300] [--repeat 3] [--batch B [--autotune]]
 
 The tolerance is set to 1e-30 so every solve runs exactly --iters
@@ -39,7 +39,7 @@ def run(size=256, precision="mixed", iters=300, repeat=3, seed=0):
     dm, dd, db = dev(minv), dev(diag), dev(b)
     dx = torch.zeros_like(db)
     g = abi.Grid(desc.res, desc.res, desc.res, desc.dh, (C.c_double * 3)(0, 0, 0))
-    prec = abi.ESF_MIXED if precision == "mixed" else abi.ESF_FP64
+    prec = {"mixed": abi.ESF_MIXED, "mixed-x64": abi.ESF_MIXED_X64}.get(precision, abi.ESF_FP64)
     stream = torch.cuda.current_stream()
     it, rr = C.c_int(), C.c_double()
     p = lambda t: C.c_void_p(t.data_ptr())
@@ -139,7 +139,7 @@ def run_batch(size=32, batch=256, iters=300, repeat=2, autotune=False):
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--size", type=int, default=256)
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed-x64", "fp64"])
     ap.add_argument("--iters", type=int, default=300)
     ap.add_argument("--repeat", type=int, default=3)
     ap.add_argument("--batch", type=int, default=1)
