@@ -198,6 +198,8 @@ extern "C" size_t esf_scene_footprint(const esf_grid* g, const esf_params* p, in
   // (estimate / measured = 1.07, 1.00, 0.99 for a 0.2-radius ball), plus
   // the one-pass FP32 iteration's second set of r, t, q (12 bytes a row)
   double bytes = T * (520.0 + 240.0 * ns) + R * 192.0;
+  // ESF_MIXED_X64: the double-float correction and direction (8 bytes each a row)
+  if (p->precision == ESF_MIXED_X64) bytes += R * 16.0;
   // scenes with several solids: each further solid's cell -> valid-cell map,
   // and every solid's rest-SDF lattice with its triangle lists (~21 MB for
   // the shipped sphere's volume)
