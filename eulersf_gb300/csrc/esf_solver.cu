@@ -1238,17 +1238,17 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
     conv = 1;
   } else if (precision == ESF_MIXED_X64 && fused) {
     // One FP32 Krylov run with its correction e and direction d in
-    // double-float (pcr_iteration_fused_x64). The run pauses for an
-    // FP64 check of ||b - A x|| whenever r.Ar has fallen by 0.1^2 since the
-    // last check, or by the ratio that predicts the tolerance if that is
-    // larger, or after kX64CheckEvery iterations; it then continues (q, d, x
-    // kept; e folded into x) from the checked residual until a check
-    // passes. The recursive
-    // FP32 residual drifts from b - A x by the rounding of q (2^-24 of each
-    // step), so it is replaced at every check; checking every 10x keeps that
-    // drift small against the residual it replaces (replacing a residual
-    // that drifted far stalls the run: the recomputed beta swamps the new
-    // direction with the old). `refinements` counts the checks.
+    // double-float (pcr_iteration_fused_x64). The run pauses for an FP64
+    // check of ||b - A x|| whenever r.Ar has fallen by 0.1^2 since the last
+    // check, or by the ratio that predicts the tolerance if that is larger,
+    // or after kX64CheckEvery iterations; it then continues from the checked
+    // residual (q and d kept, e folded into x) until a check passes. The
+    // recursive FP32 residual drifts from b - A x by the rounding of q
+    // (2^-24 of each step), so it is replaced at every check; checking every
+    // 10x keeps that drift small against the residual it replaces
+    // (replacing a residual that drifted far stalls the run: the recomputed
+    // beta swamps the new direction with the old). `refinements` counts the
+    // checks.
     constexpr int kX64CheckEvery = 1000;
     {
       esf_status e = df_buffers(w, g);
@@ -1466,14 +1466,17 @@ static esf_status time_kernels_t(PressureWork* w, const GridDev& g, const T* min
   return ESF_OK;
 }
 
-// The one-pass iteration timed on an inner solve of A e = b from e = 0 (the
-// set-up pass and one iteration untimed, then `reps` iterations; the
-// tolerance is 0, so every launch does a full iteration).
+// The double-float correction and direction of ESF_MIXED_X64 (8 bytes a
+// row each), allocated on first use.
 static esf_status df_buffers(PressureWork* w, const GridDev& g) {
   if (!w->edf) ESF_CUDA(cudaMalloc(&w->edf, g.R * 8));
   if (!w->ddf) ESF_CUDA(cudaMalloc(&w->ddf, g.R * 8));
   return ESF_OK;
 }
+
+// The one-pass iteration timed on an inner solve of A e = b from e = 0 (the
+// set-up pass and one iteration untimed, then `reps` iterations; the
+// tolerance is 0, so every launch does a full iteration).
 
 static esf_status time_fused(PressureWork* w, const GridDev& g, int reps, double* ms,
                              cudaStream_t st, bool x64) {
