@@ -79,8 +79,8 @@ def test_pressure_solve_matches_oracle(precision, gpu_lib):
         assert abs(it.value - itr) <= 5
         assert rel_err(x, xr) <= 1e-5
     elif precision == 2:
-        # ESF_MIXED_X64: one FP32 Krylov run with an FP64 iterate and
-        # direction needs about the FP64 iteration count
+        # ESF_MIXED_X64: one FP32 Krylov run with a double-float correction
+        # and direction needs about the FP64 iteration count
         assert it.value <= 1.15 * itr + 100, (it.value, itr)
         assert rel_err(x, xr) <= 1e-3
     else:
@@ -109,8 +109,9 @@ def test_mixed_step_close_to_fp64(gpu_lib):
 
 
 def test_mixed_x64_step_close_to_fp64(gpu_lib):
-    """ESF_MIXED_X64 (the pressure solve's iterate and direction in FP64,
-    one FP32 Krylov run per solve) reaches the same 1e-8 FP64 residual in
+    """ESF_MIXED_X64 (the pressure solve's correction and direction in
+    double-float, one FP32 Krylov run per solve) reaches the same 1e-8 FP64
+    residual in
     about the FP64 path's pressure iterations; fields agree with the FP64
     step as closely as the refinement's do (same bounds as
     test_mixed_step_close_to_fp64), and the maps are the same."""

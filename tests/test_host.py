@@ -131,6 +131,32 @@ def test_server_without_gpu_and_footprint_model(lib):
         q, keep = request_for(SceneDesc(N=n), 1)
         sizes.append(lib.esf_scene_footprint(C.byref(q.grid), C.byref(q.params), q.num_solids, q.solids))
     assert 0 < sizes[0] < sizes[1] and sizes[1] > 2 * sizes[0]
+    # ESF_MIXED_X64 adds its double-float correction and direction, 16 bytes a
+    # pressure row (with the estimate's 10% margin)
+    desc = SceneDesc(N=64)
+    q1, k1 = request_for(desc, 1, abi.ESF_MIXED)
+    q2, k2 = request_for(desc, 1, abi.ESF_MIXED_X64)
+    f1 = lib.esf_scene_footprint(C.byref(q1.grid), C.byref(q1.params), q1.num_solids, q1.solids)
+    f2 = lib.esf_scene_footprint(C.byref(q2.grid), C.byref(q2.params), q2.num_solids, q2.solids)
+    assert abs((f2 - f1) - 16 * 64 ** 3 * 1.1) <= 2
+
+
+def test_precision_values_and_config_key(lib, tmp_path):
+    """abi.py's precision constants are the header's, and the cfg key
+    "precision" selects each of them (a GB300 addition to the reference's
+    keys)."""
+    import re
+    hdr = open(os.path.join(ROOT, "include", "eulersf.h")).read()
+    vals = {m.group(1): int(m.group(2)) for m in re.finditer(r"\b(ESF_FP64|ESF_MIXED|ESF_MIXED_X64)\s*=\s*(\d+)", hdr)}
+    assert vals == {"ESF_FP64": abi.ESF_FP64, "ESF_MIXED": abi.ESF_MIXED, "ESF_MIXED_X64": abi.ESF_MIXED_X64}
+    cfg = scene.write_scene(scene.SceneDesc(N=16), str(tmp_path / "s"))
+    base = open(cfg).read()
+    for word, want in (("fp64", abi.ESF_FP64), ("mixed", abi.ESF_MIXED), ("mixed x64", abi.ESF_MIXED_X64)):
+        with open(cfg, "w") as f:
+            f.write(base + f"\nprecision = {word}\n")
+        g, p = abi.Grid(), abi.Params()
+        assert lib.esf_parse_config(cfg.encode(), C.byref(g), C.byref(p), None, None, 0, None, 0) == 0
+        assert p.precision == want, word
 
 
 def _free_port():
