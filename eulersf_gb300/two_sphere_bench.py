@@ -13,6 +13,7 @@ device time per launch as a fraction of the measured HBM copy bandwidth
 
     python -m eulersf_gb300.two_sphere_bench [--size 384] [--steps 10] [--seed 7]
     python -m eulersf_gb300.two_sphere_bench --collide      # the same balls, touching and approaching
+    python -m eulersf_gb300.two_sphere_bench --precision mixed-x64   # ESF_MIXED_X64 pressure solves
 
 --collide places the two balls side by side at (0.38, 0.7, 0.5) and
 (0.62, 0.7, 0.5), 0.24 apart centre to centre, moving towards each other at
@@ -50,10 +51,11 @@ def hbm_peak():
     return 6800.0, "fallback"
 
 
-def run(size=384, steps=10, seed=7, out=print, collide=False):
+def run(size=384, steps=10, seed=7, out=print, collide=False, precision="mixed"):
     desc = scene(size, seed, collide)
+    prec = abi.ESF_MIXED_X64 if precision == "mixed-x64" else abi.ESF_MIXED
     t0 = time.perf_counter()
-    I = make_scene(desc, precision=abi.ESF_MIXED)
+    I = make_scene(desc, precision=prec)
     setup_s = time.perf_counter() - t0
     rows = []
     for k in range(steps):
@@ -75,10 +77,11 @@ def run(size=384, steps=10, seed=7, out=print, collide=False):
     piters = sum(r["iterations"][1] for r in rows)
     peak, kind = hbm_peak()
     words = 17  # per row of a whole iteration but its residual check, 4-byte words
+    moved = 16 if prec == abi.ESF_MIXED_X64 else 12  # the words the one-pass kernel moves
     achieved = words * 4 * R / (upd.value * 1e-3) / 1e9 if st == 0 and upd.value > 0 else None
     summary = {"summary": True, "scene": "two spheres, radius 0.12, fluid height 0.3"
                + (", touching and approaching" if collide else ""), "size": size,
-               "steps": steps, "seed": seed, "precision": "mixed", "setup_s": setup_s,
+               "steps": steps, "seed": seed, "precision": precision, "setup_s": setup_s,
                "steps_per_s": steps / t, "cells_per_s": R * steps / t,
                "pressure_iters_per_s": piters / t, "pressure_iters_per_step": piters / steps,
                "max_rel_residual": max(max(r["rel_residual"]) for r in rows),
@@ -88,6 +91,8 @@ def run(size=384, steps=10, seed=7, out=print, collide=False):
                "pressure_kernel_us": upd.value * 1e3 if st == 0 else None,
                "pressure_kernel_gbs": achieved, "hbm_peak_gbs": peak, "peak_kind": kind,
                "hbm_frac": achieved / peak if achieved else None,
+               "moved_words": moved,
+               "frac_of_moved": (moved * 4 * R / (upd.value * 1e-3) / 1e9 / peak) if achieved else None,
                "note": "hbm_frac: the one-pass pressure iteration's 17 four-byte words per row "
                        "over its CUDA-event time per launch, against the measured copy bandwidth"}
     out(json.dumps(summary))
@@ -100,8 +105,9 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--collide", action="store_true", help="balls touching and approaching")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed-x64"])
     a = ap.parse_args(argv)
-    run(a.size, a.steps, a.seed, collide=a.collide)
+    run(a.size, a.steps, a.seed, collide=a.collide, precision=a.precision)
     return 0
 
 
