@@ -5,8 +5,11 @@ residuals, and the L-inf differences of velocity, pressure (lambda1) and
 solid displacement between the two trajectories, relative to the FP64
 field's max-norm.
 
-    python -m eulersf_gb300.precision_report [--size 256] [--steps 6] [--seed 7]
+    python -m eulersf_gb300.precision_report [--size 256] [--steps 6] [--seed 7] [--x64]
     python -m eulersf_gb300.precision_report --fp64-only --size 128 --steps 50 --seed 0
+
+--x64 steps a third integrator at ESF_MIXED_X64 (one FP32 pressure run per
+solve with a double-float correction and direction) beside the two.
 
 Prints one JSON line per step and a summary line.
 """
@@ -58,13 +61,14 @@ def run_fp64(size=128, steps=50, seed=0, mass_sample_dh=None, out=print):
     return rows, summary
 
 
-def run(size=256, steps=6, seed=7, out=print):
+def run(size=256, steps=6, seed=7, out=print, x64=False):
     desc = SceneDesc(N=size, noise_seed=seed,
                      solids=[SolidDesc(center=(0.5, 0.65, 0.5), radius=0.15, density=1100.0,
                                        E=2e5, nu=0.45)])
     A = make_scene(desc, precision=abi.ESF_FP64)
     B = make_scene(desc, precision=abi.ESF_MIXED)
-    ta = tb = 0.0
+    X = make_scene(desc, precision=abi.ESF_MIXED_X64) if x64 else None
+    ta = tb = tx = 0.0
     rows = []
     for k in range(steps):
         ra, rb = A.stepImplicit(), B.stepImplicit()
@@ -79,6 +83,14 @@ def run(size=256, steps=6, seed=7, out=print):
                "linf_pressure": _linf(B.get("lambda1"), A.get("lambda1")),
                "linf_solid_displacement": _linf(B.get("solid.u"), A.get("solid.u")),
                "dt": [ra["dt"], rb["dt"]]}
+        if X is not None:
+            rx = X.stepImplicit()
+            tx += rx["device_ms"]
+            row.update({"x64_ms": rx["device_ms"], "x64_iterations": rx["iterations"],
+                        "x64_checks": rx["refinements"][1], "x64_rel_residual": rx["rel_residual"],
+                        "x64_converged": rx["converged"],
+                        "x64_linf_velocity": _linf(X.get("velocity"), A.get("velocity")),
+                        "x64_linf_pressure": _linf(X.get("lambda1"), A.get("lambda1"))})
         rows.append(row)
         out(json.dumps(row))
     summary = {"summary": True, "size": size, "steps": steps, "seed": seed,
@@ -87,6 +99,12 @@ def run(size=256, steps=6, seed=7, out=print):
                "max_linf_velocity": max(r["linf_velocity"] for r in rows),
                "max_linf_pressure": max(r["linf_pressure"] for r in rows),
                "max_mixed_rel_residual": max(max(r["mixed_rel_residual"]) for r in rows)}
+    if X is not None:
+        summary.update({"x64_steps_per_s": steps / (tx * 1e-3), "x64_speedup": ta / tx if tx > 0 else None,
+                        "x64_max_linf_velocity": max(r["x64_linf_velocity"] for r in rows),
+                        "x64_max_linf_pressure": max(r["x64_linf_pressure"] for r in rows),
+                        "x64_max_rel_residual": max(max(r["x64_rel_residual"]) for r in rows)})
+        X.close()
     out(json.dumps(summary))
     A.close()
     B.close()
@@ -100,11 +118,12 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--fp64-only", action="store_true", help="the plain FP64 path alone")
     ap.add_argument("--mass-sample-dh", type=float, default=None)
+    ap.add_argument("--x64", action="store_true", help="also step an ESF_MIXED_X64 integrator")
     a = ap.parse_args(argv)
     if a.fp64_only:
         run_fp64(a.size, a.steps, a.seed, a.mass_sample_dh)
     else:
-        run(a.size, a.steps, a.seed)
+        run(a.size, a.steps, a.seed, x64=a.x64)
     return 0
 
 
