@@ -47,10 +47,11 @@ typedef enum esf_precision {
    * (double-float FP32 pairs; operator, residual vectors and stencil in
    * FP32; dot products, alpha/beta and periodic ||b - A x|| checks, into
    * which the correction is folded, in FP64), continued to the FP64
-   * tolerance without restarts: about the FP64 solver's iteration count
-   * instead of the refinement's 1.2-2.5x of it, for 16 instead of 12 words
-   * moved per row and iteration. Grids whose cell rows are not a multiple of
-   * 4 cells solve as ESF_MIXED. No reference counterpart. */
+   * tolerance without restarts: about the FP64 solver's iteration count,
+   * where the refinement takes 1.3x of it on average (0.4-3.4x per step on
+   * a 256^3 scene), for 16 instead of 12 words moved per row and iteration.
+   * Grids whose cell rows are not a multiple of 4 cells solve as ESF_MIXED.
+   * No reference counterpart. */
   ESF_MIXED_X64 = 2
 } esf_precision;
 
