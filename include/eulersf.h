@@ -124,7 +124,8 @@ typedef struct esf_step_report {
   int iterations[3];          /* solid solve 1, pressure solve, solid solve 2 */
   int converged[3];
   double rel_residual[3];     /* ||Ax-b|| / ||b|| at exit */
-  int refinements[3];         /* mixed: outer FP64 refinement steps per solve */
+  int refinements[3];         /* mixed: outer FP64 refinement steps per solve
+                                 (ESF_MIXED_X64 pressure solve: its FP64 checks) */
   int fp64_iterations;        /* mixed: FP64 PCR iterations that finished the pressure solve */
   int prone_to_contact;       /* CFL factor 0.6 instead of 1.8 */
   int num_particles;
