@@ -1317,7 +1317,7 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
         status = ESF_ERR_NUMERIC;
         break;
       }
-      if (sqrt(resid2) < eps * bnorm) {
+      if (sqrt(resid2) < eps * bnorm || resid2 == 0.0) {  // (exact: b = 0 meets no relative test)
         conv = 1;
         break;
       }

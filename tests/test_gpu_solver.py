@@ -108,6 +108,25 @@ def test_mixed_step_close_to_fp64(gpu_lib):
         assert np.array_equal(B.get("gridIdxToSolidIdx"), A.get("gridIdxToSolidIdx"))
 
 
+def test_mixed_x64_zero_right_hand_side_stops_at_once(gpu_lib):
+    """b = 0 from x = 0: the exact answer is already there. The relative test
+    ||b - A x|| < eps ||b|| cannot pass with ||b|| = 0, so the run must stop on
+    the exact zero residual instead of checking until max_iterations."""
+    import torch
+    X = 25
+    rng = np.random.default_rng(3)
+    g = oracle.grid(X, 0.04)
+    minv = rng.uniform(50.0, 300.0, X ** 3)
+    dm, dd = _dev(minv), _dev(_jacobi_diag(X, X, X, minv))
+    db, dx = _dev(np.zeros((X - 1) ** 3)), _dev(np.zeros((X - 1) ** 3))
+    it, rr = C.c_int(), C.c_double()
+    s = gpu_lib.esf_pressure_solve(C.byref(g), _ptr(dm), _ptr(dd), _ptr(db), _ptr(dx), 1e-8, 20000, 2,
+                                   C.byref(it), C.byref(rr), None)
+    torch.cuda.synchronize()
+    assert s == 0 and rr.value == 0.0 and it.value <= 2, (s, it.value, rr.value)
+    assert not dx.cpu().numpy().any()
+
+
 def test_mixed_x64_step_close_to_fp64(gpu_lib):
     """ESF_MIXED_X64 (the pressure solve's correction and direction in
     double-float, one FP32 Krylov run per solve) reaches the same 1e-8 FP64
