@@ -1155,9 +1155,10 @@ esf_status pressure_solve(PressureWork* w, const GridDev& g, const double* minv6
   // slow modes of this operator need long Krylov runs. If the refinements run
   // out before the tolerance is met, FP64 PCR finishes from the refined x.
   // Each inner solve restarts its Krylov space: carrying the direction across
-  // the FP64 residual replacement stalls near 1e-7, because FP32 rounding
-  // feeds the operator's near-null checkerboard modes (J J^T on the
-  // node-collocated grid).
+  // the FP64 residual replacement stalls near 1e-7 while the iterate and
+  // direction are FP32, whose rounding reaches the residual amplified by the
+  // operator's conditioning (ESF_MIXED_X64, above, carries it with both in
+  // double-float).
   ESF_COUNTED convert_vec<double, float><<<vec_blocks(g.T), VT, 0, st>>>(g.T, minv64, w->minv32);
   const TmaMaps* tma = nullptr;
   int path = P32_REGISTER;
