@@ -242,11 +242,13 @@ def test_one_pass_iteration_matches_two_kernel_split(shape, gpu_lib, monkeypatch
 
 
 
-def test_batched_solve_equals_single_solves(gpu_lib):
+@pytest.mark.parametrize("precision", [1, 2])
+def test_batched_solve_equals_single_solves(precision, gpu_lib):
     """esf_pressure_solve_batch on systems of two grid shapes (24^3 and 32^3
-    cells, mixed precision; systems of one shape share launches): each
-    answer, iteration count and residual is the same as esf_pressure_solve's
-    on that system alone, bit for bit."""
+    cells; ESF_MIXED: the inner solves of systems of one shape share
+    launches; ESF_MIXED_X64: each system runs its own double-float run):
+    each answer, iteration count and residual is the same as
+    esf_pressure_solve's on that system alone, bit for bit."""
     import torch
     systems = []
     for X, seed in ((25, 1), (33, 2), (25, 3), (33, 4), (25, 5)):
@@ -265,17 +267,18 @@ def test_batched_solve_equals_single_solves(gpu_lib):
     its, rr = (C.c_int * n)(), (C.c_double * n)()
     from eulersf_gb300.serve import BatchStats
     stats = BatchStats()
-    st = gpu_lib.esf_pressure_solve_batch(n, grids, arr(dm), arr(dd), arr(db), arr(dx), 1e-8, 20000, 1, 0,
-                                          its, rr, C.byref(stats), None)
+    st = gpu_lib.esf_pressure_solve_batch(n, grids, arr(dm), arr(dd), arr(db), arr(dx), 1e-8, 20000,
+                                          precision, 0, its, rr, C.byref(stats), None)
     torch.cuda.synchronize()
     assert st == 0, gpu_lib.esf_last_error()
-    # both shapes have several systems: their inner solves shared launches
-    assert stats.inner_solves > 0 and stats.max_tasks >= 2, stats.as_dict()
+    if precision == 1:
+        # both shapes have several systems: their inner solves shared launches
+        assert stats.inner_solves > 0 and stats.max_tasks >= 2, stats.as_dict()
     for i, (g, minv, diag, b, x0) in enumerate(systems):
         sx = _dev(x0)
         it, r1 = C.c_int(), C.c_double()
         assert gpu_lib.esf_pressure_solve(C.byref(g), _ptr(dm[i]), _ptr(dd[i]), _ptr(db[i]), _ptr(sx), 1e-8,
-                                          20000, 1, C.byref(it), C.byref(r1), None) == 0
+                                          20000, precision, C.byref(it), C.byref(r1), None) == 0
         torch.cuda.synchronize()
         assert its[i] == it.value and rr[i] == r1.value and rr[i] < 1e-8
         assert torch.equal(dx[i], sx), i
